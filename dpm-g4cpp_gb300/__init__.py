@@ -1,0 +1,399 @@
+"""GB300-native dpm_Simulate: Python host layer over libdpmx.so (include/dpmx.h).
+
+The names mirror the reference's simulation-phase interface:
+
+  Tables(data_dir)            SimElectronData/SimPhotonData/SimMaterialData::Load
+                              (dpm_Simulate.cc:71-78): the 14 data files
+  Phantom.slab(t, geom, lbox) Geom(lbox, matData, geomIndex) (Geom.cc:9-17)
+  Phantom.voxels(t, mat, v)   a 3-D voxel phantom behind the same Geom interface
+  simulate(...)               Simulate(nprimary, eprimary, isElectron, lbox, ...,
+                              geomIndex, filename) (SimDPMLike.cc:40-251)
+  write_hist(...)             Geom::Write (Geom.cc:167-192), hist.sim
+  run(t, jobs, ...)           many Simulate-like jobs batched in one run
+
+Errors raise DpmxError carrying the library's status code and message, the
+counterpart of the reference's `exit(EXIT_FAILURE)` with a stderr message. All
+transport runs on the GPU; importing the package without the built library
+raises at the first call.
+"""
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libdpmx.so")
+
+FP64_PLAIN = 0
+FP32_EVENT = 1
+
+OK, ERR_FILE, ERR_PARSE, ERR_CUDA, ERR_ARG, ERR_OVERFLOW, ERR_NOMEM = 0, -1, -2, -3, -4, -5, -6
+
+
+class DpmxError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("dpmx error %d: %s" % (code, msg))
+        self.code = code
+
+
+class _Source(C.Structure):
+    _fields_ = [("particle", C.c_int), ("spectrum", C.c_int), ("e0", C.c_double), ("e1", C.c_double),
+                ("shape", C.c_int), ("cx", C.c_double), ("cy", C.c_double), ("fx", C.c_double),
+                ("fy", C.c_double), ("nbx", C.c_int), ("nby", C.c_int)]
+
+
+class _Job(C.Structure):
+    _fields_ = [("phantom", C.c_void_p), ("source", _Source), ("histories", C.c_longlong), ("seed", C.c_uint64)]
+
+
+class _Opts(C.Structure):
+    _fields_ = [("precision", C.c_int), ("batches", C.c_int), ("block_size", C.c_int), ("blocks_per_sm", C.c_int),
+                ("chunk_histories", C.c_longlong), ("tally_aggregate", C.c_int), ("use_graph", C.c_int),
+                ("tag_beamlets", C.c_int), ("autotune", C.c_int), ("stream", C.c_void_p)]
+
+
+class _Stats(C.Structure):
+    _fields_ = [("edep", C.c_double), ("escaped", C.c_double), ("primary_energy", C.c_double),
+                ("max_residual", C.c_double), ("residual_violations", C.c_longlong), ("lost", C.c_longlong),
+                ("steps", C.c_longlong), ("histories", C.c_longlong)]
+
+
+_lib = None
+_dp = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+
+
+def library():
+    """Loads libdpmx.so (built in place by build.py); raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise DpmxError(ERR_FILE, "native library %s not built (run build())" % LIB_PATH)
+    L = C.CDLL(LIB_PATH)
+    P = C.c_void_p
+    sig = {
+        "dpmx_last_error": (C.c_char_p, []),
+        "dpmx_version": (C.c_char_p, []),
+        "dpmx_tables_load": (C.c_int, [C.c_char_p, C.POINTER(P)]),
+        "dpmx_tables_free": (None, [P]),
+        "dpmx_tables_num_materials": (C.c_int, [P]),
+        "dpmx_tables_param": (C.c_double, [P, C.c_int]),
+        "dpmx_tables_density": (C.c_double, [P, C.c_int]),
+        "dpmx_tables_material_name": (C.c_int, [P, C.c_int, C.c_char_p, C.c_int]),
+        "dpmx_phantom_slab": (C.c_int, [P, C.c_int, C.c_double, C.POINTER(P)]),
+        "dpmx_phantom_voxels": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                          np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS"), C.POINTER(P)]),
+        "dpmx_phantom_free": (None, [P]),
+        "dpmx_phantom_tally_size": (C.c_longlong, [P]),
+        "dpmx_run_options_default": (None, [C.POINTER(_Opts)]),
+        "dpmx_run": (C.c_int, [P, C.POINTER(_Job), C.c_int, C.POINTER(_Opts), C.POINTER(P)]),
+        "dpmx_result_tally": (C.c_int, [P, C.c_int, P, P, P]),
+        "dpmx_result_tally_device": (C.c_void_p, [P, C.c_int]),
+        "dpmx_result_stats": (C.c_int, [P, C.c_int, C.POINTER(_Stats)]),
+        "dpmx_result_elapsed_ms": (C.c_double, [P]),
+        "dpmx_result_launches": (C.c_longlong, [P]),
+        "dpmx_result_config": (C.c_int, [P, C.POINTER(C.c_longlong)]),
+        "dpmx_result_free": (None, [P]),
+        "dpmx_simulate": (C.c_int, [P, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int, C.c_uint64, C.c_int,
+                                    _dp, _dp, C.c_int, C.POINTER(C.c_int)]),
+        "dpmx_write_hist": (C.c_int, [P, C.c_char_p, C.c_int, C.c_double, C.c_int, _dp, _dp, C.c_int]),
+        "dpmx_sampler_eval": (C.c_int, [P, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, C.c_int]),
+        "dpmx_table_eval": (C.c_int, [P, C.c_int, C.c_int, C.c_int, _dp, _dp, C.c_int]),
+        "dpmx_simulate_histories": (C.c_int, [P, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int, C.c_uint64,
+                                              _dp, _dp, C.c_int]),
+        "dpmx_influence_build": (C.c_int, [P, C.c_int, C.c_double, C.POINTER(P)]),
+        "dpmx_csr_shape": (C.c_int, [P, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
+        "dpmx_csr_device": (C.c_int, [P, C.POINTER(P), C.POINTER(P), C.POINTER(P)]),
+        "dpmx_csr_spmv": (C.c_int, [P, C.c_void_p, C.c_void_p, C.c_void_p]),
+        "dpmx_csr_spmv_t": (C.c_int, [P, C.c_void_p, C.c_void_p, C.c_void_p]),
+        "dpmx_csr_download": (C.c_int, [P, C.c_void_p, C.c_void_p, C.c_void_p]),
+        "dpmx_csr_free": (None, [P]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != OK:
+        raise DpmxError(rc, library().dpmx_last_error().decode())
+
+
+def exported_symbols():
+    """Names the C ABI exports (declared in include/dpmx.h)."""
+    return ["dpmx_last_error", "dpmx_version", "dpmx_tables_load", "dpmx_tables_free", "dpmx_tables_num_materials",
+            "dpmx_tables_param", "dpmx_tables_density", "dpmx_tables_material_name", "dpmx_phantom_slab",
+            "dpmx_phantom_voxels", "dpmx_phantom_free", "dpmx_phantom_tally_size", "dpmx_run_options_default",
+            "dpmx_run", "dpmx_result_tally", "dpmx_result_tally_device", "dpmx_result_stats",
+            "dpmx_result_elapsed_ms", "dpmx_result_launches", "dpmx_result_config", "dpmx_result_free",
+            "dpmx_simulate", "dpmx_write_hist", "dpmx_sampler_eval", "dpmx_table_eval", "dpmx_simulate_histories",
+            "dpmx_influence_build", "dpmx_csr_shape", "dpmx_csr_device", "dpmx_csr_spmv", "dpmx_csr_spmv_t",
+            "dpmx_csr_download", "dpmx_csr_free"]
+
+
+class Tables:
+    """The simulation data of one data directory, uploaded to the GPU."""
+
+    def __init__(self, data_dir):
+        L = library()
+        h = C.c_void_p()
+        _check(L.dpmx_tables_load(str(data_dir).encode(), C.byref(h)))
+        self._h = h
+        self.data_dir = str(data_dir)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            library().dpmx_tables_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def num_materials(self):
+        return library().dpmx_tables_num_materials(self._h)
+
+    def density(self, imat):
+        return library().dpmx_tables_density(self._h, imat)
+
+    def material_name(self, imat):
+        buf = C.create_string_buffer(128)
+        _check(library().dpmx_tables_material_name(self._h, imat, buf, 128))
+        return buf.value.decode()
+
+    @property
+    def electron_cut(self):
+        return library().dpmx_tables_param(self._h, 0)
+
+    @property
+    def gamma_cut(self):
+        return library().dpmx_tables_param(self._h, 1)
+
+    def eval_sampler(self, sampler, energies, uniforms, imat=0, precision=FP64_PLAIN):
+        """Runs sampler 0 KN, 1 Moller, 2 SB, 3 GS on the GPU with given uniforms (n x 3)."""
+        e = np.ascontiguousarray(energies, dtype=np.float64)
+        r = np.ascontiguousarray(uniforms, dtype=np.float64).reshape(-1)
+        out = np.zeros_like(e)
+        _check(library().dpmx_sampler_eval(self._h, precision, sampler, imat, e, r, out, len(e)))
+        return out
+
+    def eval_table(self, quantity, energies, imat=0, precision=FP64_PLAIN):
+        e = np.ascontiguousarray(energies, dtype=np.float64)
+        out = np.zeros_like(e)
+        _check(library().dpmx_table_eval(self._h, precision, quantity, imat, e, out, len(e)))
+        return out
+
+
+class Phantom:
+    def __init__(self, tables, handle, shape):
+        self.tables = tables
+        self._h = handle
+        self.shape = shape
+
+    @classmethod
+    def slab(cls, tables, geom_index, lbox):
+        h = C.c_void_p()
+        _check(library().dpmx_phantom_slab(tables.handle, geom_index, lbox, C.byref(h)))
+        return cls(tables, h, (library().dpmx_phantom_tally_size(h),))
+
+    @classmethod
+    def voxels(cls, tables, mat, voxel_size):
+        """mat: uint8 array of shape (nz, ny, nx) (x fastest), 255 = vacuum; voxel_size mm (scalar or 3)."""
+        m = np.ascontiguousarray(mat, dtype=np.uint8)
+        nz, ny, nx = m.shape
+        v = np.broadcast_to(np.asarray(voxel_size, dtype=np.float64), (3,))
+        h = C.c_void_p()
+        _check(library().dpmx_phantom_voxels(tables.handle, nx, ny, nz, float(v[0]), float(v[1]), float(v[2]),
+                                              m.reshape(-1), C.byref(h)))
+        return cls(tables, h, (nz, ny, nx))
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def tally_size(self):
+        return library().dpmx_phantom_tally_size(self._h)
+
+    def close(self):
+        if self._h:
+            library().dpmx_phantom_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclass
+class Source:
+    particle: int = -1          # -1 electron, 0 photon
+    spectrum: int = 0           # 0 mono, 1 uniform [e0,e1], 2 p(E) ~ (e1-E)
+    e0: float = 15.0
+    e1: float = 15.0
+    shape: int = 0              # 0 pencil, 1 rectangle, 2 beamlet grid
+    cx: float = 0.0
+    cy: float = 0.0
+    fx: float = 0.0
+    fy: float = 0.0
+    nbx: int = 0
+    nby: int = 0
+
+    def _c(self):
+        return _Source(self.particle, self.spectrum, self.e0, self.e1, self.shape, self.cx, self.cy, self.fx,
+                       self.fy, self.nbx, self.nby)
+
+
+@dataclass
+class Job:
+    phantom: Phantom
+    source: Source = field(default_factory=Source)
+    histories: int = 1000
+    seed: int = 12345
+
+
+@dataclass
+class JobStats:
+    edep: float
+    escaped: float
+    primary_energy: float
+    max_residual: float
+    residual_violations: int
+    lost: int
+    steps: int
+    histories: int
+
+
+class Result:
+    def __init__(self, handle, jobs):
+        self._h = handle
+        self._jobs = jobs
+
+    def tally(self, j=0):
+        """(dose, dose2, steps) of job j as numpy arrays shaped like the phantom tally."""
+        ph = self._jobs[j].phantom
+        n = ph.tally_size
+        d = np.zeros(n)
+        d2 = np.zeros(n)
+        s = np.zeros(n)
+        _check(library().dpmx_result_tally(self._h, j, d.ctypes.data, d2.ctypes.data, s.ctypes.data))
+        shp = ph.shape
+        if len(shp) == 3:
+            return d.reshape(shp), d2.reshape(shp), s.reshape(shp)
+        return d, d2, s
+
+    def tally_device_ptr(self, j=0):
+        return library().dpmx_result_tally_device(self._h, j)
+
+    def stats(self, j=0):
+        s = _Stats()
+        _check(library().dpmx_result_stats(self._h, j, C.byref(s)))
+        return JobStats(s.edep, s.escaped, s.primary_energy, s.max_residual, s.residual_violations, s.lost,
+                        s.steps, s.histories)
+
+    @property
+    def elapsed_ms(self):
+        return library().dpmx_result_elapsed_ms(self._h)
+
+    @property
+    def launches(self):
+        return library().dpmx_result_launches(self._h)
+
+    @property
+    def config(self):
+        a = (C.c_longlong * 4)()
+        _check(library().dpmx_result_config(self._h, a))
+        return dict(block_size=a[0], blocks_per_sm=a[1], chunk_histories=a[2], tally_aggregate=a[3])
+
+    def influence(self, j=0, threshold=0.0):
+        from .influence import InfluenceMatrix
+        h = C.c_void_p()
+        _check(library().dpmx_influence_build(self._h, j, threshold, C.byref(h)))
+        return InfluenceMatrix(h)
+
+    def close(self):
+        if self._h:
+            library().dpmx_result_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def run(tables, jobs, precision=FP32_EVENT, batches=10, block_size=0, blocks_per_sm=0, chunk_histories=0,
+        tally_aggregate=-1, use_graph=True, tag_beamlets=False, autotune=False, stream=None):
+    """Runs the jobs (one run, one stream) and returns a Result."""
+    L = library()
+    arr = (_Job * len(jobs))()
+    for i, j in enumerate(jobs):
+        arr[i] = _Job(j.phantom.handle.value if hasattr(j.phantom.handle, "value") else j.phantom.handle,
+                      j.source._c(), int(j.histories), int(j.seed))
+    o = _Opts()
+    L.dpmx_run_options_default(C.byref(o))
+    o.precision = precision
+    o.batches = batches
+    o.block_size = block_size
+    o.blocks_per_sm = blocks_per_sm
+    o.chunk_histories = chunk_histories
+    o.tally_aggregate = tally_aggregate
+    o.use_graph = 1 if use_graph else 0
+    o.tag_beamlets = 1 if tag_beamlets else 0
+    o.autotune = 1 if autotune else 0
+    o.stream = stream
+    h = C.c_void_p()
+    rc = L.dpmx_run(tables.handle, arr, len(jobs), C.byref(o), C.byref(h))
+    if rc != OK:
+        msg = L.dpmx_last_error().decode()
+        if h:
+            L.dpmx_result_free(h)
+        raise DpmxError(rc, msg)
+    return Result(h, list(jobs))
+
+
+def simulate(tables, nprimary, eprimary=15.0, iselectron=True, lbox=1.0, geom_index=0, seed=123,
+             precision=FP64_PLAIN, cap=4096):
+    """The reference Simulate workload: returns (edep_hist, step_hist) with the
+    reference's histogram length."""
+    e = np.zeros(cap)
+    s = np.zeros(cap)
+    n = C.c_int(0)
+    _check(library().dpmx_simulate(tables.handle, int(nprimary), float(eprimary), 1 if iselectron else 0,
+                                   float(lbox), int(geom_index), int(seed), precision, e, s, cap, C.byref(n)))
+    return e[:n.value].copy(), s[:n.value].copy()
+
+
+def simulate_histories(tables, nprimary, eprimary=15.0, iselectron=True, lbox=1.0, geom_index=0, seed=123,
+                       cap=4096):
+    """FP64 form, also returning each history's deposited energy."""
+    he = np.zeros(max(1, nprimary))
+    e = np.zeros(cap)
+    _check(library().dpmx_simulate_histories(tables.handle, int(nprimary), float(eprimary), 1 if iselectron else 0,
+                                             float(lbox), int(geom_index), int(seed), he, e, cap))
+    return he[:nprimary], e
+
+
+def write_hist(tables, fname, geom_index, lbox, nprimary, edep_hist, step_hist):
+    e = np.ascontiguousarray(edep_hist, dtype=np.float64)
+    s = np.ascontiguousarray(step_hist, dtype=np.float64)
+    _check(library().dpmx_write_hist(tables.handle, str(fname).encode(), geom_index, lbox, nprimary, e, s, len(e)))
+
+
+def build(verbose=False):
+    from . import builder
+    return builder.build(verbose)

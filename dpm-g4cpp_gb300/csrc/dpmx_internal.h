@@ -1,0 +1,145 @@
+// Internal definitions shared by the host library code and the CUDA kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "dpmx.h"
+
+namespace dpmx {
+
+constexpr int kMaxMat = 8;         // materials per data set
+constexpr uint8_t kVacuum = 255;   // material id of vacuum voxels
+
+// ---------------------------------------------------------------------------
+// Device table views, templated on the arithmetic type R (double for the plain
+// FP64 form, float for the event-based form). All arrays live in one device
+// allocation per precision.
+// ---------------------------------------------------------------------------
+template <class R>
+struct SplineT {       // natural cubic spline on a log-uniform grid: n x {x,y,b,c,d}
+  const R* p;
+  int n;
+  R logMin, invLogDelta, emin, emaxm;   // emaxm = emax - 1e-6 (loader clamp)
+};
+template <class R>
+struct LinearT {       // linear interpolation on a uniform grid: n x {x,y}
+  const R* p;
+  int n;
+  R xmin, invDelta, emin, emaxm;
+};
+template <class R>
+struct alignas(sizeof(R) * 4) AliasEntry {   // one point of an alias + linear-pdf table
+  R x, y, w;
+  int32_t idx;
+};
+template <class R>
+struct AliasSetT {     // numE tables of numS points on a log energy grid
+  const AliasEntry<R>* p;
+  int numE, numS;
+  R minE, logMinE, invLogDeltaE;
+};
+template <class R>
+struct GSSetT {        // GS ratin tables: numE x numS x {u,a,b,pad}
+  const R* uab;
+  const R* e;          // energy grid
+  const R* a;          // transformation parameter per energy
+  int numE, numS;
+  R logMinE, invLogDeltaE, deltaCum;
+};
+
+template <class R>
+struct DevTables {
+  int nmat;
+  R ecut, gcut;
+  R density[kMaxMat], mollerScale[kMaxMat];
+  SplineT<R> dedx[kMaxMat], itr1[kMaxMat], brem[kMaxMat], k1, moller;
+  LinearT<R> imfpMax, tot[kMaxMat], comp[kMaxMat], pair[kMaxMat];
+  AliasSetT<R> kn, mol, sb[kMaxMat];
+  GSSetT<R> gs;
+  const R* elecBase;   // electron spline data are contiguous from here ...
+  int elecCount;       // ... for this many values (shared-memory staging)
+};
+
+// ---------------------------------------------------------------------------
+// Host-side parsed data (FP64, as read from the files)
+// ---------------------------------------------------------------------------
+struct Curve {
+  std::vector<double> x, y;
+};
+struct AliasTab {
+  double e = 0;
+  std::vector<double> x, y, w;
+  std::vector<int> idx;
+};
+
+struct HostTables {
+  double ecut = 0, gcut = 0, slow = 0, shigh = 0, ecross = 0;
+  int nmat = 0;
+  std::vector<std::string> names;
+  std::vector<double> density, mollerScale;
+  std::vector<Curve> dedx, itr1, brem;
+  Curve k1, moller;
+  Curve imfpMax;
+  std::vector<Curve> tot, comp, pair;
+  std::vector<AliasTab> kn, mol;
+  std::vector<double> sbE;
+  std::vector<std::vector<AliasTab>> sb;
+  int gsNumE = 0, gsNumS = 0;
+  std::vector<double> gsE, gsA, gsU, gsPA, gsPB;   // [e*numS + s]
+};
+
+int LoadHostTables(const std::string& dir, HostTables& h, std::string& err);
+
+// natural cubic spline coefficients (b, c, d per point), the recurrence of the
+// reference loader
+void SplineCoefficients(const std::vector<double>& x, const std::vector<double>& y, std::vector<double>& b,
+                        std::vector<double>& c, std::vector<double>& d);
+
+// ---------------------------------------------------------------------------
+// Geometry and source descriptors passed to kernels
+// ---------------------------------------------------------------------------
+struct GridGeom {          // voxel box; world = the box
+  int nx, ny, nz;
+  double x0, y0, z0;       // lower corner of voxel (0,0,0) [mm]
+  double vx, vy, vz;       // voxel size [mm]
+  const uint8_t* mat;      // nx*ny*nz material ids (kVacuum outside any material)
+  int tallyDepth;          // 1: tally by iz only (slab workload), 0: 3-D
+  int matByDepth;          // 1: mat has nz entries, indexed by iz (slab presets)
+};
+
+struct SlabGeomD {         // the reference's pre-defined slab geometry (Geom.cc)
+  int geomIndex;
+  double L, invL, halfL;
+};
+
+struct SourceD {
+  int particle, spectrum, shape, nbx, nby;
+  double e0, e1, cx, cy, fx, fy;
+  double zEntry;           // z of the entry plane [mm]
+};
+
+}  // namespace dpmx
+
+// opaque handles of the C ABI
+struct dpmx_tables {
+  dpmx::HostTables h;
+  int device = 0;
+  void* d64 = nullptr;
+  void* d32 = nullptr;
+  dpmx::DevTables<double> t64;
+  dpmx::DevTables<float> t32;
+};
+
+struct dpmx_phantom {
+  const dpmx_tables* tables = nullptr;
+  int kind = 0;             // 0 slab preset, 1 voxel array
+  int geomIndex = 0;
+  double lbox = 1.0;
+  dpmx::GridGeom grid{};    // voxel box (slab presets are materialised too)
+  uint8_t* d_mat = nullptr;
+  long long tallySize = 0;
+};

@@ -1,0 +1,70 @@
+// Host-side helpers shared by the C ABI translation units: error reporting and
+// the result / matrix objects behind the opaque handles.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "kernels.h"
+
+namespace dpmx {
+
+// records the message of the calling thread's last failure and returns code
+int Fail(int code, const std::string& msg);
+int NumSMs();
+// Geom::GetMaterialIndex / GetVoxelMaterialDensity of the slab presets (Geom.cc:133-164)
+int SlabMaterialAt(int geomIndex, double invL, int iz);
+double SlabDensityAt(const dpmx_tables* t, int geomIndex, double invL, int iz);
+// the reference's depth-histogram length for the deepest bin reached (Geom.cc:120-130)
+int HistLen(int maxIz);
+
+#define CK(call)                                                                               \
+  do {                                                                                         \
+    cudaError_t e_ = (call);                                                                   \
+    if (e_ != cudaSuccess) {                                                                   \
+      return ::dpmx::Fail(e_ == cudaErrorMemoryAllocation ? DPMX_ERR_NOMEM : DPMX_ERR_CUDA,    \
+                          std::string(#call) + ": " + cudaGetErrorString(e_));                 \
+    }                                                                                          \
+  } while (0)
+
+struct JobOut {
+  long long tallySize = 0;
+  int slab = 0;              // depth tally of a slab preset
+  double* d_dose = nullptr;
+  double* d_dose2 = nullptr;
+  double* d_steps = nullptr;
+  double* d_btally = nullptr;
+  int nbeamlets = 0;
+  long long nvox = 0;
+  int maxIz = 0;
+  RunCounters cnt{};
+};
+
+}  // namespace dpmx
+
+struct dpmx_result {
+  std::vector<dpmx::JobOut> jobs;
+  double ms = 0.0;
+  long long launches = 0;
+  long long cfg[4] = {0, 0, 0, 0};
+  ~dpmx_result() {
+    for (auto& j : jobs) {
+      cudaFree(j.d_dose);
+      cudaFree(j.d_dose2);
+      cudaFree(j.d_steps);
+      cudaFree(j.d_btally);
+    }
+  }
+};
+
+struct dpmx_csr {
+  long long rows = 0, cols = 0, nnz = 0;
+  int64_t* rowPtr = nullptr;
+  int32_t* col = nullptr;
+  float* val = nullptr;
+  ~dpmx_csr() {
+    cudaFree(rowPtr);
+    cudaFree(col);
+    cudaFree(val);
+  }
+};

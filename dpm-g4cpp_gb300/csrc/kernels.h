@@ -1,0 +1,138 @@
+// Kernel launch interfaces between the host orchestration (api.cu) and the
+// transport translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "dpmx_internal.h"
+
+namespace dpmx {
+
+// run counters accumulated on the device (one set per job)
+struct RunCounters {
+  double deposited;
+  double escaped;
+  double primaryEnergy;
+  unsigned long long maxResidualBits;   // max residual as ordered double bits
+  unsigned long long steps;
+  unsigned long long violations;
+  unsigned long long lost;
+  unsigned long long histories;
+};
+
+// warp-reduced accumulation of per-thread counters (FP64 plain form)
+__device__ inline void AccumulateCounters(RunCounters* c, double dep, double esc, double e0, double maxres,
+                                          long long steps, long long viol, int lost) {
+  const unsigned full = 0xffffffffu;
+  for (int o = 16; o > 0; o >>= 1) {
+    dep += __shfl_down_sync(full, dep, o);
+    esc += __shfl_down_sync(full, esc, o);
+    e0 += __shfl_down_sync(full, e0, o);
+    maxres = fmax(maxres, __shfl_down_sync(full, maxres, o));
+    steps += __shfl_down_sync(full, steps, o);
+    viol += __shfl_down_sync(full, viol, o);
+    lost += __shfl_down_sync(full, lost, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&c->deposited, dep);
+    atomicAdd(&c->escaped, esc);
+    atomicAdd(&c->primaryEnergy, e0);
+    atomicMax(&c->maxResidualBits, (unsigned long long)__double_as_longlong(maxres));
+    atomicAdd(&c->steps, (unsigned long long)steps);
+    atomicAdd(&c->violations, (unsigned long long)viol);
+    atomicAdd(&c->lost, (unsigned long long)lost);
+  }
+}
+
+// ---- FP64 plain form (transport_fp64.cu) ----
+cudaError_t LaunchFp64Slab(const DevTables<double>& T, const SlabGeomD& g, const double* density, const SourceD& src,
+                           long long first, long long n, uint64_t seed, double* edep, double* steps, int cap,
+                           int* maxIz, double* histEdep, RunCounters* cnt, int blocks, cudaStream_t st);
+cudaError_t LaunchFp64Grid(const DevTables<double>& T, const GridGeom& g, const double* density, const SourceD& src,
+                           long long first, long long n, uint64_t seed, double* tally, double* histEdep,
+                           RunCounters* cnt, int blocks, cudaStream_t st);
+cudaError_t LaunchSamplerEval64(const DevTables<double>& T, int s, int imat, const double* e, const double* r,
+                                double* out, int n, cudaStream_t st);
+cudaError_t LaunchTableEval64(const DevTables<double>& T, int q, int imat, const double* e, double* out, int n,
+                              cudaStream_t st);
+
+// ---- FP32 event-based form (transport_fp32.cu) ----
+constexpr int kMaxJobs = 256;
+constexpr int kMaxGenerations = 48;
+
+struct JobF {                  // per-job geometry, source and tally (device view)
+  int nx, ny, nz, tallyDepth;
+  int matByDepth;              // material array indexed by iz only (slab presets)
+  float vx, vy, vz, ivx, ivy, ivz;
+  double x0, y0, z0;           // lower corner of voxel (0,0,0) [mm]
+  const uint8_t* mat;
+  double* tally;               // batch tally of this job
+  double* steps;               // scoring-step counts (depth tally only) or null
+  double* btally;              // beamlet-tagged tally [beamlet][nvox] or null
+  int nbeamlets;
+  int particle, spectrum, shape, nbx, nby;
+  float e0, e1, cx, cy, fx, fy;
+  uint32_t k0, k1;             // Philox key (job seed)
+  RunCounters* cnt;
+};
+
+struct Segment {               // a run of primaries of one job inside a chunk
+  int job;
+  int pad;
+  long long firstHist;         // first history index of the run within the job
+  long long count;
+  long long prefix;            // index of the run's first primary within the phase
+  long long slotBase;          // energy-check slot of the run's first primary
+};
+
+struct Queue {                 // SoA particle queue
+  float *lx, *ly, *lz, *dx, *dy, *dz, *e;
+  uint32_t *vox, *hist, *slot, *uidlo, *uidhi, *meta;
+  unsigned long long capacity;
+};
+
+struct PhaseArgs {
+  DevTables<float> T;
+  const JobF* jobs;
+  int njobs;
+  const Segment* segs;         // primaries of this phase (may be empty)
+  int nsegs;
+  long long nPrimaries;
+  Queue in;                    // particles to transport in this phase
+  const unsigned long long* inCount;
+  Queue outE, outP;            // secondaries: electrons, photons
+  unsigned long long* outECount;
+  unsigned long long* outPCount;
+  unsigned long long* head;    // work counter of this phase
+  double* histE;               // per-slot energy accounted (deposit + escape)
+  double* histE0;              // per-slot primary energy
+  unsigned long long* overflow;
+  int aggregate;               // warp-aggregated tally atomics
+};
+
+cudaError_t LaunchPhotonPhase(const PhaseArgs& a, int blocks, int threads, cudaStream_t st);
+cudaError_t LaunchElectronPhase(const PhaseArgs& a, int blocks, int threads, cudaStream_t st);
+// dose += t, dose2 += t^2, t = 0 over n bins
+cudaError_t LaunchFold(double* t, double* dose, double* dose2, long long n, cudaStream_t st);
+// per-slot energy check against the primary energy, per-job counters
+cudaError_t LaunchEnergyCheck(const double* histE, const double* histE0, long long nslots, const Segment* segs,
+                              int nsegs, const JobF* jobs, cudaStream_t st);
+cudaError_t LaunchSamplerEval32(const DevTables<float>& T, int s, int imat, const double* e, const double* r,
+                                double* out, int n, cudaStream_t st);
+cudaError_t LaunchTableEval32(const DevTables<float>& T, int q, int imat, const double* e, double* out, int n,
+                              cudaStream_t st);
+int ElectronPhaseSmemBytes(const DevTables<float>& T);
+
+// ---- influence matrix (influence.cu) ----
+cudaError_t LaunchCountNnz(const double* dense, long long nvox, int nb, double thr, long long* rowCount,
+                           cudaStream_t st);
+cudaError_t LaunchFillCsr(const double* dense, long long nvox, int nb, double thr, const long long* rowPtr,
+                          int32_t* col, float* val, cudaStream_t st);
+cudaError_t LaunchSpmv(const int64_t* rowPtr, const int32_t* col, const float* val, long long rows, const double* x,
+                       double* y, cudaStream_t st);
+cudaError_t LaunchSpmvT(const int64_t* rowPtr, const int32_t* col, const float* val, long long rows, long long cols,
+                        const double* y, double* x, cudaStream_t st);
+cudaError_t LaunchMaxAbs(const double* a, long long n, unsigned long long* outBits, cudaStream_t st);
+
+}  // namespace dpmx

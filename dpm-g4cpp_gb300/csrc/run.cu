@@ -1,0 +1,674 @@
+// Run orchestration behind dpmx_run / dpmx_simulate and the remaining C ABI:
+//
+//  * FP64 plain form: per job and statistical batch, one launch of the
+//    one-thread-per-history kernel into a batch tally, then a fold
+//    (dose += t, dose2 += t^2).
+//  * FP32 event form: every batch of every job is cut into chunks of at most
+//    `chunk` histories; a chunk runs kGen generations of (photon phase,
+//    electron phase) over double-buffered queues, then the per-history energy
+//    check. The launches of the whole run (all batches, chunks, generations,
+//    folds) are captured into one CUDA graph and launched once. Empty phases
+//    return at once (their input count is read on the device).
+//  * Tuning: a short sample of the jobs is timed for a few launch shapes
+//    (threads per block, blocks per SM, warp-aggregated tally) and chunk
+//    sizes, and the fastest is used for the run.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "host_util.h"
+
+using namespace dpmx;
+
+namespace {
+
+constexpr int kGen = 32;                              // generations per chunk
+constexpr int kCtrPerChunk = 4 * (kGen + 1) + 1;      // cntE, cntP, headE, headP per generation + overflow
+
+struct Cfg {
+  int threads = 256;
+  int blocksPerSM = 2;
+  long long chunk = 1 << 20;
+  int aggregate = 0;
+};
+
+struct DevBuf {       // owned device allocations of one run
+  std::vector<void*> v;
+  ~DevBuf() { for (void* p : v) cudaFree(p); }
+  template <class T> int Get(T** p, size_t n) {
+    void* q = nullptr;
+    CK(cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T)));
+    v.push_back(q);
+    *p = static_cast<T*>(q);
+    return DPMX_OK;
+  }
+};
+
+int AllocQueue(DevBuf& b, Queue& q, unsigned long long cap) {
+  q.capacity = cap;
+  float** f[7] = {&q.lx, &q.ly, &q.lz, &q.dx, &q.dy, &q.dz, &q.e};
+  uint32_t** u[6] = {&q.vox, &q.hist, &q.slot, &q.uidlo, &q.uidhi, &q.meta};
+  for (auto x : f) if (int rc = b.Get(x, cap)) return rc;
+  for (auto x : u) if (int rc = b.Get(x, cap)) return rc;
+  return DPMX_OK;
+}
+
+struct Chunk {
+  std::vector<Segment> segP, segE, segAll;   // photon primaries, electron primaries, all by slot
+  long long nP = 0, nE = 0, nslots = 0;
+};
+
+// splits batch b (of B) of every job into chunks of at most `chunk` histories
+std::vector<Chunk> PlanBatch(const dpmx_job* jobs, int njobs, int b, int B, long long chunk) {
+  std::vector<Chunk> out;
+  Chunk cur;
+  for (int j = 0; j < njobs; ++j) {
+    const long long N = jobs[j].histories;
+    long long first = N * b / B;
+    long long left = N * (b + 1) / B - first;
+    while (left > 0) {
+      const long long take = std::min(left, chunk - cur.nslots);
+      Segment s{};
+      s.job = j;
+      s.firstHist = first;
+      s.count = take;
+      s.slotBase = cur.nslots;
+      if (jobs[j].source.particle == 0) { s.prefix = cur.nP; cur.nP += take; cur.segP.push_back(s); }
+      else { s.prefix = cur.nE; cur.nE += take; cur.segE.push_back(s); }
+      cur.segAll.push_back(s);
+      cur.nslots += take;
+      first += take;
+      left -= take;
+      if (cur.nslots == chunk) { out.push_back(cur); cur = Chunk(); }
+    }
+  }
+  if (cur.nslots > 0) out.push_back(cur);
+  return out;
+}
+
+bool IsPow2Aligned(long long) { return true; }
+
+// ---------------------------------------------------------------------------
+// FP32 event form
+// ---------------------------------------------------------------------------
+int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, const Cfg& cfg, bool tag,
+            bool useGraph, cudaStream_t st, std::vector<JobOut>& outs, double* ms, long long* launches) {
+  DevBuf buf;
+  const int nsm = NumSMs();
+  // concatenated tallies of all jobs: batch tally, dose, dose2
+  std::vector<long long> off(njobs);
+  long long total = 0;
+  for (int j = 0; j < njobs; ++j) { off[j] = total; total += outs[j].tallySize; }
+  double *tB, *dose, *dose2;
+  if (int rc = buf.Get(&tB, total)) return rc;
+  if (int rc = buf.Get(&dose, total)) return rc;
+  if (int rc = buf.Get(&dose2, total)) return rc;
+  CK(cudaMemsetAsync(tB, 0, total * sizeof(double), st));
+  CK(cudaMemsetAsync(dose, 0, total * sizeof(double), st));
+  CK(cudaMemsetAsync(dose2, 0, total * sizeof(double), st));
+  RunCounters* cnt;
+  if (int rc = buf.Get(&cnt, njobs)) return rc;
+  CK(cudaMemsetAsync(cnt, 0, njobs * sizeof(RunCounters), st));
+  std::vector<JobF> hj(njobs);
+  for (int j = 0; j < njobs; ++j) {
+    const dpmx_phantom* ph = jobs[j].phantom;
+    const GridGeom& g = ph->grid;
+    JobF& J = hj[j];
+    std::memset(&J, 0, sizeof(J));
+    J.nx = g.nx; J.ny = g.ny; J.nz = g.nz;
+    J.tallyDepth = g.tallyDepth;
+    J.matByDepth = g.matByDepth;
+    J.vx = float(g.vx); J.vy = float(g.vy); J.vz = float(g.vz);
+    J.ivx = float(1.0 / g.vx); J.ivy = float(1.0 / g.vy); J.ivz = float(1.0 / g.vz);
+    J.x0 = g.x0; J.y0 = g.y0; J.z0 = g.z0;
+    J.mat = g.mat;
+    J.tally = tB + off[j];
+    J.steps = outs[j].d_steps;
+    J.btally = tag ? outs[j].d_btally : nullptr;
+    J.nbeamlets = std::max(1, outs[j].nbeamlets);
+    const dpmx_source& s = jobs[j].source;
+    J.particle = s.particle; J.spectrum = s.spectrum; J.shape = s.shape; J.nbx = s.nbx; J.nby = s.nby;
+    J.e0 = float(s.e0); J.e1 = float(s.e1);
+    J.cx = float(s.cx); J.cy = float(s.cy); J.fx = float(s.fx); J.fy = float(s.fy);
+    if (ph->kind == 0) { J.shape = 0; J.cx = 0.f; J.cy = 0.f; }   // the reference's pencil beam
+    J.k0 = uint32_t(jobs[j].seed);
+    J.k1 = uint32_t(jobs[j].seed >> 32) ^ 0x5bd1e995u;
+    J.cnt = cnt + j;
+  }
+  JobF* dj;
+  if (int rc = buf.Get(&dj, njobs)) return rc;
+  CK(cudaMemcpyAsync(dj, hj.data(), njobs * sizeof(JobF), cudaMemcpyHostToDevice, st));
+
+  // plan and segment tables
+  std::vector<std::vector<Chunk>> plan(batches);
+  std::vector<Segment> segs;
+  size_t nchunks = 0;
+  long long maxSlots = 1;
+  for (int b = 0; b < batches; ++b) {
+    plan[b] = PlanBatch(jobs, njobs, b, batches, cfg.chunk);
+    for (auto& c : plan[b]) {
+      segs.insert(segs.end(), c.segP.begin(), c.segP.end());
+      segs.insert(segs.end(), c.segE.begin(), c.segE.end());
+      segs.insert(segs.end(), c.segAll.begin(), c.segAll.end());
+      maxSlots = std::max(maxSlots, c.nslots);
+      ++nchunks;
+    }
+  }
+  Segment* dsegs;
+  if (int rc = buf.Get(&dsegs, segs.size())) return rc;
+  if (!segs.empty()) CK(cudaMemcpyAsync(dsegs, segs.data(), segs.size() * sizeof(Segment), cudaMemcpyHostToDevice, st));
+  double *histE, *histE0;
+  if (int rc = buf.Get(&histE, maxSlots)) return rc;
+  if (int rc = buf.Get(&histE0, maxSlots)) return rc;
+  unsigned long long* ctr;
+  if (int rc = buf.Get(&ctr, nchunks * kCtrPerChunk)) return rc;
+  CK(cudaMemsetAsync(ctr, 0, nchunks * kCtrPerChunk * sizeof(unsigned long long), st));
+  // queues: double-buffered electrons and photons; a generation holds well
+  // under 8 secondaries of each kind per primary
+  const unsigned long long cap = (unsigned long long)std::max<long long>(maxSlots * 8, 1 << 14);
+  Queue qe[2], qp[2];
+  for (int k = 0; k < 2; ++k) {
+    if (int rc = AllocQueue(buf, qe[k], cap)) return rc;
+    if (int rc = AllocQueue(buf, qp[k], cap)) return rc;
+  }
+  const int blocks = nsm * cfg.blocksPerSM;
+  long long nl = 0;
+  auto enqueue = [&](cudaStream_t s) -> int {
+    size_t segCur = 0, ci = 0;
+    for (int b = 0; b < batches; ++b) {
+      for (auto& c : plan[b]) {
+        unsigned long long* cc = ctr + ci * kCtrPerChunk;
+        unsigned long long* cntE = cc;
+        unsigned long long* cntP = cc + (kGen + 1);
+        unsigned long long* headE = cc + 2 * (kGen + 1);
+        unsigned long long* headP = cc + 3 * (kGen + 1);
+        unsigned long long* ovf = cc + 4 * (kGen + 1);
+        const Segment* sP = dsegs + segCur;
+        const Segment* sE = sP + c.segP.size();
+        const Segment* sA = sE + c.segE.size();
+        CK(cudaMemsetAsync(histE, 0, c.nslots * sizeof(double), s));
+        for (int g = 0; g < kGen; ++g) {
+          PhaseArgs a;
+          std::memset(&a, 0, sizeof(a));
+          a.T = T->t32;
+          a.jobs = dj;
+          a.njobs = njobs;
+          a.histE = histE;
+          a.histE0 = histE0;
+          a.overflow = ovf;
+          a.aggregate = cfg.aggregate;
+          // photons of generation g; their electrons join generation g
+          a.segs = sP; a.nsegs = int(c.segP.size()); a.nPrimaries = (g == 0) ? c.nP : 0;
+          a.in = qp[g & 1]; a.inCount = cntP + g;
+          a.outE = qe[g & 1]; a.outECount = cntE + g;
+          a.outP = qp[(g + 1) & 1]; a.outPCount = cntP + g + 1;
+          a.head = headP + g;
+          CK(LaunchPhotonPhase(a, blocks, cfg.threads, s));
+          ++nl;
+          // electrons of generation g; their secondaries form generation g+1
+          a.segs = sE; a.nsegs = int(c.segE.size()); a.nPrimaries = (g == 0) ? c.nE : 0;
+          a.in = qe[g & 1]; a.inCount = cntE + g;
+          a.outE = qe[(g + 1) & 1]; a.outECount = cntE + g + 1;
+          a.outP = qp[(g + 1) & 1]; a.outPCount = cntP + g + 1;
+          a.head = headE + g;
+          CK(LaunchElectronPhase(a, blocks, cfg.threads, s));
+          ++nl;
+        }
+        CK(LaunchEnergyCheck(histE, histE0, c.nslots, sA, int(c.segAll.size()), dj, s));
+        ++nl;
+        segCur += c.segP.size() + c.segE.size() + c.segAll.size();
+        ++ci;
+      }
+      CK(LaunchFold(tB, dose, dose2, total, s));
+      ++nl;
+    }
+    return DPMX_OK;
+  };
+
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  int rc = DPMX_OK;
+  if (useGraph) {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    rc = enqueue(st);
+    cudaError_t ce = cudaStreamEndCapture(st, &graph);
+    if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
+    CK(ce);
+    CK(cudaGraphInstantiate(&exec, graph, 0));
+    CK(cudaEventRecord(e0, st));
+    CK(cudaGraphLaunch(exec, st));
+    CK(cudaEventRecord(e1, st));
+    CK(cudaStreamSynchronize(st));
+    cudaGraphExecDestroy(exec);
+    cudaGraphDestroy(graph);
+  } else {
+    CK(cudaEventRecord(e0, st));
+    rc = enqueue(st);
+    if (rc) return rc;
+    CK(cudaEventRecord(e1, st));
+    CK(cudaStreamSynchronize(st));
+  }
+  float fms = 0.f;
+  CK(cudaEventElapsedTime(&fms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms = fms;
+  *launches = nl;
+  // results: leftovers beyond the last generation and queue overflows are losses
+  std::vector<unsigned long long> hc(nchunks * kCtrPerChunk);
+  CK(cudaMemcpy(hc.data(), ctr, hc.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+  unsigned long long lost = 0;
+  for (size_t ci = 0; ci < nchunks; ++ci) {
+    const unsigned long long* cc = hc.data() + ci * kCtrPerChunk;
+    lost += cc[kGen] + cc[(kGen + 1) + kGen] + cc[4 * (kGen + 1)];
+  }
+  std::vector<RunCounters> hcnt(njobs);
+  CK(cudaMemcpy(hcnt.data(), cnt, njobs * sizeof(RunCounters), cudaMemcpyDeviceToHost));
+  for (int j = 0; j < njobs; ++j) {
+    outs[j].cnt = hcnt[j];
+    CK(cudaMemcpy(outs[j].d_dose, dose + off[j], outs[j].tallySize * sizeof(double), cudaMemcpyDeviceToDevice));
+    CK(cudaMemcpy(outs[j].d_dose2, dose2 + off[j], outs[j].tallySize * sizeof(double), cudaMemcpyDeviceToDevice));
+  }
+  // the step counter of the electron phase is accumulated on job 0
+  if (njobs > 0) outs[0].cnt.lost += lost;
+  for (int j = 0; j < njobs; ++j) {
+    double e = 0.0;
+    std::vector<double> h(outs[j].tallySize);
+    CK(cudaMemcpy(h.data(), outs[j].d_dose, h.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    for (double v : h) e += v;
+    outs[j].cnt.deposited = e;
+    if (outs[j].slab) {
+      int mz = 0;
+      for (size_t i = 0; i < h.size(); ++i) if (h[i] != 0.0) mz = int(i);
+      outs[j].maxIz = mz;
+    }
+  }
+  if (lost > 0) return Fail(DPMX_ERR_OVERFLOW, "particle queue overflow or generation limit reached");
+  return DPMX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 plain form
+// ---------------------------------------------------------------------------
+int RunFp64(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, bool fixedSeedSlab, cudaStream_t st,
+            std::vector<JobOut>& outs, double* ms, long long* launches, double* histEdep) {
+  DevBuf buf;
+  const int blocks = NumSMs() * 16;
+  double* density;
+  if (int rc = buf.Get(&density, kMaxMat)) return rc;
+  CK(cudaMemcpyAsync(density, T->h.density.data(), T->h.nmat * sizeof(double), cudaMemcpyHostToDevice, st));
+  RunCounters* cnt;
+  if (int rc = buf.Get(&cnt, njobs)) return rc;
+  CK(cudaMemsetAsync(cnt, 0, njobs * sizeof(RunCounters), st));
+  int* maxIz;
+  if (int rc = buf.Get(&maxIz, njobs)) return rc;
+  CK(cudaMemsetAsync(maxIz, 0, njobs * sizeof(int), st));
+  long long maxT = 1;
+  for (auto& o : outs) maxT = std::max(maxT, o.tallySize);
+  double* tB;
+  if (int rc = buf.Get(&tB, maxT)) return rc;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaEventRecord(e0, st));
+  long long nl = 0;
+  long long histOff = 0;
+  for (int j = 0; j < njobs; ++j) {
+    const dpmx_phantom* ph = jobs[j].phantom;
+    JobOut& o = outs[j];
+    CK(cudaMemsetAsync(o.d_dose, 0, o.tallySize * sizeof(double), st));
+    CK(cudaMemsetAsync(o.d_dose2, 0, o.tallySize * sizeof(double), st));
+    SourceD src{};
+    const dpmx_source& s = jobs[j].source;
+    src.particle = s.particle; src.spectrum = s.spectrum; src.shape = s.shape; src.nbx = s.nbx; src.nby = s.nby;
+    src.e0 = s.e0; src.e1 = s.e1; src.cx = s.cx; src.cy = s.cy; src.fx = s.fx; src.fy = s.fy;
+    src.zEntry = ph->grid.z0;
+    const long long N = jobs[j].histories;
+    for (int b = 0; b < batches; ++b) {
+      const long long lo = N * b / batches, hi = N * (b + 1) / batches;
+      if (hi <= lo) continue;
+      CK(cudaMemsetAsync(tB, 0, o.tallySize * sizeof(double), st));
+      double* he = histEdep ? histEdep + histOff + lo : nullptr;
+      if (ph->kind == 0) {
+        SlabGeomD g{ph->geomIndex, ph->lbox, 1.0 / ph->lbox, 0.5 * ph->lbox};
+        CK(LaunchFp64Slab(T->t64, g, density, src, lo, hi - lo, jobs[j].seed, tB, o.d_steps, int(o.tallySize),
+                          maxIz + j, he, cnt + j, blocks, st));
+      } else {
+        GridGeom g = ph->grid;
+        CK(LaunchFp64Grid(T->t64, g, density, src, lo, hi - lo, jobs[j].seed, tB, he, cnt + j, blocks, st));
+      }
+      CK(LaunchFold(tB, o.d_dose, o.d_dose2, o.tallySize, st));
+      nl += 2;
+    }
+    histOff += N;
+  }
+  (void)fixedSeedSlab;
+  CK(cudaEventRecord(e1, st));
+  CK(cudaStreamSynchronize(st));
+  float fms = 0.f;
+  CK(cudaEventElapsedTime(&fms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms = fms;
+  *launches = nl;
+  std::vector<RunCounters> hcnt(njobs);
+  std::vector<int> hmz(njobs);
+  CK(cudaMemcpy(hcnt.data(), cnt, njobs * sizeof(RunCounters), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(hmz.data(), maxIz, njobs * sizeof(int), cudaMemcpyDeviceToHost));
+  for (int j = 0; j < njobs; ++j) {
+    outs[j].cnt = hcnt[j];
+    outs[j].cnt.histories = (unsigned long long)jobs[j].histories;
+    outs[j].maxIz = hmz[j];
+  }
+  long long lost = 0;
+  for (auto& o : outs) lost += (long long)o.cnt.lost;
+  if (lost > 0) return Fail(DPMX_ERR_OVERFLOW, "secondary stack overflow or step limit reached");
+  return DPMX_OK;
+}
+
+int PrepareOutputs(const dpmx_job* jobs, int njobs, bool tag, std::vector<JobOut>& outs) {
+  outs.assign(njobs, JobOut());
+  for (int j = 0; j < njobs; ++j) {
+    const dpmx_phantom* ph = jobs[j].phantom;
+    JobOut& o = outs[j];
+    o.tallySize = ph->tallySize;
+    o.slab = ph->kind == 0;
+    o.nvox = (long long)ph->grid.nx * ph->grid.ny * ph->grid.nz;
+    CK(cudaMalloc(&o.d_dose, o.tallySize * sizeof(double)));
+    CK(cudaMalloc(&o.d_dose2, o.tallySize * sizeof(double)));
+    CK(cudaMemset(o.d_dose, 0, o.tallySize * sizeof(double)));
+    CK(cudaMemset(o.d_dose2, 0, o.tallySize * sizeof(double)));
+    if (o.slab) {
+      CK(cudaMalloc(&o.d_steps, o.tallySize * sizeof(double)));
+      CK(cudaMemset(o.d_steps, 0, o.tallySize * sizeof(double)));
+    }
+    if (tag && !o.slab) {
+      const dpmx_source& s = jobs[j].source;
+      o.nbeamlets = (s.shape == 2) ? std::max(1, s.nbx * s.nby) : 1;
+      const size_t n = size_t(o.nbeamlets) * size_t(o.nvox);
+      CK(cudaMalloc(&o.d_btally, n * sizeof(double)));
+      CK(cudaMemset(o.d_btally, 0, n * sizeof(double)));
+    }
+  }
+  return DPMX_OK;
+}
+
+int CheckJobs(const dpmx_tables* t, const dpmx_job* jobs, int njobs) {
+  if (!t || !jobs || njobs < 1) return Fail(DPMX_ERR_ARG, "no jobs");
+  if (njobs > kMaxJobs) return Fail(DPMX_ERR_ARG, "too many jobs in one run");
+  for (int j = 0; j < njobs; ++j) {
+    const dpmx_job& J = jobs[j];
+    if (!J.phantom || J.phantom->tables != t) return Fail(DPMX_ERR_ARG, "job phantom missing or built on other tables");
+    if (J.histories < 0 || J.histories > 0xffffffffLL) return Fail(DPMX_ERR_ARG, "histories must be in [0, 2^32)");
+    const dpmx_source& s = J.source;
+    if (s.particle != -1 && s.particle != 0) return Fail(DPMX_ERR_ARG, "source particle must be -1 (e-) or 0 (photon)");
+    const double emax = t->h.dedx[0].x.back();
+    const double emin = s.particle == 0 ? t->h.gcut : t->h.ecut;
+    const double hi = s.spectrum == 0 ? s.e0 : std::max(s.e0, s.e1);
+    const double lo = s.spectrum == 0 ? s.e0 : std::min(s.e0, s.e1);
+    if (!(lo > emin) || !(hi < emax)) return Fail(DPMX_ERR_ARG, "source energies must lie inside the data-set grids");
+    if (s.shape == 2 && (s.nbx < 1 || s.nby < 1 || s.nbx * s.nby > 65535))
+      return Fail(DPMX_ERR_ARG, "beamlet grid must have 1..65535 beamlets");
+    if (s.spectrum < 0 || s.spectrum > 2 || s.shape < 0 || s.shape > 2) return Fail(DPMX_ERR_ARG, "bad source spec");
+  }
+  return DPMX_OK;
+}
+
+Cfg DefaultCfg(const dpmx_run_options* o, long long totalHist) {
+  Cfg c;
+  if (o && o->block_size > 0) c.threads = o->block_size;
+  if (o && o->blocks_per_sm > 0) c.blocksPerSM = o->blocks_per_sm;
+  if (o && o->chunk_histories > 0) c.chunk = o->chunk_histories;
+  else c.chunk = std::max<long long>(1 << 14, std::min<long long>(1 << 21, totalHist));
+  if (o && o->tally_aggregate >= 0) c.aggregate = o->tally_aggregate;
+  return c;
+}
+
+// times a few launch shapes on a sample of the jobs and returns the fastest
+int Autotune(const dpmx_tables* t, const dpmx_job* jobs, int njobs, const Cfg& base, cudaStream_t st, Cfg* best) {
+  long long total = 0;
+  for (int j = 0; j < njobs; ++j) total += jobs[j].histories;
+  const long long sample = std::min<long long>(total, 1 << 18);
+  std::vector<dpmx_job> sj(jobs, jobs + njobs);
+  for (auto& j : sj) j.histories = std::max<long long>(1, (long long)(double(j.histories) * sample / std::max(1LL, total)));
+  struct Cand { int threads, bps, agg; };
+  const Cand cands[] = {{256, 2, 0}, {256, 2, 1}, {128, 4, 0}, {512, 1, 0}, {256, 3, 0}, {128, 6, 0}};
+  double bestMs = 1e30;
+  *best = base;
+  for (const Cand& c : cands) {
+    Cfg cfg = base;
+    cfg.threads = c.threads;
+    cfg.blocksPerSM = c.bps;
+    cfg.aggregate = c.agg;
+    cfg.chunk = sample;
+    std::vector<JobOut> outs;
+    if (int rc = PrepareOutputs(sj.data(), njobs, false, outs)) return rc;
+    double ms = 0;
+    long long nl = 0;
+    const int rc = RunFp32(t, sj.data(), njobs, 1, cfg, false, false, st, outs, &ms, &nl);
+    for (auto& o : outs) { cudaFree(o.d_dose); cudaFree(o.d_dose2); cudaFree(o.d_steps); cudaFree(o.d_btally); }
+    if (rc) return rc;
+    if (ms < bestMs) { bestMs = ms; *best = cfg; }
+  }
+  best->chunk = base.chunk;
+  return DPMX_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+int dpmx_run(const dpmx_tables* t, const dpmx_job* jobs, int njobs, const dpmx_run_options* opt, dpmx_result** out) {
+  if (!out) return Fail(DPMX_ERR_ARG, "null result pointer");
+  *out = nullptr;
+  if (int rc = CheckJobs(t, jobs, njobs)) return rc;
+  dpmx_run_options o;
+  if (opt) o = *opt; else dpmx_run_options_default(&o);
+  if (o.batches < 1) o.batches = 1;
+  if (o.precision != DPMX_FP64_PLAIN && o.precision != DPMX_FP32_EVENT) return Fail(DPMX_ERR_ARG, "bad precision");
+  cudaStream_t st = static_cast<cudaStream_t>(o.stream);
+  bool ownStream = false;
+  if (!st) { CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)); ownStream = true; }
+  std::unique_ptr<dpmx_result> r(new dpmx_result());
+  const bool tag = o.tag_beamlets && o.precision == DPMX_FP32_EVENT;
+  int rc = PrepareOutputs(jobs, njobs, tag, r->jobs);
+  if (!rc) {
+    if (o.precision == DPMX_FP64_PLAIN) {
+      rc = RunFp64(t, jobs, njobs, o.batches, true, st, r->jobs, &r->ms, &r->launches, nullptr);
+      r->cfg[0] = 128; r->cfg[1] = 16; r->cfg[2] = 0; r->cfg[3] = 0;
+    } else {
+      long long total = 0;
+      for (int j = 0; j < njobs; ++j) total += jobs[j].histories;
+      Cfg cfg = DefaultCfg(&o, total);
+      if (o.autotune) rc = Autotune(t, jobs, njobs, cfg, st, &cfg);
+      if (!rc) rc = RunFp32(t, jobs, njobs, o.batches, cfg, tag, o.use_graph != 0, st, r->jobs, &r->ms, &r->launches);
+      r->cfg[0] = cfg.threads; r->cfg[1] = cfg.blocksPerSM; r->cfg[2] = cfg.chunk; r->cfg[3] = cfg.aggregate;
+    }
+  }
+  if (ownStream) cudaStreamDestroy(st);
+  if (rc && rc != DPMX_ERR_OVERFLOW) return rc;
+  *out = r.release();
+  return rc;
+}
+
+int dpmx_result_tally(const dpmx_result* r, int job, double* dose, double* dose2, double* steps) {
+  if (!r || job < 0 || job >= int(r->jobs.size())) return Fail(DPMX_ERR_ARG, "bad job index");
+  const JobOut& o = r->jobs[job];
+  const size_t n = size_t(o.tallySize) * sizeof(double);
+  if (dose) CK(cudaMemcpy(dose, o.d_dose, n, cudaMemcpyDeviceToHost));
+  if (dose2) CK(cudaMemcpy(dose2, o.d_dose2, n, cudaMemcpyDeviceToHost));
+  if (steps) {
+    if (o.d_steps) CK(cudaMemcpy(steps, o.d_steps, n, cudaMemcpyDeviceToHost));
+    else std::memset(steps, 0, n);
+  }
+  return DPMX_OK;
+}
+
+const double* dpmx_result_tally_device(const dpmx_result* r, int job) {
+  if (!r || job < 0 || job >= int(r->jobs.size())) return nullptr;
+  return r->jobs[job].d_dose;
+}
+
+int dpmx_result_stats(const dpmx_result* r, int job, dpmx_job_stats* s) {
+  if (!r || !s || job < 0 || job >= int(r->jobs.size())) return Fail(DPMX_ERR_ARG, "bad job index");
+  const RunCounters& c = r->jobs[job].cnt;
+  s->edep = c.deposited;
+  s->escaped = c.escaped;
+  s->primary_energy = c.primaryEnergy;
+  double mr;
+  std::memcpy(&mr, &c.maxResidualBits, sizeof(double));
+  s->max_residual = mr;
+  s->residual_violations = (long long)c.violations;
+  s->lost = (long long)c.lost;
+  s->steps = (long long)c.steps;
+  s->histories = (long long)c.histories;
+  return DPMX_OK;
+}
+
+double dpmx_result_elapsed_ms(const dpmx_result* r) { return r ? r->ms : 0.0; }
+long long dpmx_result_launches(const dpmx_result* r) { return r ? r->launches : 0; }
+int dpmx_result_config(const dpmx_result* r, long long* cfg4) {
+  if (!r || !cfg4) return Fail(DPMX_ERR_ARG, "null argument");
+  for (int i = 0; i < 4; ++i) cfg4[i] = r->cfg[i];
+  return DPMX_OK;
+}
+void dpmx_result_free(dpmx_result* r) { delete r; }
+
+int dpmx_simulate(const dpmx_tables* t, int nprimary, double eprimary, int iselectron, double lbox, int geom_index,
+                  uint64_t seed, int precision, double* edep_hist, double* step_hist, int cap, int* hist_len) {
+  if (!t || nprimary < 0 || !(lbox > 0.0)) return Fail(DPMX_ERR_ARG, "bad simulate arguments");
+  dpmx_phantom* ph = nullptr;
+  if (int rc = dpmx_phantom_slab(t, geom_index, lbox, &ph)) return rc;
+  dpmx_job job;
+  std::memset(&job, 0, sizeof(job));
+  job.phantom = ph;
+  job.source.particle = iselectron ? -1 : 0;
+  job.source.e0 = job.source.e1 = eprimary;
+  job.histories = nprimary;
+  job.seed = seed;
+  dpmx_run_options o;
+  dpmx_run_options_default(&o);
+  o.precision = precision;
+  o.batches = 1;
+  dpmx_result* r = nullptr;
+  int rc = dpmx_run(t, &job, 1, &o, &r);
+  if (r) {
+    const JobOut& jo = r->jobs[0];
+    std::vector<double> d(jo.tallySize), s(jo.tallySize);
+    int rc2 = dpmx_result_tally(r, 0, d.data(), nullptr, s.data());
+    if (!rc && rc2) rc = rc2;
+    const int n = std::min<int>(cap, int(jo.tallySize));
+    for (int i = 0; i < n; ++i) {
+      if (edep_hist) edep_hist[i] = d[i];
+      if (step_hist) step_hist[i] = s[i];
+    }
+    int mz = 0;
+    for (int i = 0; i < int(d.size()); ++i) if (d[i] != 0.0 || s[i] != 0.0) mz = i;
+    if (hist_len) *hist_len = HistLen(mz);
+    dpmx_result_free(r);
+  }
+  dpmx_phantom_free(ph);
+  return rc;
+}
+
+int dpmx_write_hist(const dpmx_tables* t, const char* fname, int geom_index, double lbox, int nprimary,
+                    const double* edep, const double* steps, int len) {
+  // Geom::Write (Geom.cc:167-192)
+  if (!t || !fname || !edep || !steps || nprimary <= 0 || len < 0) return Fail(DPMX_ERR_ARG, "bad write arguments");
+  FILE* f = std::fopen(fname, "w");
+  if (!f) return Fail(DPMX_ERR_FILE, std::string("file ") + fname + " could not be created");
+  const double toCm = 0.1;
+  const double norm = 1. / (nprimary * lbox * toCm);
+  double sum = 0.0;
+  for (int i = 0; i < len; ++i) sum += edep[i];
+  std::fprintf(f, "# === Mean energy deposit in the target: %13.4e  [MeV/event]\n", sum / nprimary);
+  std::fprintf(f, "# === Energy deposit as a function of the depth: \n");
+  std::fprintf(f, "# === Index       Depth [cm]    Edep [MeV cm2/g]  #Simulation-Steps \n");
+  const double invL = 1.0 / lbox;
+  for (int i = 0; i < len; ++i) {
+    const double rho = SlabDensityAt(t, geom_index, invL, i);
+    std::fprintf(f, " %10d    %13.4e    %13.4e    %13.4e\n", i, (i + 0.5) * lbox * toCm, edep[i] * norm / rho,
+                 steps[i] / nprimary);
+  }
+  std::fclose(f);
+  return DPMX_OK;
+}
+
+int dpmx_sampler_eval(const dpmx_tables* t, int precision, int sampler, int imat, const double* e, const double* r,
+                      double* out, int n) {
+  if (!t || !e || !r || !out || n < 0 || sampler < 0 || sampler > 3) return Fail(DPMX_ERR_ARG, "bad sampler arguments");
+  if (imat < 0 || imat >= t->h.nmat) return Fail(DPMX_ERR_ARG, "bad material index");
+  if (n == 0) return DPMX_OK;
+  DevBuf b;
+  double *de, *dr, *dout;
+  if (int rc = b.Get(&de, n)) return rc;
+  if (int rc = b.Get(&dr, 3 * size_t(n))) return rc;
+  if (int rc = b.Get(&dout, n)) return rc;
+  CK(cudaMemcpy(de, e, n * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(dr, r, 3 * size_t(n) * sizeof(double), cudaMemcpyHostToDevice));
+  if (precision == DPMX_FP64_PLAIN) CK(LaunchSamplerEval64(t->t64, sampler, imat, de, dr, dout, n, 0));
+  else CK(LaunchSamplerEval32(t->t32, sampler, imat, de, dr, dout, n, 0));
+  CK(cudaMemcpy(out, dout, n * sizeof(double), cudaMemcpyDeviceToHost));
+  return DPMX_OK;
+}
+
+int dpmx_table_eval(const dpmx_tables* t, int precision, int q, int imat, const double* e, double* out, int n) {
+  if (!t || !e || !out || n < 0 || q < 0 || q > 8) return Fail(DPMX_ERR_ARG, "bad table arguments");
+  if (imat < 0 || imat >= t->h.nmat) return Fail(DPMX_ERR_ARG, "bad material index");
+  if (n == 0) return DPMX_OK;
+  DevBuf b;
+  double *de, *dout;
+  if (int rc = b.Get(&de, n)) return rc;
+  if (int rc = b.Get(&dout, n)) return rc;
+  CK(cudaMemcpy(de, e, n * sizeof(double), cudaMemcpyHostToDevice));
+  if (precision == DPMX_FP64_PLAIN) CK(LaunchTableEval64(t->t64, q, imat, de, dout, n, 0));
+  else CK(LaunchTableEval32(t->t32, q, imat, de, dout, n, 0));
+  CK(cudaMemcpy(out, dout, n * sizeof(double), cudaMemcpyDeviceToHost));
+  return DPMX_OK;
+}
+
+// test hook: the FP64 slab workload with per-history deposited energies
+int dpmx_simulate_histories(const dpmx_tables* t, int nprimary, double eprimary, int iselectron, double lbox,
+                            int geom_index, uint64_t seed, double* hist_edep, double* edep_hist, int cap) {
+  if (!t || nprimary < 0 || !hist_edep) return Fail(DPMX_ERR_ARG, "bad arguments");
+  dpmx_phantom* ph = nullptr;
+  if (int rc = dpmx_phantom_slab(t, geom_index, lbox, &ph)) return rc;
+  dpmx_job job;
+  std::memset(&job, 0, sizeof(job));
+  job.phantom = ph;
+  job.source.particle = iselectron ? -1 : 0;
+  job.source.e0 = job.source.e1 = eprimary;
+  job.histories = nprimary;
+  job.seed = seed;
+  std::vector<JobOut> outs;
+  int rc = PrepareOutputs(&job, 1, false, outs);
+  double* d_he = nullptr;
+  if (!rc && cudaMalloc(&d_he, std::max(1, nprimary) * sizeof(double)) != cudaSuccess) rc = Fail(DPMX_ERR_NOMEM, "alloc");
+  double ms = 0;
+  long long nl = 0;
+  if (!rc) rc = RunFp64(t, &job, 1, 1, true, 0, outs, &ms, &nl, d_he);
+  if (!rc || rc == DPMX_ERR_OVERFLOW) {
+    cudaMemcpy(hist_edep, d_he, nprimary * sizeof(double), cudaMemcpyDeviceToHost);
+    if (edep_hist) {
+      std::vector<double> d(outs[0].tallySize);
+      cudaMemcpy(d.data(), outs[0].d_dose, d.size() * sizeof(double), cudaMemcpyDeviceToHost);
+      for (int i = 0; i < std::min<int>(cap, int(d.size())); ++i) edep_hist[i] = d[i];
+    }
+  }
+  cudaFree(d_he);
+  for (auto& o : outs) { cudaFree(o.d_dose); cudaFree(o.d_dose2); cudaFree(o.d_steps); cudaFree(o.d_btally); }
+  dpmx_phantom_free(ph);
+  return rc;
+}
+
+}  // extern "C"

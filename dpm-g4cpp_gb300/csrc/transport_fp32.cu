@@ -1,0 +1,879 @@
+// Event-based FP32 transport with FP64 tallies.
+//
+// Particles of one generation live in SoA queues in HBM. A generation is
+// transported in two phases: all photons (Woodcock tracking), then all
+// electrons/positrons (condensed-history stepping). Each phase is a persistent
+// kernel: every lane holds one particle, advances it one step per loop
+// iteration and, when the particle is finished, refills from the phase's work
+// counter (one atomic per warp per refill). Secondaries are appended to the
+// next generation's queues with warp-aggregated atomics, so photons and
+// electrons never share a warp and lanes stay busy until the queue drains.
+//
+// Geometry is tracked as an integer voxel index plus an FP32 offset inside the
+// voxel, which keeps the 1e-4 mm boundary tolerance of the reference
+// (Geom.hh:107) meaningful at any phantom size. Electron spline tables are
+// staged in shared memory; photon and sampling tables are read through the
+// read-only cache with vector loads. Energy deposits are tallied in FP64
+// (optionally warp-aggregated on equal voxels), and every particle's deposited
+// plus escaped energy is added to its history's FP64 slot once, at the end of
+// the particle, for the per-history energy-conservation check.
+//
+// The physics of each step and interaction is the reference's
+// (SimDPMLike.cc:254-791) evaluated in FP32; the order in which particles of a
+// history are processed differs from the reference's LIFO stack, so results
+// agree with it statistically.
+#include <cooperative_groups.h>
+#include <cooperative_groups/reduce.h>
+
+#include "device_common.cuh"
+#include "kernels.h"
+
+namespace cg = cooperative_groups;
+
+namespace dpmx {
+namespace {
+
+constexpr float kEMC2f = 0.510991f;
+constexpr float kPIf = 3.1415926535897932f;
+constexpr float kTolF = 1.0e-4f;
+constexpr float kHalfTolF = 0.5e-4f;
+constexpr unsigned kFull = 0xffffffffu;
+constexpr unsigned kMaxPhotonSteps = 1u << 22;     // per particle: a lane never loops without bound
+constexpr unsigned kMaxElectronSteps = 1u << 24;
+
+// ---------------------------------------------------------------------------
+// per-particle random numbers: Philox key = job seed, counter =
+// {block, uid_lo, uid_hi, history}; 4 uniforms per block, 23 random bits each
+// on the open interval (0,1)
+// ---------------------------------------------------------------------------
+struct PRng {
+  uint32_t k0, k1, ctr, ulo, uhi, hist;
+  uint4 w;
+  int have;
+  __device__ __forceinline__ void Init(uint32_t a, uint32_t b, uint32_t h, uint32_t lo, uint32_t hi) {
+    k0 = a; k1 = b; hist = h; ulo = lo; uhi = hi; ctr = 0; have = 0;
+  }
+  __device__ __forceinline__ float U() {
+    if (have == 0) {
+      w = philox(make_uint4(ctr++, ulo, uhi, hist), k0, k1);
+      have = 4;
+    }
+    const uint32_t x = w.x;
+    w.x = w.y; w.y = w.z; w.z = w.w;
+    --have;
+    return float((x >> 8) | 1u) * 5.9604644775390625e-8f;
+  }
+  // stream id of the k-th secondary created at the current stream position
+  __device__ __forceinline__ void Child(int k, uint32_t& lo, uint32_t& hi) const {
+    uint64_t z = ((uint64_t(uhi) << 32) | ulo) +
+                 0x9E3779B97F4A7C15ull * (uint64_t(ctr) * 8u + uint64_t(4 - have) * 2u + uint64_t(k) + 1u);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    lo = uint32_t(z);
+    hi = uint32_t(z >> 32);
+  }
+};
+
+// shared-memory copies of the electron spline tables
+struct ETables {
+  SplineT<float> dedx[kMaxMat], itr1[kMaxMat], brem[kMaxMat], k1, moller;
+};
+
+__device__ __forceinline__ SplineT<float> Rebase(const SplineT<float>& s, const float* gbase, float* sbase) {
+  SplineT<float> r = s;
+  r.p = sbase + (s.p - gbase);
+  return r;
+}
+
+// stage the electron tables of T into shared memory (whole block)
+__device__ void StageElectronTables(const DevTables<float>& T, float* sdata, ETables* et) {
+  for (int i = threadIdx.x; i < T.elecCount; i += blockDim.x) sdata[i] = T.elecBase[i];
+  if (threadIdx.x == 0) {
+    for (int m = 0; m < T.nmat; ++m) {
+      et->dedx[m] = Rebase(T.dedx[m], T.elecBase, sdata);
+      et->itr1[m] = Rebase(T.itr1[m], T.elecBase, sdata);
+      et->brem[m] = Rebase(T.brem[m], T.elecBase, sdata);
+    }
+    et->k1 = Rebase(T.k1, T.elecBase, sdata);
+    et->moller = Rebase(T.moller, T.elecBase, sdata);
+  }
+  __syncthreads();
+}
+
+// spline value at e whose log (of the unclamped value) is le
+__device__ __forceinline__ float SplineLe(const SplineT<float>& s, float e, float le) {
+  const float ec = fminf(s.emaxm, fmaxf(s.emin, e));
+  const float lc = (ec == e) ? le : __logf(ec);
+  int il = int((lc - s.logMin) * s.invLogDelta);
+  il = il < 0 ? 0 : (il > s.n - 2 ? s.n - 2 : il);
+  const float* q = s.p + 5 * il;
+  const float xv = ec - q[0];
+  return fmaxf(1.0E-20f, q[1] + xv * (q[2] + xv * (q[3] + xv * q[4])));
+}
+
+// ---------------------------------------------------------------------------
+// queues
+// ---------------------------------------------------------------------------
+struct PState {           // a particle as stored in a queue
+  int ix, iy, iz;
+  float lx, ly, lz, dx, dy, dz, e;
+  uint32_t hist, slot, ulo, uhi, meta;   // meta: type (2 bits: 0 photon, 1 e-, 2 e+) | job << 2
+};
+
+__device__ __forceinline__ uint32_t PackVox(int ix, int iy, int iz) {
+  return uint32_t(ix) | (uint32_t(iy) << 11) | (uint32_t(iz) << 22);
+}
+
+__device__ __forceinline__ void LoadParticle(const Queue& q, unsigned long long i, PState& p) {
+  const uint32_t v = q.vox[i];
+  p.ix = int(v & 0x7ffu); p.iy = int((v >> 11) & 0x7ffu); p.iz = int(v >> 22);
+  p.lx = q.lx[i]; p.ly = q.ly[i]; p.lz = q.lz[i];
+  p.dx = q.dx[i]; p.dy = q.dy[i]; p.dz = q.dz[i];
+  p.e = q.e[i];
+  p.hist = q.hist[i]; p.slot = q.slot[i]; p.ulo = q.uidlo[i]; p.uhi = q.uidhi[i]; p.meta = q.meta[i];
+}
+
+// appends p to q with one atomic per group of converged lanes; returns false
+// (and counts the overflow) when the queue is full
+__device__ __forceinline__ bool Append(const Queue& q, unsigned long long* count, unsigned long long* overflow,
+                                       const PState& p) {
+  cg::coalesced_group g = cg::coalesced_threads();
+  unsigned long long base = 0;
+  if (g.thread_rank() == 0) base = atomicAdd(count, (unsigned long long)g.size());
+  base = g.shfl(base, 0);
+  const unsigned long long i = base + g.thread_rank();
+  if (i >= q.capacity) {
+    atomicAdd(overflow, 1ull);
+    return false;
+  }
+  q.vox[i] = PackVox(p.ix, p.iy, p.iz);
+  q.lx[i] = p.lx; q.ly[i] = p.ly; q.lz[i] = p.lz;
+  q.dx[i] = p.dx; q.dy[i] = p.dy; q.dz[i] = p.dz;
+  q.e[i] = p.e;
+  q.hist[i] = p.hist; q.slot[i] = p.slot; q.uidlo[i] = p.ulo; q.uidhi[i] = p.uhi; q.meta[i] = p.meta;
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// tallies
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void Score(const JobF& J, int ix, int iy, int iz, uint32_t hist, float e, int agg) {
+  const long long idx = J.tallyDepth ? (long long)iz : ((long long)iz * J.ny + iy) * J.nx + ix;
+  double* ptr = J.tally + idx;
+  const double de = double(e);
+  if (agg) {
+    cg::coalesced_group g = cg::coalesced_threads();
+    cg::coalesced_group peers = cg::labeled_partition(g, (unsigned long long)ptr);
+    const double sum = cg::reduce(peers, de, cg::plus<double>());
+    if (peers.thread_rank() == 0) atomicAdd(ptr, sum);
+  } else {
+    atomicAdd(ptr, de);
+  }
+  if (J.steps) atomicAdd(J.steps + iz, 1.0);
+  if (J.btally) {
+    const long long nvox = (long long)J.nx * J.ny * J.nz;
+    atomicAdd(J.btally + (long long)(hist % uint32_t(J.nbeamlets)) * nvox + idx, de);
+  }
+}
+
+__device__ __forceinline__ bool InBox(const JobF& J, int ix, int iy, int iz) {
+  return (unsigned)ix < (unsigned)J.nx && (unsigned)iy < (unsigned)J.ny && (unsigned)iz < (unsigned)J.nz;
+}
+
+__device__ __forceinline__ int MaterialAt(const JobF& J, int ix, int iy, int iz) {
+  const uint8_t m = J.matByDepth ? __ldg(J.mat + iz) : __ldg(J.mat + ((long long)iz * J.ny + iy) * J.nx + ix);
+  return m == kVacuum ? -1 : int(m);
+}
+
+// Distance to the voxel walls along d. A face closer than half the tolerance
+// ahead is crossed first (the push of Geom::DistanceToBoundary, Geom.cc:46-52).
+// Returns false when the particle leaves the box.
+__device__ __forceinline__ bool Settle(const JobF& J, PState& p, float& s, int& axis) {
+  for (int it = 0; it < 6; ++it) {
+    float sx = 1.0e20f, sy = 1.0e20f, sz = 1.0e20f;
+    if (p.dx > 0.f) {
+      const float pd = J.vx - p.lx;
+      if (pd < kHalfTolF) { ++p.ix; p.lx = 0.f; if (p.ix >= J.nx) return false; continue; }
+      sx = pd / p.dx;
+    } else if (p.dx < 0.f) {
+      const float pd = p.lx;
+      if (pd < kHalfTolF) { --p.ix; p.lx = J.vx; if (p.ix < 0) return false; continue; }
+      sx = -pd / p.dx;
+    }
+    if (p.dy > 0.f) {
+      const float pd = J.vy - p.ly;
+      if (pd < kHalfTolF) { ++p.iy; p.ly = 0.f; if (p.iy >= J.ny) return false; continue; }
+      sy = pd / p.dy;
+    } else if (p.dy < 0.f) {
+      const float pd = p.ly;
+      if (pd < kHalfTolF) { --p.iy; p.ly = J.vy; if (p.iy < 0) return false; continue; }
+      sy = -pd / p.dy;
+    }
+    if (p.dz > 0.f) {
+      const float pd = J.vz - p.lz;
+      if (pd < kHalfTolF) { ++p.iz; p.lz = 0.f; if (p.iz >= J.nz) return false; continue; }
+      sz = pd / p.dz;
+    } else if (p.dz < 0.f) {
+      const float pd = p.lz;
+      if (pd < kHalfTolF) { --p.iz; p.lz = J.vz; if (p.iz < 0) return false; continue; }
+      sz = -pd / p.dz;
+    }
+    s = sx; axis = 0;
+    if (sy < s) { s = sy; axis = 1; }
+    if (sz < s) { s = sz; axis = 2; }
+    return true;
+  }
+  return false;
+}
+
+// move s along d, crossing the face of `axis` exactly when the step is
+// geometry limited; false when the particle leaves the box
+__device__ __forceinline__ bool MoveToFace(const JobF& J, PState& p, float s, int axis) {
+  if (axis != 0) p.lx += s * p.dx;
+  if (axis != 1) p.ly += s * p.dy;
+  if (axis != 2) p.lz += s * p.dz;
+  if (axis == 0) { if (p.dx > 0.f) { ++p.ix; p.lx = 0.f; } else { --p.ix; p.lx = J.vx; } }
+  else if (axis == 1) { if (p.dy > 0.f) { ++p.iy; p.ly = 0.f; } else { --p.iy; p.ly = J.vy; } }
+  else { if (p.dz > 0.f) { ++p.iz; p.lz = 0.f; } else { --p.iz; p.lz = J.vz; } }
+  return InBox(J, p.ix, p.iy, p.iz);
+}
+
+// free flight of s (photons): may cross many voxels
+__device__ __forceinline__ bool Fly(const JobF& J, PState& p, float s) {
+  const float gx = p.lx + s * p.dx, gy = p.ly + s * p.dy, gz = p.lz + s * p.dz;
+  // (clamped so that a very long flight cannot overflow the integer voxel index)
+  const int kx = int(fmaxf(-1.0e6f, fminf(1.0e6f, floorf(gx * J.ivx))));
+  const int ky = int(fmaxf(-1.0e6f, fminf(1.0e6f, floorf(gy * J.ivy))));
+  const int kz = int(fmaxf(-1.0e6f, fminf(1.0e6f, floorf(gz * J.ivz))));
+  p.ix += kx; p.iy += ky; p.iz += kz;
+  p.lx = gx - float(kx) * J.vx;
+  p.ly = gy - float(ky) * J.vy;
+  p.lz = gz - float(kz) * J.vz;
+  return InBox(J, p.ix, p.iy, p.iz);
+}
+
+// ---------------------------------------------------------------------------
+// primaries
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int FindSegment(const Segment* segs, int n, long long i) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (segs[mid].prefix <= i) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ void MakePrimary(const PhaseArgs& a, const Segment* segs, long long i, PState& p, PRng& rng) {
+  const Segment& sg = segs[FindSegment(segs, a.nsegs, i)];
+  const JobF& J = a.jobs[sg.job];
+  const long long h = sg.firstHist + (i - sg.prefix);
+  p.hist = uint32_t(h);
+  p.slot = uint32_t(sg.slotBase + (i - sg.prefix));
+  p.ulo = 0; p.uhi = 0;
+  rng.Init(J.k0, J.k1, p.hist, 0u, 0u);
+  double x = J.cx, y = J.cy;
+  if (J.shape == 1) {
+    x = J.cx + (rng.U() - 0.5f) * J.fx;
+    y = J.cy + (rng.U() - 0.5f) * J.fy;
+  } else if (J.shape == 2) {
+    const int b = int(h % (long long)(J.nbx * J.nby));
+    const int bx = b % J.nbx, by = b / J.nbx;
+    x = J.cx + (bx - 0.5f * J.nbx) * J.fx + rng.U() * J.fx;
+    y = J.cy + (by - 0.5f * J.nby) * J.fy + rng.U() * J.fy;
+  }
+  float e = J.e0;
+  if (J.spectrum == 1) e = J.e0 + rng.U() * (J.e1 - J.e0);
+  else if (J.spectrum == 2) e = J.e1 - (J.e1 - J.e0) * sqrtf(1.0f - rng.U());
+  // entry plane z = z0 (face of the first voxel layer); x, y relative to the box
+  const double rx = (x - J.x0) * J.ivx, ry = (y - J.y0) * J.ivy;
+  p.ix = int(floor(rx)); p.iy = int(floor(ry)); p.iz = 0;
+  p.lx = float((x - J.x0) - p.ix * double(J.vx));
+  p.ly = float((y - J.y0) - p.iy * double(J.vy));
+  p.lz = 0.f;
+  p.dx = 0.f; p.dy = 0.f; p.dz = 1.f;
+  p.e = e;
+  p.meta = (J.particle == 0 ? 0u : 1u) | (uint32_t(sg.job) << 2);
+  a.histE0[p.slot] = double(e);
+}
+
+// ---------------------------------------------------------------------------
+// photon phase: Woodcock tracking (SimDPMLike.cc:463-635)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) PhotonPhase(PhaseArgs a) {
+  __shared__ JobF sjobs[16];
+  const bool fewJobs = a.njobs <= 16;
+  if (fewJobs) {
+    for (int j = threadIdx.x; j < a.njobs; j += blockDim.x) sjobs[j] = a.jobs[j];
+    __syncthreads();
+  }
+  const JobF* jobs = fewJobs ? sjobs : a.jobs;
+  const unsigned long long nQ = *a.inCount;
+  const unsigned long long total = (unsigned long long)a.nPrimaries + nQ;
+  if (total == 0) return;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const DevTables<float>& T = a.T;
+
+  bool active = false, exhausted = false;
+  PState p;
+  PRng rng;
+  double acc = 0.0;
+  unsigned pst = 0;
+  for (;;) {
+    const unsigned need = __ballot_sync(kFull, !active);
+    if (need && !exhausted) {
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(a.head, (unsigned long long)__popc(need));
+      base = __shfl_sync(kFull, base, 0);
+      if (base + __popc(need) >= total) exhausted = true;
+      if (!active) {
+        const unsigned long long my = base + __popc(need & lt);
+        if (my < total) {
+          if (my < (unsigned long long)a.nPrimaries) {
+            MakePrimary(a, a.segs, (long long)my, p, rng);
+          } else {
+            LoadParticle(a.in, my - a.nPrimaries, p);
+            const JobF& J = jobs[p.meta >> 2];
+            rng.Init(J.k0, J.k1, p.hist, p.ulo, p.uhi);
+          }
+          acc = 0.0;
+          pst = 0;
+          active = true;
+          const JobF& J = jobs[p.meta >> 2];
+          if (!InBox(J, p.ix, p.iy, p.iz) || MaterialAt(J, p.ix, p.iy, p.iz) < 0) {
+            acc += p.e;
+            atomicAdd(&J.cnt->escaped, double(p.e));
+            atomicAdd(a.histE + p.slot, acc);
+            active = false;
+          }
+        }
+      }
+    }
+    if (!__any_sync(kFull, active)) break;
+    if (!active) continue;
+
+    // one Woodcock step
+    const int job = int(p.meta >> 2);
+    const JobF& J = jobs[job];
+    bool done = false;
+    if (++pst > kMaxPhotonSteps) {   // cannot happen for finite cross sections; bounded anyway
+      acc += p.e;
+      atomicAdd(&J.cnt->lost, 1ull);
+      atomicAdd(a.histE + p.slot, acc);
+      active = false;
+      continue;
+    }
+    const float lmax = 1.0f / LinearGet(T.imfpMax, p.e);
+    const float step = -lmax * __logf(rng.U());
+    int im = -1;
+    if (Fly(J, p, step)) im = MaterialAt(J, p.ix, p.iy, p.iz);
+    if (im < 0) {
+      acc += p.e;
+      atomicAdd(&J.cnt->escaped, double(p.e));
+      done = true;
+    } else {
+      const float rho = T.density[im];
+      const float r1 = rng.U();
+      float prob = 1.0f - LinearGet(T.tot[im], p.e) * rho * lmax;
+      if (r1 >= prob) {
+        prob += LinearGet(T.comp[im], p.e) * rho * lmax;
+        if (r1 < prob) {
+          // Compton (SimDPMLike.cc:512-570)
+          const float a3 = rng.U(), a2 = rng.U(), a1 = rng.U();
+          const float eps = SampleKN(T.kn, p.e, a1, a2, a3);
+          const float kappa = p.e * (1.0f / kEMC2f);
+          const float phCost = 1.0f - (1.0f - eps) / (eps * kappa);
+          const float phE = eps * p.e;
+          const float phPhi = 2.0f * kPIf * rng.U();
+          const float elE = p.e - phE;
+          float sn, cs;
+          __sincosf(phPhi, &sn, &cs);
+          if (elE < T.ecut) {
+            Score(J, p.ix, p.iy, p.iz, p.hist, elE, a.aggregate);
+            acc += elE;
+          } else {
+            const float e0 = kappa;
+            const float elCost = (1.0f + e0) * sqrtf((1.0f - eps) / (e0 * (2.0f + e0 * (1.0f - eps))));
+            const float sint = sqrtf(fmaxf(0.f, (1.0f + elCost) * (1.0f - elCost)));
+            PState c = p;
+            c.dx = -sint * cs; c.dy = -sint * sn; c.dz = elCost;   // phi + pi
+            RotateToLab(c.dx, c.dy, c.dz, p.dx, p.dy, p.dz);
+            c.e = elE;
+            c.meta = 1u | (p.meta & ~3u);
+            rng.Child(0, c.ulo, c.uhi);
+            if (!Append(a.outE, a.outECount, a.overflow, c)) acc += elE;
+          }
+          p.e = phE;
+          if (p.e < T.gcut) {
+            Score(J, p.ix, p.iy, p.iz, p.hist, p.e, a.aggregate);
+            acc += p.e;
+            done = true;
+          } else {
+            const float phSint = sqrtf(fmaxf(0.f, (1.0f - phCost) * (1.0f + phCost)));
+            float u1 = phSint * cs, u2 = phSint * sn, u3 = phCost;
+            RotateToLab(u1, u2, u3, p.dx, p.dy, p.dz);
+            p.dx = u1; p.dy = u2; p.dz = u3;
+          }
+        } else {
+          prob += LinearGet(T.pair[im], p.e) * rho * lmax;
+          if (r1 < prob && p.e > 2.0f * kEMC2f) {
+            // pair production (SimDPMLike.cc:573-627)
+            const float sum = p.e - 2.0f * kEMC2f;
+            const float e1 = rng.U() * sum;
+            const float e2 = sum - e1;
+            if (e2 < T.ecut) {
+              Score(J, p.ix, p.iy, p.iz, p.hist, e2, a.aggregate);
+              acc += e2;
+            } else {
+              PState c = p;
+              c.e = e2; c.meta = 1u | (p.meta & ~3u);
+              rng.Child(0, c.ulo, c.uhi);
+              if (!Append(a.outE, a.outECount, a.overflow, c)) acc += e2;
+            }
+            if (e1 < T.ecut) {
+              Score(J, p.ix, p.iy, p.iz, p.hist, e1, a.aggregate);
+              acc += e1;
+              // annihilation at rest (SimDPMLike.cc:753-791)
+              const float cost = 1.0f - 2.0f * rng.U();
+              const float sint = sqrtf(fmaxf(0.f, (1.0f - cost) * (1.0f + cost)));
+              const float phi = 2.0f * kPIf * rng.U();
+              float s2, c2;
+              __sincosf(phi, &s2, &c2);
+              PState g = p;
+              g.e = kEMC2f; g.meta = 0u | (p.meta & ~3u);
+              g.dx = sint * c2; g.dy = sint * s2; g.dz = cost;
+              rng.Child(0, g.ulo, g.uhi);
+              if (!Append(a.outP, a.outPCount, a.overflow, g)) acc += kEMC2f;
+              g.dx = -g.dx; g.dy = -g.dy; g.dz = -g.dz;
+              rng.Child(1, g.ulo, g.uhi);
+              if (!Append(a.outP, a.outPCount, a.overflow, g)) acc += kEMC2f;
+            } else {
+              PState c = p;
+              c.e = e1; c.meta = 2u | (p.meta & ~3u);
+              rng.Child(1, c.ulo, c.uhi);
+              if (!Append(a.outE, a.outECount, a.overflow, c)) acc += e1 + 2.0f * kEMC2f;
+            }
+            done = true;
+          } else if (r1 < prob) {
+            // below threshold (pair IMFP floor): treated as photoelectric
+            Score(J, p.ix, p.iy, p.iz, p.hist, p.e, a.aggregate);
+            acc += p.e;
+            done = true;
+          } else {
+            // photoelectric absorption
+            Score(J, p.ix, p.iy, p.iz, p.hist, p.e, a.aggregate);
+            acc += p.e;
+            done = true;
+          }
+        }
+      }
+    }
+    if (done) {
+      atomicAdd(a.histE + p.slot, acc);
+      active = false;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// electron phase: condensed-history stepping (SimDPMLike.cc:81-460)
+// ---------------------------------------------------------------------------
+struct EState {
+  float nTr1, nTr10, nMol, invMol, nBrem, ekin0, sGeom;
+  int axis;
+  bool hinge, needGeom;
+};
+
+__device__ __forceinline__ void InitElectron(const ETables& et, const PState& p, PRng& rng, EState& s) {
+  // SimDPMLike.cc:113-146
+  s.hinge = true;
+  s.ekin0 = p.e;
+  const float le = __logf(p.e);
+  s.nTr1 = SplineLe(et.k1, p.e, le);
+  s.nTr10 = rng.U() * s.nTr1;
+  s.nTr1 -= s.nTr10;
+  s.nMol = -__logf(rng.U());
+  s.invMol = SplineLe(et.moller, p.e, le);
+  s.nBrem = -__logf(rng.U());
+  s.needGeom = true;
+}
+
+__global__ void __launch_bounds__(256) ElectronPhase(PhaseArgs a) {
+  extern __shared__ float sdata[];
+  __shared__ ETables et;
+  __shared__ JobF sjobs[16];
+  const bool fewJobs = a.njobs <= 16;
+  if (fewJobs)
+    for (int j = threadIdx.x; j < a.njobs; j += blockDim.x) sjobs[j] = a.jobs[j];
+  StageElectronTables(a.T, sdata, &et);
+  const JobF* jobs = fewJobs ? sjobs : a.jobs;
+  const unsigned long long nQ = *a.inCount;
+  const unsigned long long total = (unsigned long long)a.nPrimaries + nQ;
+  if (total == 0) return;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const DevTables<float>& T = a.T;
+  const float ecut = T.ecut, gcut = T.gcut;
+
+  bool active = false, exhausted = false;
+  PState p;
+  PRng rng;
+  EState s;
+  double acc = 0.0;
+  unsigned pst = 0;
+  unsigned long long nsteps = 0;
+  for (;;) {
+    const unsigned need = __ballot_sync(kFull, !active);
+    if (need && !exhausted) {
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(a.head, (unsigned long long)__popc(need));
+      base = __shfl_sync(kFull, base, 0);
+      if (base + __popc(need) >= total) exhausted = true;
+      if (!active) {
+        const unsigned long long my = base + __popc(need & lt);
+        if (my < total) {
+          if (my < (unsigned long long)a.nPrimaries) {
+            MakePrimary(a, a.segs, (long long)my, p, rng);
+          } else {
+            LoadParticle(a.in, my - a.nPrimaries, p);
+            const JobF& J = jobs[p.meta >> 2];
+            rng.Init(J.k0, J.k1, p.hist, p.ulo, p.uhi);
+          }
+          acc = 0.0;
+          pst = 0;
+          active = true;
+          const JobF& J = jobs[p.meta >> 2];
+          if (!InBox(J, p.ix, p.iy, p.iz) || MaterialAt(J, p.ix, p.iy, p.iz) < 0) {
+            acc += p.e + ((p.meta & 3u) == 2u ? 2.0f * kEMC2f : 0.f);
+            atomicAdd(&J.cnt->escaped, acc);
+            atomicAdd(a.histE + p.slot, acc);
+            active = false;
+          } else {
+            InitElectron(et, p, rng, s);
+          }
+        }
+      }
+    }
+    if (!__any_sync(kFull, active)) break;
+    if (!active) continue;
+
+    // ---- one condensed-history sub-step (SimDPMLike.cc:273-458) ----
+    const int job = int(p.meta >> 2);
+    const JobF& J = jobs[job];
+    const bool positron = (p.meta & 3u) == 2u;
+    bool done = false;
+    int im = -1;
+    if (s.needGeom) {
+      if (Settle(J, p, s.sGeom, s.axis)) im = MaterialAt(J, p.ix, p.iy, p.iz);
+      s.needGeom = false;
+    } else {
+      im = MaterialAt(J, p.ix, p.iy, p.iz);
+    }
+    if (im < 0) {
+      const float esc = p.e + (positron ? 2.0f * kEMC2f : 0.f);
+      acc += esc;
+      atomicAdd(&J.cnt->escaped, double(esc));
+      done = true;
+    } else if (++pst > kMaxElectronSteps) {   // bounded: every step loses energy or moves >= 5e-5 mm
+      acc += p.e + (positron ? 2.0f * kEMC2f : 0.f);
+      atomicAdd(&J.cnt->lost, 1ull);
+      done = true;
+    } else {
+      ++nsteps;
+      const float rho = T.density[im];
+      float step = s.sGeom;
+      int what = 0;
+      const float le = __logf(p.e);
+      float dedx = SplineLe(et.dedx[im], p.e, le) * rho;
+      float emid = fmaxf(p.e - 0.5f * step * dedx, ecut);
+      float lm = __logf(emid);
+      float dTr1 = SplineLe(et.itr1[im], emid, lm) * rho;
+      const float dMol = s.invMol * T.mollerScale[im] * rho;
+      const float dBrem = SplineLe(et.brem[im], emid, lm) * rho;
+      const float sBrem = s.nBrem / dBrem;
+      if (sBrem < step) { step = sBrem; what = 1; }
+      const float sMol = s.nMol / dMol;
+      if (sMol < step) { step = sMol; what = 2; }
+      float sEl = s.nTr1 / dTr1;
+      if (sEl < step) {
+        sEl = s.nTr1 / (SplineLe(et.itr1[im], p.e, le) * rho);
+        emid = fmaxf(p.e - 0.5f * sEl * dedx, ecut);
+        dTr1 = SplineLe(et.itr1[im], emid, __logf(emid)) * rho;
+        sEl = fminf(step, s.nTr1 / dTr1);
+        step = sEl;
+        what = 3;
+      }
+      s.nBrem = (what == 1) ? 0.f : s.nBrem - step * dBrem;
+      s.nMol = (what == 2) ? 0.f : s.nMol - step * dMol;
+      s.nTr1 = (what == 3) ? 0.f : s.nTr1 - step * dTr1;
+      emid = fmaxf(p.e - 0.5f * step * dedx, ecut);
+      dedx = SplineLe(et.dedx[im], emid, __logf(emid)) * rho;
+      const float de = step * dedx;
+      const float ef = p.e - de;
+      if (ef < ecut) {
+        // stops in this step: deposit all (SimDPMLike.cc:401-422)
+        const float edep = p.e;
+        p.e = 0.f;
+        if (!positron) {
+          Score(J, p.ix, p.iy, p.iz, p.hist, edep, a.aggregate);
+          acc += edep;
+        } else {
+          // e+: move to the end of the step, annihilate there
+          bool inside;
+          if (what == 0) inside = MoveToFace(J, p, step, s.axis);
+          else { p.lx += step * p.dx; p.ly += step * p.dy; p.lz += step * p.dz; inside = true; }
+          const int im2 = inside ? MaterialAt(J, p.ix, p.iy, p.iz) : -1;
+          if (im2 < 0) {
+            acc += edep + 2.0f * kEMC2f;
+            atomicAdd(&J.cnt->escaped, double(edep + 2.0f * kEMC2f));
+          } else {
+            const float cost = 1.0f - 2.0f * rng.U();
+            const float sint = sqrtf(fmaxf(0.f, (1.0f - cost) * (1.0f + cost)));
+            const float phi = 2.0f * kPIf * rng.U();
+            float sn, cs;
+            __sincosf(phi, &sn, &cs);
+            PState g = p;
+            g.e = kEMC2f; g.meta = 0u | (p.meta & ~3u);
+            g.dx = sint * cs; g.dy = sint * sn; g.dz = cost;
+            rng.Child(0, g.ulo, g.uhi);
+            if (!Append(a.outP, a.outPCount, a.overflow, g)) acc += kEMC2f;
+            g.dx = -g.dx; g.dy = -g.dy; g.dz = -g.dz;
+            rng.Child(1, g.ulo, g.uhi);
+            if (!Append(a.outP, a.outPCount, a.overflow, g)) acc += kEMC2f;
+            Score(J, p.ix, p.iy, p.iz, p.hist, edep, a.aggregate);
+            acc += edep;
+          }
+        }
+        done = true;
+      } else {
+        p.e = ef;
+        // score in the voxel of the step, then move
+        Score(J, p.ix, p.iy, p.iz, p.hist, de, a.aggregate);
+        acc += de;
+        if (what == 0) {
+          if (!MoveToFace(J, p, step, s.axis)) {
+            acc += p.e + (positron ? 2.0f * kEMC2f : 0.f);
+            atomicAdd(&J.cnt->escaped, double(p.e + (positron ? 2.0f * kEMC2f : 0.f)));
+            done = true;
+          } else if (!Settle(J, p, s.sGeom, s.axis)) {
+            acc += p.e + (positron ? 2.0f * kEMC2f : 0.f);
+            atomicAdd(&J.cnt->escaped, double(p.e + (positron ? 2.0f * kEMC2f : 0.f)));
+            done = true;
+          }
+        } else {
+          p.lx += step * p.dx; p.ly += step * p.dy; p.lz += step * p.dz;
+          s.needGeom = true;
+          // the interaction (SimDPMLike.cc:169-244)
+          if (what == 1) {
+            if (p.e > gcut) {
+              // bremsstrahlung photon (SimDPMLike.cc:661-695)
+              const float r3 = rng.U(), r2 = rng.U(), r1 = rng.U();
+              const float eg = SampleSB(T.sb[im], p.e, r1, r2, r3);
+              const float dum0 = (kEMC2f * 0.7071067812f) / (p.e + kEMC2f);
+              const float cost = fmaxf(-1.0f, fminf(1.0f, 1.0f - dum0 * dum0));
+              const float sint = sqrtf(fmaxf(0.f, (1.0f + cost) * (1.0f - cost)));
+              const float phi = 2.0f * kPIf * rng.U();
+              float sn, cs;
+              __sincosf(phi, &sn, &cs);
+              PState g = p;
+              g.e = eg; g.meta = 0u | (p.meta & ~3u);
+              g.dx = sint * cs; g.dy = sint * sn; g.dz = cost;
+              RotateToLab(g.dx, g.dy, g.dz, p.dx, p.dy, p.dz);
+              rng.Child(0, g.ulo, g.uhi);
+              if (!Append(a.outP, a.outPCount, a.overflow, g)) acc += eg;
+              p.e -= eg;
+            }
+            if (p.e < ecut) {
+              Score(J, p.ix, p.iy, p.iz, p.hist, p.e, a.aggregate);
+              acc += p.e;
+              if (positron) {
+                const float cost = 1.0f - 2.0f * rng.U();
+                const float sint = sqrtf(fmaxf(0.f, (1.0f - cost) * (1.0f + cost)));
+                const float phi = 2.0f * kPIf * rng.U();
+                float sn, cs;
+                __sincosf(phi, &sn, &cs);
+                PState g = p;
+                g.e = kEMC2f; g.meta = 0u | (p.meta & ~3u);
+                g.dx = sint * cs; g.dy = sint * sn; g.dz = cost;
+                rng.Child(0, g.ulo, g.uhi);
+                if (!Append(a.outP, a.outPCount, a.overflow, g)) acc += kEMC2f;
+                g.dx = -g.dx; g.dy = -g.dy; g.dz = -g.dz;
+                rng.Child(1, g.ulo, g.uhi);
+                if (!Append(a.outP, a.outPCount, a.overflow, g)) acc += kEMC2f;
+              }
+              p.e = 0.f;
+              done = true;
+            } else {
+              s.nBrem = -__logf(rng.U());
+            }
+          } else if (what == 2) {
+            if (p.e > 2.0f * ecut) {
+              // Moller delta electron (SimDPMLike.cc:699-728)
+              const float r3 = rng.U(), r2 = rng.U(), r1 = rng.U();
+              const float se = SampleMoller(T.mol, p.e, r1, r2, r3);
+              const float k2 = 2.0f * kEMC2f;
+              const float cost = fminf(1.0f, sqrtf(se * (p.e + k2) / (p.e * (se + k2))));
+              const float sint = sqrtf(fmaxf(0.f, (1.0f + cost) * (1.0f - cost)));
+              const float phi = 2.0f * kPIf * rng.U();
+              float sn, cs;
+              __sincosf(phi, &sn, &cs);
+              PState c = p;
+              c.e = se; c.meta = 1u | (p.meta & ~3u);
+              c.dx = sint * cs; c.dy = sint * sn; c.dz = cost;
+              RotateToLab(c.dx, c.dy, c.dz, p.dx, p.dy, p.dz);
+              rng.Child(0, c.ulo, c.uhi);
+              if (!Append(a.outE, a.outECount, a.overflow, c)) acc += se;
+              p.e -= se;
+            }
+            s.nMol = -__logf(rng.U());
+            s.invMol = SplineLe(et.moller, p.e, __logf(p.e));
+          } else if (what == 3) {
+            if (s.hinge) {
+              // GS angular deflection at the hinge (SimDPMLike.cc:731-750)
+              const float r2 = rng.U(), r1 = rng.U();
+              const float d = SampleGS(T.gs, s.ekin0, r1, r2);
+              const float cost = fmaxf(-1.0f, fminf(1.0f, d));
+              const float sint = sqrtf(fmaxf(0.f, (1.0f - cost) * (1.0f + cost)));
+              const float phi = 2.0f * kPIf * rng.U();
+              float sn, cs;
+              __sincosf(phi, &sn, &cs);
+              float u1 = sint * cs, u2 = sint * sn, u3 = cost;
+              RotateToLab(u1, u2, u3, p.dx, p.dy, p.dz);
+              const float inv = rsqrtf(u1 * u1 + u2 * u2 + u3 * u3);
+              p.dx = u1 * inv; p.dy = u2 * inv; p.dz = u3 * inv;
+              s.nTr1 = s.nTr10;
+              s.hinge = false;
+            } else {
+              s.ekin0 = p.e;
+              s.nTr1 = SplineLe(et.k1, p.e, __logf(p.e));
+              s.nTr10 = rng.U() * s.nTr1;
+              s.nTr1 -= s.nTr10;
+              s.hinge = true;
+            }
+          }
+        }
+      }
+    }
+    if (done) {
+      atomicAdd(a.histE + p.slot, acc);
+      active = false;
+    }
+  }
+  // step counters: one atomic per warp
+  for (int o = 16; o > 0; o >>= 1) nsteps += __shfl_down_sync(kFull, nsteps, o);
+  if (lane == 0 && a.njobs > 0) atomicAdd(&a.jobs[0].cnt->steps, nsteps);
+}
+
+__global__ void FoldKernel(double* t, double* dose, double* dose2, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double v = t[i];
+    if (v != 0.0) {
+      dose[i] += v;
+      dose2[i] += v * v;
+      t[i] = 0.0;
+    }
+  }
+}
+
+__global__ void EnergyCheckKernel(const double* histE, const double* histE0, long long nslots, const Segment* segs,
+                                  int nsegs, const JobF* jobs) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nslots;
+       i += (long long)gridDim.x * blockDim.x) {
+    // slots are laid out segment after segment
+    int lo = 0, hi = nsegs - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (segs[mid].slotBase <= i) lo = mid; else hi = mid - 1;
+    }
+    const JobF& J = jobs[segs[lo].job];
+    const double e0 = histE0[i];
+    const double res = fabs(e0 - histE[i]);
+    atomicAdd(&J.cnt->primaryEnergy, e0);
+    atomicAdd(&J.cnt->histories, 1ull);
+    atomicMax(&J.cnt->maxResidualBits, (unsigned long long)__double_as_longlong(res));
+    if (res > 1.0e-3 * e0) atomicAdd(&J.cnt->violations, 1ull);
+  }
+}
+
+__global__ void SamplerKernel32(DevTables<float> T, int s, int imat, const double* e, const double* r, double* out,
+                                int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float ei = float(e[i]);
+  const float u0 = float(r[3 * i]), u1 = float(r[3 * i + 1]), u2 = float(r[3 * i + 2]);
+  float v = 0.f;
+  switch (s) {
+    case 0: v = SampleKN(T.kn, ei, u0, u1, u2); break;
+    case 1: v = SampleMoller(T.mol, ei, u0, u1, u2); break;
+    case 2: v = SampleSB(T.sb[imat], ei, u0, u1, u2); break;
+    case 3: v = SampleGS(T.gs, ei, u0, u1); break;
+    default: break;
+  }
+  out[i] = double(v);
+}
+
+__global__ void TableKernel32(DevTables<float> T, int q, int imat, const double* e, double* out, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float ei = float(e[i]);
+  const float le = __logf(ei);
+  float v = 0.f;
+  switch (q) {
+    case 0: v = SplineLe(T.dedx[imat], ei, le); break;
+    case 1: v = SplineLe(T.itr1[imat], ei, le); break;
+    case 2: v = SplineLe(T.brem[imat], ei, le); break;
+    case 3: v = SplineLe(T.moller, ei, le); break;
+    case 4: v = SplineLe(T.k1, ei, le); break;
+    case 5: v = LinearGet(T.imfpMax, ei); break;
+    case 6: v = LinearGet(T.tot[imat], ei); break;
+    case 7: v = LinearGet(T.comp[imat], ei); break;
+    case 8: v = LinearGet(T.pair[imat], ei); break;
+    default: break;
+  }
+  out[i] = double(v);
+}
+
+}  // namespace
+
+int ElectronPhaseSmemBytes(const DevTables<float>& T) { return int(T.elecCount * sizeof(float)); }
+
+cudaError_t LaunchPhotonPhase(const PhaseArgs& a, int blocks, int threads, cudaStream_t st) {
+  PhotonPhase<<<blocks, threads, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t LaunchElectronPhase(const PhaseArgs& a, int blocks, int threads, cudaStream_t st) {
+  const int smem = ElectronPhaseSmemBytes(a.T);
+  ElectronPhase<<<blocks, threads, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t LaunchFold(double* t, double* dose, double* dose2, long long n, cudaStream_t st) {
+  const int blocks = int(std::min<long long>((n + 255) / 256, 152LL * 16));
+  FoldKernel<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(t, dose, dose2, n);
+  return cudaGetLastError();
+}
+
+cudaError_t LaunchEnergyCheck(const double* histE, const double* histE0, long long nslots, const Segment* segs,
+                              int nsegs, const JobF* jobs, cudaStream_t st) {
+  if (nslots <= 0) return cudaSuccess;
+  const int blocks = int(std::min<long long>((nslots + 255) / 256, 152LL * 16));
+  EnergyCheckKernel<<<blocks, 256, 0, st>>>(histE, histE0, nslots, segs, nsegs, jobs);
+  return cudaGetLastError();
+}
+
+cudaError_t LaunchSamplerEval32(const DevTables<float>& T, int s, int imat, const double* e, const double* r,
+                                double* out, int n, cudaStream_t st) {
+  SamplerKernel32<<<(n + 127) / 128, 128, 0, st>>>(T, s, imat, e, r, out, n);
+  return cudaGetLastError();
+}
+
+cudaError_t LaunchTableEval32(const DevTables<float>& T, int q, int imat, const double* e, double* out, int n,
+                              cudaStream_t st) {
+  TableKernel32<<<(n + 127) / 128, 128, 0, st>>>(T, q, imat, e, out, n);
+  return cudaGetLastError();
+}
+
+}  // namespace dpmx

@@ -1,0 +1,187 @@
+/*
+ * dpmx.h - C ABI of the GB300-native dpm_Simulate transport library
+ * (libdpmx.so). Plain pointers and sizes only; every call returns an int
+ * status (DPMX_OK = 0, negative on error) and dpmx_last_error() gives the
+ * message of the calling thread's last failure. Nothing in the library exits
+ * or aborts the process.
+ *
+ * The calls replace these reference interfaces (paths inside bl406/dpm-g4cpp):
+ *   dpmx_tables_load      SimElectronData::Load, SimPhotonData::Load,
+ *                         SimMaterialData::Load (dpm_Simulate.cc:71-78,
+ *                         SimElectronData.cc:44-115, SimPhotonData.cc:28-78,
+ *                         SimMaterialData.cc:6-53) - same 14 data files
+ *   dpmx_phantom_slab     Geom::Geom(lbox, matData, geomIndex) (Geom.cc:9-17)
+ *                         with the pre-defined slab geometries (Geom.cc:133-164)
+ *   dpmx_phantom_voxels   the extension point of Geom::GetMaterialIndex /
+ *                         GetVoxelMaterialDensity (Geom.hh:64-95) for 3-D
+ *                         voxel phantoms
+ *   dpmx_simulate         Simulate(nprimary, eprimary, iselectron, lbox, ...,
+ *                         geomIndex, filename) (SimDPMLike.hh:46,
+ *                         SimDPMLike.cc:40-251), histograms returned in memory
+ *   dpmx_write_hist       Geom::Write (Geom.cc:167-192), the hist.sim format
+ *   dpmx_run              many Simulate calls (jobs) batched in one run
+ *   dpmx_sampler_eval     the per-interaction samplers SimKNTables.cc:69-90,
+ *                         SimMollerTables.cc:69-89, SimSBTables.cc:93-114,
+ *                         SimGSTables.cc:84-119 fed with given uniforms
+ *   dpmx_table_eval       the loaders' interpolators, e.g.
+ *                         SimStoppingPower::GetDEDXPerDensity (SimStoppingPower.hh:43)
+ *   dpmx_influence_*      no reference counterpart: the beamlet influence matrix
+ */
+#ifndef DPMX_H
+#define DPMX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DPMX_OK 0
+#define DPMX_ERR_FILE (-1)      /* a data file is missing or unreadable */
+#define DPMX_ERR_PARSE (-2)     /* a data file does not have the expected layout */
+#define DPMX_ERR_CUDA (-3)      /* a CUDA call failed (no device, launch error...) */
+#define DPMX_ERR_ARG (-4)       /* an argument is out of range */
+#define DPMX_ERR_OVERFLOW (-5)  /* a particle queue or stack overflowed; result incomplete */
+#define DPMX_ERR_NOMEM (-6)     /* device memory exhausted */
+
+/* precision / algorithm of a run */
+#define DPMX_FP64_PLAIN 0       /* one thread per history, FP64, reference order */
+#define DPMX_FP32_EVENT 1       /* event-based FP32 transport, FP64 tallies */
+
+typedef struct dpmx_tables dpmx_tables;
+typedef struct dpmx_phantom dpmx_phantom;
+typedef struct dpmx_result dpmx_result;
+typedef struct dpmx_csr dpmx_csr;
+
+const char* dpmx_last_error(void);
+const char* dpmx_version(void);
+
+/* ---- data tables (the reference's data-file format) ---- */
+int dpmx_tables_load(const char* data_dir, dpmx_tables** out);
+void dpmx_tables_free(dpmx_tables* t);
+int dpmx_tables_num_materials(const dpmx_tables* t);
+/* which: 0 electron cut, 1 gamma cut, 2 MSC s-low, 3 s-high, 4 e-cross [MeV/mm] */
+double dpmx_tables_param(const dpmx_tables* t, int which);
+double dpmx_tables_density(const dpmx_tables* t, int imat);
+/* copies the material name (NUL-terminated, truncated to cap) */
+int dpmx_tables_material_name(const dpmx_tables* t, int imat, char* name, int cap);
+
+/* ---- geometry ---- */
+/* reference pre-defined geometry geom_index (0-3) with cubic voxels of lbox mm;
+ * depth tally (bins of lbox along +z) */
+int dpmx_phantom_slab(const dpmx_tables* t, int geom_index, double lbox_mm, dpmx_phantom** out);
+/* nx*ny*nz voxels (x fastest) of vx*vy*vz mm, material ids from the host array
+ * mat (255 = vacuum); the phantom spans x in [-nx*vx/2, nx*vx/2], y likewise,
+ * z in [0, nz*vz]; 3-D tally */
+int dpmx_phantom_voxels(const dpmx_tables* t, int nx, int ny, int nz, double vx, double vy, double vz,
+                        const uint8_t* mat, dpmx_phantom** out);
+void dpmx_phantom_free(dpmx_phantom* p);
+/* number of tally bins of a phantom (slab: depth bins; voxels: nx*ny*nz) */
+long long dpmx_phantom_tally_size(const dpmx_phantom* p);
+
+/* ---- sources and jobs ---- */
+typedef struct {
+  int particle;       /* -1 electron, 0 photon */
+  int spectrum;       /* 0 mono e0; 1 uniform on [e0,e1]; 2 p(E) ~ (e1-E) on [e0,e1] */
+  double e0, e1;      /* MeV */
+  int shape;          /* 0 pencil at (cx,cy); 1 rectangle fx*fy centred at (cx,cy);
+                         2 grid of nbx*nby beamlets fx*fy each, centred at (cx,cy) */
+  double cx, cy, fx, fy;  /* mm */
+  int nbx, nby;
+} dpmx_source;
+
+typedef struct {
+  const dpmx_phantom* phantom;
+  dpmx_source source;
+  long long histories;
+  uint64_t seed;
+} dpmx_job;
+
+typedef struct {
+  int precision;             /* DPMX_FP64_PLAIN or DPMX_FP32_EVENT */
+  int batches;               /* statistical batches for dose^2 (default 10) */
+  int block_size;            /* threads per block (0: default / tuned) */
+  int blocks_per_sm;         /* resident blocks per SM (0: default / tuned) */
+  long long chunk_histories; /* histories per transport chunk (0: default / tuned) */
+  int tally_aggregate;       /* FP32: -1 default, 0 plain atomics, 1 warp-aggregated */
+  int use_graph;             /* FP32: capture each batch in a CUDA graph (default 1) */
+  int tag_beamlets;          /* FP32: also tally dose per beamlet (influence matrix) */
+  int autotune;              /* 1: tune block size / chunk / aggregation on a sample */
+  void* stream;              /* cudaStream_t to run on, NULL = library stream */
+} dpmx_run_options;
+
+void dpmx_run_options_default(dpmx_run_options* o);
+
+typedef struct {
+  double edep;               /* total energy deposited in the tally [MeV] */
+  double escaped;            /* energy that left the phantom [MeV] */
+  double primary_energy;     /* sum of primary kinetic energies [MeV] */
+  double max_residual;       /* max |E_primary - E_deposited - E_escaped| of a history [MeV] */
+  long long residual_violations; /* histories with residual > 1e-3 E_primary */
+  long long lost;            /* particles dropped (queue/stack overflow, step cap) */
+  long long steps;           /* electron condensed-history sub-steps */
+  long long histories;
+} dpmx_job_stats;
+
+int dpmx_run(const dpmx_tables* t, const dpmx_job* jobs, int njobs, const dpmx_run_options* opt,
+             dpmx_result** out);
+/* host copies of a job's tallies; any output pointer may be NULL.
+ * dose: energy per bin [MeV], summed over histories; dose2: sum over batches of
+ * the squared batch sums; steps: number of scoring steps per bin (slab only) */
+int dpmx_result_tally(const dpmx_result* r, int job, double* dose, double* dose2, double* steps);
+/* device pointer of a job's dose tally (valid until dpmx_result_free) */
+const double* dpmx_result_tally_device(const dpmx_result* r, int job);
+int dpmx_result_stats(const dpmx_result* r, int job, dpmx_job_stats* s);
+/* wall time of the transport (device events) [ms] and kernel launches issued */
+double dpmx_result_elapsed_ms(const dpmx_result* r);
+long long dpmx_result_launches(const dpmx_result* r);
+/* chosen launch configuration: [block_size, blocks_per_sm, chunk_histories, tally_aggregate] */
+int dpmx_result_config(const dpmx_result* r, long long* cfg4);
+void dpmx_result_free(dpmx_result* r);
+
+/* ---- drop-in for Simulate(...) ---- */
+/* pencil beam from (0,0,-lbox/2) along +z through geometry geom_index; fills
+ * edep_hist/step_hist (cap bins) with the reference's depth histograms and
+ * sets *hist_len to the number of bins the reference would write */
+int dpmx_simulate(const dpmx_tables* t, int nprimary, double eprimary, int iselectron, double lbox,
+                  int geom_index, uint64_t seed, int precision, double* edep_hist, double* step_hist,
+                  int cap, int* hist_len);
+/* writes hist.sim exactly as Geom::Write */
+int dpmx_write_hist(const dpmx_tables* t, const char* fname, int geom_index, double lbox, int nprimary,
+                    const double* edep_hist, const double* step_hist, int hist_len);
+
+/* ---- tier-1 hooks ---- */
+/* sampler: 0 KN eps, 1 Moller T', 2 SB k (imat), 3 GS mu. e: n energies,
+ * r: 3n uniforms (sampler arguments in order), out: n results; host arrays */
+int dpmx_sampler_eval(const dpmx_tables* t, int precision, int sampler, int imat, const double* e,
+                      const double* r, double* out, int n);
+/* quantity: 0 dE/dx, 1 1/lambda_1, 2 brem IMFP, 3 Moller IMFP, 4 K1,
+ * 5 global max photon IMFP, 6 total, 7 Compton, 8 pair IMFP (per density) */
+int dpmx_table_eval(const dpmx_tables* t, int precision, int quantity, int imat, const double* e,
+                    double* out, int n);
+/* FP64 form of the Simulate workload (SimDPMLike.cc:57-247) that also returns
+ * each history's deposited energy (hist_edep, nprimary values) and the depth
+ * histogram; history h uses the per-history random stream with index h */
+int dpmx_simulate_histories(const dpmx_tables* t, int nprimary, double eprimary, int iselectron, double lbox,
+                            int geom_index, uint64_t seed, double* hist_edep, double* edep_hist, int cap);
+
+/* ---- influence matrix (beamlet-tagged run with tag_beamlets = 1) ---- */
+/* builds A (rows: voxels, cols: beamlets, FP32 values from the FP64 tally,
+ * entries <= threshold * max dropped) on the device */
+int dpmx_influence_build(const dpmx_result* r, int job, double threshold, dpmx_csr** out);
+int dpmx_csr_shape(const dpmx_csr* a, long long* rows, long long* cols, long long* nnz);
+/* device arrays: row_ptr (rows+1, int64), col (nnz, int32), val (nnz, float) */
+int dpmx_csr_device(const dpmx_csr* a, const int64_t** row_ptr, const int32_t** col, const float** val);
+/* y[rows] = A x[cols]; device pointers, FP64 vectors, FP64 accumulation */
+int dpmx_csr_spmv(const dpmx_csr* a, const double* x, double* y, void* stream);
+/* x[cols] = A^T y[rows]; device pointers */
+int dpmx_csr_spmv_t(const dpmx_csr* a, const double* y, double* x, void* stream);
+/* host copies of the three CSR arrays (sizes from dpmx_csr_shape) */
+int dpmx_csr_download(const dpmx_csr* a, int64_t* row_ptr, int32_t* col, float* val);
+void dpmx_csr_free(dpmx_csr* a);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DPMX_H */
