@@ -1,0 +1,302 @@
+#!/usr/bin/env python
+"""Benchmark: histories/s of the FP32 event-based transport (FP64 tallies) on
+the precision-form workload: a 128x128x256 phantom of 2 mm voxels (water body,
+G4_LUNG_ICRP slab z = 60-120 mm, G4_BONE_COMPACT_ICRU cylinder r = 15 mm along
+y at x = 0, z = 180 mm), a 10x10 cm2 photon beam with energy uniform in
+1-20 MeV, seed 7. A step is one run of `--hist` histories (default 1e7; 10
+steps = the workload's 1e8 histories) with 10 statistical batches.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the CPU oracle (the restatement of the reference's
+double-precision transport) on the host cores on a bounded sample of the same
+workload. Under torchrun each rank runs its own history range (weak scaling).
+"""
+import argparse
+import importlib
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+DATA = os.path.join(ROOT, "data", "water_lung_bone")
+METRIC = "histories/s"
+WORKLOAD = "precision form: 128x128x256 x 2 mm water/lung-slab/bone-cylinder phantom, 10x10 cm2 photon beam U[1,20] MeV"
+
+# algorithmic bytes per unit (FP32 form): an electron sub-step reads 4 spline
+# segments of 5 floats (80 B), one material byte, and updates one FP64 tally
+# bin (16 B read+write); a photon step reads 3 linear-table points (24 B) and
+# one material byte; a queued particle is written once and read once (2 x 52 B)
+BYTES_E_STEP = 80 + 1 + 16
+BYTES_P_STEP = 24 + 1
+BYTES_PARTICLE = 2 * 52
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--hist", type=float, default=1e7, help="histories per step and GPU")
+    ap.add_argument("--cpu-hist", type=int, default=4000, help="oracle histories per CPU worker and step")
+    ap.add_argument("--batches", type=int, default=10, help="statistical batches per step")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# CPU oracle (reference arm and cpu_baseline): one process per core
+# ---------------------------------------------------------------------------
+def _oracle_worker(args):
+    first, n, seed = args
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, ROOT)
+    import numpy as np  # noqa: F401
+    orc = importlib.import_module("cpu_oracle")
+    wl = importlib.import_module("dpm-g4cpp_gb300.workloads")
+    o = orc.Oracle(DATA)
+    m = wl.precision_phantom()
+    s = wl.precision_source()
+    src = dict(particle=s.particle, spectrum=s.spectrum, e0=s.e0, e1=s.e1, shape=s.shape, cx=s.cx, cy=s.cy,
+               fx=s.fx, fy=s.fy, nbx=s.nbx, nby=s.nby)
+    t0 = time.perf_counter()
+    if n > 0:
+        o.simulate_voxel(m, 2.0, src, n, seed, first=first)
+    return time.perf_counter() - t0
+
+
+def oracle_pool():
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    pool = mp.get_context("spawn").Pool(cores)
+    pool.map(_oracle_worker, [(0, 0, 7)] * cores)   # load oracle + phantom in every worker
+    return pool, cores
+
+
+def oracle_step(pool, cores, per, step):
+    t0 = time.perf_counter()
+    pool.map(_oracle_worker, [((step * cores + k) * per, per, 7) for k in range(cores)])
+    dt = time.perf_counter() - t0
+    return cores * per / dt, dt
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, n in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower().startswith("active"):
+                    reasons.add(n)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+def main():
+    a = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if a.impl == "reference":
+        if rank != 0:
+            return 0
+        pool, cores = oracle_pool()
+        for w in range(a.warmup):
+            oracle_step(pool, cores, max(1, a.cpu_hist // 4), w)
+        tot_h, tot_t = 0.0, 0.0
+        for k in range(a.steps):
+            rate, dt = oracle_step(pool, cores, a.cpu_hist, a.warmup + k)
+            tot_h += cores * a.cpu_hist
+            tot_t += dt
+        pool.close()
+        value = tot_h / tot_t
+        sample = "%d histories per core per step on %d cores" % (a.cpu_hist, cores)
+        print(json.dumps({
+            "impl": "reference", "metric": METRIC, "value": value, "unit": "histories/s", "n_gpus": a.gpus,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * tot_t / a.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "histories_per_step": cores * a.cpu_hist, "l2": "n/a (CPU)"},
+            "cpu_baseline": {"value": value, "unit": "histories/s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "histories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }))
+        return 0
+
+    # CPU baseline workers start before the first GPU call (spawned processes)
+    pool = cores = None
+    if rank == 0:
+        pool, cores = oracle_pool()
+
+    import numpy as np
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dpm = importlib.import_module("dpm-g4cpp_gb300")
+    wl = importlib.import_module("dpm-g4cpp_gb300.workloads")
+    tables = dpm.Tables(DATA)
+    mat = wl.precision_phantom()
+    src = wl.precision_source()
+    ph = dpm.Phantom.voxels(tables, mat, 2.0)
+    H = int(a.hist)
+    # a non-default stream: the library captures each run into a CUDA graph on it,
+    # and the timing events are recorded on the same stream
+    stream = torch.cuda.Stream()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")   # > L2 (129 MB)
+
+    def seed_of(step):
+        return 7 + 1000003 * rank + step
+
+    def one(step, profile=False):
+        return dpm.run(tables, [dpm.Job(ph, src, H, seed_of(step))], batches=a.batches, stream=stream.cuda_stream,
+                       profile_phases=profile)
+
+    for w in range(a.warmup):
+        one(-1 - w).close()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
+    launches = 0
+    stats = []
+    torch.cuda.synchronize()
+    for k in range(a.steps):
+        flush.fill_(float(k))          # L2 flush between timed steps (outside the events)
+        ev[k][0].record(stream)
+        r = one(k)
+        ev[k][1].record(stream)
+        launches += r.launches
+        stats.append(r.stats(0))
+        r.close()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = sum(e0.elapsed_time(e1) for e0, e1 in ev)
+    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.barrier()
+    ms_max = float(t.item())
+    value = world * H * a.steps / (ms_max * 1e-3)
+
+    # e2e through the public API with host buffers: per step the phantom goes
+    # host->device from pinned memory and the dose + dose^2 come back
+    pinned = torch.from_numpy(mat.reshape(-1)).pin_memory().numpy().reshape(mat.shape)
+    e2e_steps = max(1, min(3, a.steps))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(e2e_steps):
+        p2 = dpm.Phantom.voxels(tables, pinned, 2.0)
+        r = dpm.run(tables, [dpm.Job(p2, src, H, seed_of(100 + k))], batches=a.batches)
+        d, d2, _ = r.tally(0)
+        r.close()
+        p2.close()
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": world * H * e2e_steps / e2e_s, "unit": "histories/s",
+           "h2d_bytes_per_step": int(mat.nbytes), "d2h_bytes_per_step": int(2 * d.nbytes)}
+
+    # live roofline of the dominant kernel from a profiled run (every phase launch timed)
+    r = one(10**6, profile=True)
+    pr = r.profile
+    r.close()
+    peak, peak_kind = measured_peaks()
+    e_bytes = pr["electron_steps"] * BYTES_E_STEP + pr["electrons"] * BYTES_PARTICLE
+    p_bytes = pr["photon_steps"] * BYTES_P_STEP + pr["photons"] * BYTES_PARTICLE
+    if pr["electron_ms"] >= pr["photon_ms"]:
+        kname, kms, kbytes, nl = "ElectronPhase", pr["electron_ms"], e_bytes, pr["electron_launches"]
+    else:
+        kname, kms, kbytes, nl = "PhotonPhase", pr["photon_ms"], p_bytes, pr["photon_launches"]
+    achieved = kbytes / (kms * 1e-3) / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tf):
+        with open(tf) as f:
+            traffic = json.load(f).get(kname)
+    roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+                "algorithmic_bytes_per_launch": kbytes / max(1.0, nl), "avg_launch_ms": kms / max(1.0, nl),
+                "electron_phase_share": pr["electron_ms"] / max(1e-9, pr["total_ms"]),
+                "photon_phase_share": pr["photon_ms"] / max(1e-9, pr["total_ms"]),
+                "electron_steps_per_s": pr["electron_steps"] / max(1e-9, pr["electron_ms"] * 1e-3),
+                "photon_steps_per_s": pr["photon_steps"] / max(1e-9, pr["photon_ms"] * 1e-3)}
+
+    cpu = None
+    if rank == 0:
+        rate, dt = oracle_step(pool, cores, 5 * a.cpu_hist, 0)
+        pool.close()
+        cpu = {"value": rate, "unit": "histories/s", "cores": cores, "kind": "port",
+               "sample": "%d histories per core on %d cores (%.1f s wall)" % (5 * a.cpu_hist, cores, dt)}
+    st = stats[-1]
+    if rank == 0:
+        print(json.dumps({
+            "metric": METRIC, "value": value, "unit": "histories/s", "n_gpus": world, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": ms_max / a.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64-tally", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "histories_per_step": H, "batches": a.batches, "phantom": [256, 128, 128],
+                       "voxel_mm": 2.0, "seed": 7, "l2": "flushed between steps (256 MB write)"},
+            "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+            "energy_check": {"max_residual_mev": st.max_residual, "violations": st.residual_violations,
+                             "lost": st.lost},
+        }))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

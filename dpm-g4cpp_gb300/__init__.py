@@ -50,7 +50,8 @@ class _Job(C.Structure):
 class _Opts(C.Structure):
     _fields_ = [("precision", C.c_int), ("batches", C.c_int), ("block_size", C.c_int), ("blocks_per_sm", C.c_int),
                 ("chunk_histories", C.c_longlong), ("tally_aggregate", C.c_int), ("use_graph", C.c_int),
-                ("tag_beamlets", C.c_int), ("autotune", C.c_int), ("stream", C.c_void_p)]
+                ("tag_beamlets", C.c_int), ("autotune", C.c_int), ("profile_phases", C.c_int),
+                ("stream", C.c_void_p)]
 
 
 class _Stats(C.Structure):
@@ -94,6 +95,7 @@ def library():
         "dpmx_result_elapsed_ms": (C.c_double, [P]),
         "dpmx_result_launches": (C.c_longlong, [P]),
         "dpmx_result_config": (C.c_int, [P, C.POINTER(C.c_longlong)]),
+        "dpmx_result_profile": (C.c_int, [P, C.POINTER(C.c_double)]),
         "dpmx_result_free": (None, [P]),
         "dpmx_simulate": (C.c_int, [P, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int, C.c_uint64, C.c_int,
                                     _dp, _dp, C.c_int, C.POINTER(C.c_int)]),
@@ -129,7 +131,8 @@ def exported_symbols():
             "dpmx_tables_param", "dpmx_tables_density", "dpmx_tables_material_name", "dpmx_phantom_slab",
             "dpmx_phantom_voxels", "dpmx_phantom_free", "dpmx_phantom_tally_size", "dpmx_run_options_default",
             "dpmx_run", "dpmx_result_tally", "dpmx_result_tally_device", "dpmx_result_stats",
-            "dpmx_result_elapsed_ms", "dpmx_result_launches", "dpmx_result_config", "dpmx_result_free",
+            "dpmx_result_elapsed_ms", "dpmx_result_launches", "dpmx_result_config", "dpmx_result_profile",
+            "dpmx_result_free",
             "dpmx_simulate", "dpmx_write_hist", "dpmx_sampler_eval", "dpmx_table_eval", "dpmx_simulate_histories",
             "dpmx_influence_build", "dpmx_csr_shape", "dpmx_csr_device", "dpmx_csr_spmv", "dpmx_csr_spmv_t",
             "dpmx_csr_download", "dpmx_csr_free"]
@@ -318,6 +321,15 @@ class Result:
         _check(library().dpmx_result_config(self._h, a))
         return dict(block_size=a[0], blocks_per_sm=a[1], chunk_histories=a[2], tally_aggregate=a[3])
 
+    @property
+    def profile(self):
+        """Phase profile of a run made with profile_phases=True."""
+        a = (C.c_double * 10)()
+        _check(library().dpmx_result_profile(self._h, a))
+        keys = ["electron_ms", "photon_ms", "electron_launches", "photon_launches", "electron_steps",
+                "photon_steps", "electrons", "photons", "histories", "total_ms"]
+        return dict(zip(keys, list(a)))
+
     def influence(self, j=0, threshold=0.0):
         from .influence import InfluenceMatrix
         h = C.c_void_p()
@@ -337,7 +349,7 @@ class Result:
 
 
 def run(tables, jobs, precision=FP32_EVENT, batches=10, block_size=0, blocks_per_sm=0, chunk_histories=0,
-        tally_aggregate=-1, use_graph=True, tag_beamlets=False, autotune=False, stream=None):
+        tally_aggregate=-1, use_graph=True, tag_beamlets=False, autotune=False, profile_phases=False, stream=None):
     """Runs the jobs (one run, one stream) and returns a Result."""
     L = library()
     arr = (_Job * len(jobs))()
@@ -355,6 +367,7 @@ def run(tables, jobs, precision=FP32_EVENT, batches=10, block_size=0, blocks_per
     o.use_graph = 1 if use_graph else 0
     o.tag_beamlets = 1 if tag_beamlets else 0
     o.autotune = 1 if autotune else 0
+    o.profile_phases = 1 if profile_phases else 0
     o.stream = stream
     h = C.c_void_p()
     rc = L.dpmx_run(tables.handle, arr, len(jobs), C.byref(o), C.byref(h))

@@ -47,6 +47,7 @@ struct dpmx_result {
   double ms = 0.0;
   long long launches = 0;
   long long cfg[4] = {0, 0, 0, 0};
+  double prof[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   ~dpmx_result() {
     for (auto& j : jobs) {
       cudaFree(j.d_dose);

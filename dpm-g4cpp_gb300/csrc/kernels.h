@@ -19,6 +19,7 @@ struct RunCounters {
   unsigned long long violations;
   unsigned long long lost;
   unsigned long long histories;
+  unsigned long long photonSteps;   // Woodcock steps (FP32 form, accumulated on job 0)
 };
 
 // warp-reduced accumulation of per-thread counters (FP64 plain form)
@@ -86,10 +87,17 @@ struct Segment {               // a run of primaries of one job inside a chunk
   long long slotBase;          // energy-check slot of the run's first primary
 };
 
+// A queue is split into kStripes stripes, each with its own append counter
+// (chosen by the appending warp), so that appends from all SMs do not meet on
+// one atomic. Stripe s holds entries [s*stripeCap, s*stripeCap + count[s]).
+constexpr int kStripes = 16;
+constexpr int kWorkGrab = 64;  // queue items a warp claims per atomic
+
 struct Queue {                 // SoA particle queue
   float *lx, *ly, *lz, *dx, *dy, *dz, *e;
   uint32_t *vox, *hist, *slot, *uidlo, *uidhi, *meta;
-  unsigned long long capacity;
+  unsigned long long capacity;   // total entries
+  unsigned long long stripeCap;  // entries per stripe
 };
 
 struct PhaseArgs {
@@ -100,9 +108,9 @@ struct PhaseArgs {
   int nsegs;
   long long nPrimaries;
   Queue in;                    // particles to transport in this phase
-  const unsigned long long* inCount;
+  const unsigned long long* inCount;   // kStripes counters
   Queue outE, outP;            // secondaries: electrons, photons
-  unsigned long long* outECount;
+  unsigned long long* outECount;       // kStripes counters each
   unsigned long long* outPCount;
   unsigned long long* head;    // work counter of this phase
   double* histE;               // per-slot energy accounted (deposit + escape)

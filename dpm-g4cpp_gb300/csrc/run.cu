@@ -27,7 +27,10 @@ using namespace dpmx;
 namespace {
 
 constexpr int kGen = 32;                              // generations per chunk
-constexpr int kCtrPerChunk = 4 * (kGen + 1) + 1;      // cntE, cntP, headE, headP per generation + overflow
+// per chunk: striped counts of the electron and photon queues of every
+// generation, the two work counters of every generation, and the overflow count
+constexpr int kCntStride = (kGen + 1) * kStripes;
+constexpr int kCtrPerChunk = 2 * kCntStride + 2 * (kGen + 1) + 1;
 
 struct Cfg {
   int threads = 256;
@@ -49,6 +52,8 @@ struct DevBuf {       // owned device allocations of one run
 };
 
 int AllocQueue(DevBuf& b, Queue& q, unsigned long long cap) {
+  q.stripeCap = (cap + kStripes - 1) / kStripes;
+  cap = q.stripeCap * kStripes;
   q.capacity = cap;
   float** f[7] = {&q.lx, &q.ly, &q.lz, &q.dx, &q.dy, &q.dz, &q.e};
   uint32_t** u[6] = {&q.vox, &q.hist, &q.slot, &q.uidlo, &q.uidhi, &q.meta};
@@ -96,7 +101,12 @@ bool IsPow2Aligned(long long) { return true; }
 // FP32 event form
 // ---------------------------------------------------------------------------
 int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, const Cfg& cfg, bool tag,
-            bool useGraph, cudaStream_t st, std::vector<JobOut>& outs, double* ms, long long* launches) {
+            bool useGraph, cudaStream_t st, std::vector<JobOut>& outs, double* ms, long long* launches,
+            double* prof = nullptr) {
+  // prof (optional, launches not captured): events around every phase launch
+  // give the electron / photon phase times; see dpmx_result_profile
+  const bool profile = prof != nullptr && !useGraph;
+  std::vector<cudaEvent_t> evE, evP;
   DevBuf buf;
   const int nsm = NumSMs();
   // concatenated tallies of all jobs: batch tally, dose, dose2
@@ -169,7 +179,7 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
   CK(cudaMemsetAsync(ctr, 0, nchunks * kCtrPerChunk * sizeof(unsigned long long), st));
   // queues: double-buffered electrons and photons; a generation holds well
   // under 8 secondaries of each kind per primary
-  const unsigned long long cap = (unsigned long long)std::max<long long>(maxSlots * 8, 1 << 14);
+  const unsigned long long cap = (unsigned long long)std::max<long long>(maxSlots * 8, 1 << 18);
   Queue qe[2], qp[2];
   for (int k = 0; k < 2; ++k) {
     if (int rc = AllocQueue(buf, qe[k], cap)) return rc;
@@ -182,11 +192,11 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
     for (int b = 0; b < batches; ++b) {
       for (auto& c : plan[b]) {
         unsigned long long* cc = ctr + ci * kCtrPerChunk;
-        unsigned long long* cntE = cc;
-        unsigned long long* cntP = cc + (kGen + 1);
-        unsigned long long* headE = cc + 2 * (kGen + 1);
-        unsigned long long* headP = cc + 3 * (kGen + 1);
-        unsigned long long* ovf = cc + 4 * (kGen + 1);
+        unsigned long long* cntE = cc;                       // [gen][stripe]
+        unsigned long long* cntP = cc + kCntStride;
+        unsigned long long* headE = cc + 2 * kCntStride;     // [gen]
+        unsigned long long* headP = headE + (kGen + 1);
+        unsigned long long* ovf = headP + (kGen + 1);
         const Segment* sP = dsegs + segCur;
         const Segment* sE = sP + c.segP.size();
         const Segment* sA = sE + c.segE.size();
@@ -203,19 +213,33 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
           a.aggregate = cfg.aggregate;
           // photons of generation g; their electrons join generation g
           a.segs = sP; a.nsegs = int(c.segP.size()); a.nPrimaries = (g == 0) ? c.nP : 0;
-          a.in = qp[g & 1]; a.inCount = cntP + g;
-          a.outE = qe[g & 1]; a.outECount = cntE + g;
-          a.outP = qp[(g + 1) & 1]; a.outPCount = cntP + g + 1;
+          a.in = qp[g & 1]; a.inCount = cntP + g * kStripes;
+          a.outE = qe[g & 1]; a.outECount = cntE + g * kStripes;
+          a.outP = qp[(g + 1) & 1]; a.outPCount = cntP + (g + 1) * kStripes;
           a.head = headP + g;
+          if (profile) {
+            evP.resize(evP.size() + 2);
+            CK(cudaEventCreate(&evP[evP.size() - 2]));
+            CK(cudaEventCreate(&evP.back()));
+            CK(cudaEventRecord(evP[evP.size() - 2], s));
+          }
           CK(LaunchPhotonPhase(a, blocks, cfg.threads, s));
+          if (profile) CK(cudaEventRecord(evP.back(), s));
           ++nl;
           // electrons of generation g; their secondaries form generation g+1
           a.segs = sE; a.nsegs = int(c.segE.size()); a.nPrimaries = (g == 0) ? c.nE : 0;
-          a.in = qe[g & 1]; a.inCount = cntE + g;
-          a.outE = qe[(g + 1) & 1]; a.outECount = cntE + g + 1;
-          a.outP = qp[(g + 1) & 1]; a.outPCount = cntP + g + 1;
+          a.in = qe[g & 1]; a.inCount = cntE + g * kStripes;
+          a.outE = qe[(g + 1) & 1]; a.outECount = cntE + (g + 1) * kStripes;
+          a.outP = qp[(g + 1) & 1]; a.outPCount = cntP + (g + 1) * kStripes;
           a.head = headE + g;
+          if (profile) {
+            evE.resize(evE.size() + 2);
+            CK(cudaEventCreate(&evE[evE.size() - 2]));
+            CK(cudaEventCreate(&evE.back()));
+            CK(cudaEventRecord(evE[evE.size() - 2], s));
+          }
           CK(LaunchElectronPhase(a, blocks, cfg.threads, s));
+          if (profile) CK(cudaEventRecord(evE.back(), s));
           ++nl;
         }
         CK(LaunchEnergyCheck(histE, histE0, c.nslots, sA, int(c.segAll.size()), dj, s));
@@ -265,9 +289,48 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
   std::vector<unsigned long long> hc(nchunks * kCtrPerChunk);
   CK(cudaMemcpy(hc.data(), ctr, hc.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
   unsigned long long lost = 0;
+  double nElec = 0, nPhot = 0;
   for (size_t ci = 0; ci < nchunks; ++ci) {
     const unsigned long long* cc = hc.data() + ci * kCtrPerChunk;
-    lost += cc[kGen] + cc[(kGen + 1) + kGen] + cc[4 * (kGen + 1)];
+    for (int k = 0; k < kStripes; ++k) lost += cc[kGen * kStripes + k] + cc[kCntStride + kGen * kStripes + k];
+    lost += cc[2 * kCntStride + 2 * (kGen + 1)];
+    for (int g = 0; g < kGen; ++g)
+      for (int k = 0; k < kStripes; ++k) {
+        nElec += double(cc[g * kStripes + k]);
+        nPhot += double(cc[kCntStride + g * kStripes + k]);
+      }
+  }
+  if (prof) {
+    double te = 0, tp = 0;
+    for (size_t k = 0; k + 1 < evE.size(); k += 2) {
+      float x = 0.f;
+      CK(cudaEventElapsedTime(&x, evE[k], evE[k + 1]));
+      te += x;
+    }
+    for (size_t k = 0; k + 1 < evP.size(); k += 2) {
+      float x = 0.f;
+      CK(cudaEventElapsedTime(&x, evP[k], evP[k + 1]));
+      tp += x;
+    }
+    for (auto e : evE) cudaEventDestroy(e);
+    for (auto e : evP) cudaEventDestroy(e);
+    double hist = 0, primE = 0, primP = 0;
+    for (int j = 0; j < njobs; ++j) {
+      hist += double(jobs[j].histories);
+      (jobs[j].source.particle == 0 ? primP : primE) += double(jobs[j].histories);
+    }
+    RunCounters c0{};
+    CK(cudaMemcpy(&c0, cnt, sizeof(RunCounters), cudaMemcpyDeviceToHost));
+    prof[0] = te;
+    prof[1] = tp;
+    prof[2] = double(evE.size() / 2);
+    prof[3] = double(evP.size() / 2);
+    prof[4] = double(c0.steps);
+    prof[5] = double(c0.photonSteps);
+    prof[6] = nElec + primE;
+    prof[7] = nPhot + primP;
+    prof[8] = hist;
+    prof[9] = fms;
   }
   std::vector<RunCounters> hcnt(njobs);
   CK(cudaMemcpy(hcnt.data(), cnt, njobs * sizeof(RunCounters), cudaMemcpyDeviceToHost));
@@ -491,7 +554,9 @@ int dpmx_run(const dpmx_tables* t, const dpmx_job* jobs, int njobs, const dpmx_r
       for (int j = 0; j < njobs; ++j) total += jobs[j].histories;
       Cfg cfg = DefaultCfg(&o, total);
       if (o.autotune) rc = Autotune(t, jobs, njobs, cfg, st, &cfg);
-      if (!rc) rc = RunFp32(t, jobs, njobs, o.batches, cfg, tag, o.use_graph != 0, st, r->jobs, &r->ms, &r->launches);
+      if (!rc)
+        rc = RunFp32(t, jobs, njobs, o.batches, cfg, tag, o.use_graph != 0 && !o.profile_phases, st, r->jobs, &r->ms,
+                     &r->launches, o.profile_phases ? r->prof : nullptr);
       r->cfg[0] = cfg.threads; r->cfg[1] = cfg.blocksPerSM; r->cfg[2] = cfg.chunk; r->cfg[3] = cfg.aggregate;
     }
   }
@@ -542,6 +607,12 @@ int dpmx_result_config(const dpmx_result* r, long long* cfg4) {
   for (int i = 0; i < 4; ++i) cfg4[i] = r->cfg[i];
   return DPMX_OK;
 }
+int dpmx_result_profile(const dpmx_result* r, double* out10) {
+  if (!r || !out10) return Fail(DPMX_ERR_ARG, "null argument");
+  for (int i = 0; i < 10; ++i) out10[i] = r->prof[i];
+  return DPMX_OK;
+}
+
 void dpmx_result_free(dpmx_result* r) { delete r; }
 
 int dpmx_simulate(const dpmx_tables* t, int nprimary, double eprimary, int iselectron, double lbox, int geom_index,

@@ -125,6 +125,16 @@ __device__ __forceinline__ uint32_t PackVox(int ix, int iy, int iz) {
   return uint32_t(ix) | (uint32_t(iy) << 11) | (uint32_t(iz) << 22);
 }
 
+// queue entry of the item-th particle of a striped queue (prefix: kStripes+1
+// running counts of the stripes)
+__device__ __forceinline__ unsigned long long StripedIndex(const Queue& q, const unsigned long long* prefix,
+                                                           unsigned long long item) {
+  int s = 0;
+#pragma unroll
+  for (int k = 1; k < kStripes; ++k) s += (item >= prefix[k]) ? 1 : 0;
+  return (unsigned long long)s * q.stripeCap + (item - prefix[s]);
+}
+
 __device__ __forceinline__ void LoadParticle(const Queue& q, unsigned long long i, PState& p) {
   const uint32_t v = q.vox[i];
   p.ix = int(v & 0x7ffu); p.iy = int((v >> 11) & 0x7ffu); p.iz = int(v >> 22);
@@ -139,14 +149,16 @@ __device__ __forceinline__ void LoadParticle(const Queue& q, unsigned long long 
 __device__ __forceinline__ bool Append(const Queue& q, unsigned long long* count, unsigned long long* overflow,
                                        const PState& p) {
   cg::coalesced_group g = cg::coalesced_threads();
+  const int stripe = int((blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) & (kStripes - 1));
   unsigned long long base = 0;
-  if (g.thread_rank() == 0) base = atomicAdd(count, (unsigned long long)g.size());
+  if (g.thread_rank() == 0) base = atomicAdd(count + stripe, (unsigned long long)g.size());
   base = g.shfl(base, 0);
-  const unsigned long long i = base + g.thread_rank();
-  if (i >= q.capacity) {
+  const unsigned long long j = base + g.thread_rank();
+  if (j >= q.stripeCap) {
     atomicAdd(overflow, 1ull);
     return false;
   }
+  const unsigned long long i = (unsigned long long)stripe * q.stripeCap + j;
   q.vox[i] = PackVox(p.ix, p.iy, p.iz);
   q.lx[i] = p.lx; q.ly[i] = p.ly; q.lz[i] = p.lz;
   q.dx[i] = p.dx; q.dy[i] = p.dy; q.dz[i] = p.dz;
@@ -301,57 +313,110 @@ __device__ void MakePrimary(const PhaseArgs& a, const Segment* segs, long long i
 // ---------------------------------------------------------------------------
 // photon phase: Woodcock tracking (SimDPMLike.cc:463-635)
 // ---------------------------------------------------------------------------
+// Work distribution of a persistent phase kernel. A warp claims kWorkGrab
+// consecutive items per atomic on the phase's work counter and hands them to
+// its idle lanes over later iterations (warp-uniform state).
+struct WorkPool {
+  unsigned long long lo = 0, hi = 0, total = 0;
+  bool exhausted = false;
+  // returns the item for this lane (or ~0ull); `need` is the ballot of idle lanes
+  __device__ __forceinline__ unsigned long long Take(unsigned need, bool idle, unsigned long long* head, int lane) {
+    unsigned long long item = ~0ull;
+    if (need == 0 || exhausted) return item;
+    if (lo >= hi) {
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(head, (unsigned long long)kWorkGrab);
+      base = __shfl_sync(kFull, base, 0);
+      lo = base;
+      hi = base + kWorkGrab < total ? base + kWorkGrab : total;
+      if (base >= total) { exhausted = true; return item; }
+    }
+    const unsigned long long my = lo + __popc(need & ((1u << lane) - 1u));
+    if (idle && my < hi) item = my;
+    const unsigned long long n = __popc(need);
+    lo = lo + n < hi ? lo + n : hi;
+    return item;
+  }
+};
+
+// escaped energy summed in the lane and flushed once per job change
+struct EscTally {
+  double e = 0.0;
+  int job = -1;
+  __device__ __forceinline__ void Add(const JobF* jobs, int j, double x) {
+    if (j != job) {
+      if (job >= 0 && e != 0.0) atomicAdd(&jobs[job].cnt->escaped, e);
+      e = 0.0;
+      job = j;
+    }
+    e += x;
+  }
+  __device__ __forceinline__ void Flush(const JobF* jobs) {
+    if (job >= 0 && e != 0.0) atomicAdd(&jobs[job].cnt->escaped, e);
+    e = 0.0;
+  }
+};
+
+// running counts of the input stripes into shared memory; returns the total
+__device__ __forceinline__ unsigned long long StripePrefix(const unsigned long long* counts, unsigned long long* pre) {
+  if (threadIdx.x == 0) {
+    unsigned long long s = 0;
+    for (int k = 0; k < kStripes; ++k) { pre[k] = s; s += counts[k]; }
+    pre[kStripes] = s;
+  }
+  __syncthreads();
+  return pre[kStripes];
+}
+
 __global__ void __launch_bounds__(256) PhotonPhase(PhaseArgs a) {
   __shared__ JobF sjobs[16];
+  __shared__ unsigned long long spre[kStripes + 1];
   const bool fewJobs = a.njobs <= 16;
   if (fewJobs) {
     for (int j = threadIdx.x; j < a.njobs; j += blockDim.x) sjobs[j] = a.jobs[j];
-    __syncthreads();
   }
+  const unsigned long long nQ = StripePrefix(a.inCount, spre);
   const JobF* jobs = fewJobs ? sjobs : a.jobs;
-  const unsigned long long nQ = *a.inCount;
   const unsigned long long total = (unsigned long long)a.nPrimaries + nQ;
   if (total == 0) return;
   const int lane = threadIdx.x & 31;
-  const unsigned lt = (1u << lane) - 1u;
   const DevTables<float>& T = a.T;
 
-  bool active = false, exhausted = false;
+  bool active = false;
+  WorkPool pool;
+  pool.total = total;
+  EscTally esc;
   PState p;
   PRng rng;
   double acc = 0.0;
   unsigned pst = 0;
+  unsigned long long nph = 0;
   for (;;) {
     const unsigned need = __ballot_sync(kFull, !active);
-    if (need && !exhausted) {
-      unsigned long long base = 0;
-      if (lane == 0) base = atomicAdd(a.head, (unsigned long long)__popc(need));
-      base = __shfl_sync(kFull, base, 0);
-      if (base + __popc(need) >= total) exhausted = true;
-      if (!active) {
-        const unsigned long long my = base + __popc(need & lt);
-        if (my < total) {
-          if (my < (unsigned long long)a.nPrimaries) {
-            MakePrimary(a, a.segs, (long long)my, p, rng);
-          } else {
-            LoadParticle(a.in, my - a.nPrimaries, p);
-            const JobF& J = jobs[p.meta >> 2];
-            rng.Init(J.k0, J.k1, p.hist, p.ulo, p.uhi);
-          }
-          acc = 0.0;
-          pst = 0;
-          active = true;
-          const JobF& J = jobs[p.meta >> 2];
-          if (!InBox(J, p.ix, p.iy, p.iz) || MaterialAt(J, p.ix, p.iy, p.iz) < 0) {
-            acc += p.e;
-            atomicAdd(&J.cnt->escaped, double(p.e));
-            atomicAdd(a.histE + p.slot, acc);
-            active = false;
-          }
-        }
+    const unsigned long long my = pool.Take(need, !active, a.head, lane);
+    if (my != ~0ull) {
+      if (my < (unsigned long long)a.nPrimaries) {
+        MakePrimary(a, a.segs, (long long)my, p, rng);
+      } else {
+        LoadParticle(a.in, StripedIndex(a.in, spre, my - a.nPrimaries), p);
+        const JobF& J = jobs[p.meta >> 2];
+        rng.Init(J.k0, J.k1, p.hist, p.ulo, p.uhi);
+      }
+      acc = 0.0;
+      pst = 0;
+      active = true;
+      const JobF& J = jobs[p.meta >> 2];
+      if (!InBox(J, p.ix, p.iy, p.iz) || MaterialAt(J, p.ix, p.iy, p.iz) < 0) {
+        acc += p.e;
+        esc.Add(jobs, int(p.meta >> 2), double(p.e));
+        atomicAdd(a.histE + p.slot, acc);
+        active = false;
       }
     }
-    if (!__any_sync(kFull, active)) break;
+    if (!__any_sync(kFull, active)) {
+      if (pool.exhausted) break;
+      continue;
+    }
     if (!active) continue;
 
     // one Woodcock step
@@ -365,13 +430,14 @@ __global__ void __launch_bounds__(256) PhotonPhase(PhaseArgs a) {
       active = false;
       continue;
     }
+    ++nph;
     const float lmax = 1.0f / LinearGet(T.imfpMax, p.e);
     const float step = -lmax * __logf(rng.U());
     int im = -1;
     if (Fly(J, p, step)) im = MaterialAt(J, p.ix, p.iy, p.iz);
     if (im < 0) {
       acc += p.e;
-      atomicAdd(&J.cnt->escaped, double(p.e));
+      esc.Add(jobs, job, double(p.e));
       done = true;
     } else {
       const float rho = T.density[im];
@@ -475,6 +541,9 @@ __global__ void __launch_bounds__(256) PhotonPhase(PhaseArgs a) {
       active = false;
     }
   }
+  esc.Flush(jobs);
+  for (int o = 16; o > 0; o >>= 1) nph += __shfl_down_sync(kFull, nph, o);
+  if (lane == 0 && a.njobs > 0) atomicAdd(&a.jobs[0].cnt->photonSteps, nph);
 }
 
 // ---------------------------------------------------------------------------
@@ -507,17 +576,20 @@ __global__ void __launch_bounds__(256) ElectronPhase(PhaseArgs a) {
   const bool fewJobs = a.njobs <= 16;
   if (fewJobs)
     for (int j = threadIdx.x; j < a.njobs; j += blockDim.x) sjobs[j] = a.jobs[j];
+  __shared__ unsigned long long spre[kStripes + 1];
   StageElectronTables(a.T, sdata, &et);
+  const unsigned long long nQ = StripePrefix(a.inCount, spre);
   const JobF* jobs = fewJobs ? sjobs : a.jobs;
-  const unsigned long long nQ = *a.inCount;
   const unsigned long long total = (unsigned long long)a.nPrimaries + nQ;
   if (total == 0) return;
   const int lane = threadIdx.x & 31;
-  const unsigned lt = (1u << lane) - 1u;
   const DevTables<float>& T = a.T;
   const float ecut = T.ecut, gcut = T.gcut;
 
-  bool active = false, exhausted = false;
+  bool active = false;
+  WorkPool pool;
+  pool.total = total;
+  EscTally esc;
   PState p;
   PRng rng;
   EState s;
@@ -526,37 +598,32 @@ __global__ void __launch_bounds__(256) ElectronPhase(PhaseArgs a) {
   unsigned long long nsteps = 0;
   for (;;) {
     const unsigned need = __ballot_sync(kFull, !active);
-    if (need && !exhausted) {
-      unsigned long long base = 0;
-      if (lane == 0) base = atomicAdd(a.head, (unsigned long long)__popc(need));
-      base = __shfl_sync(kFull, base, 0);
-      if (base + __popc(need) >= total) exhausted = true;
-      if (!active) {
-        const unsigned long long my = base + __popc(need & lt);
-        if (my < total) {
-          if (my < (unsigned long long)a.nPrimaries) {
-            MakePrimary(a, a.segs, (long long)my, p, rng);
-          } else {
-            LoadParticle(a.in, my - a.nPrimaries, p);
-            const JobF& J = jobs[p.meta >> 2];
-            rng.Init(J.k0, J.k1, p.hist, p.ulo, p.uhi);
-          }
-          acc = 0.0;
-          pst = 0;
-          active = true;
-          const JobF& J = jobs[p.meta >> 2];
-          if (!InBox(J, p.ix, p.iy, p.iz) || MaterialAt(J, p.ix, p.iy, p.iz) < 0) {
-            acc += p.e + ((p.meta & 3u) == 2u ? 2.0f * kEMC2f : 0.f);
-            atomicAdd(&J.cnt->escaped, acc);
-            atomicAdd(a.histE + p.slot, acc);
-            active = false;
-          } else {
-            InitElectron(et, p, rng, s);
-          }
-        }
+    const unsigned long long my = pool.Take(need, !active, a.head, lane);
+    if (my != ~0ull) {
+      if (my < (unsigned long long)a.nPrimaries) {
+        MakePrimary(a, a.segs, (long long)my, p, rng);
+      } else {
+        LoadParticle(a.in, StripedIndex(a.in, spre, my - a.nPrimaries), p);
+        const JobF& J = jobs[p.meta >> 2];
+        rng.Init(J.k0, J.k1, p.hist, p.ulo, p.uhi);
+      }
+      acc = 0.0;
+      pst = 0;
+      active = true;
+      const JobF& J = jobs[p.meta >> 2];
+      if (!InBox(J, p.ix, p.iy, p.iz) || MaterialAt(J, p.ix, p.iy, p.iz) < 0) {
+        acc += p.e + ((p.meta & 3u) == 2u ? 2.0f * kEMC2f : 0.f);
+        esc.Add(jobs, int(p.meta >> 2), acc);
+        atomicAdd(a.histE + p.slot, acc);
+        active = false;
+      } else {
+        InitElectron(et, p, rng, s);
       }
     }
-    if (!__any_sync(kFull, active)) break;
+    if (!__any_sync(kFull, active)) {
+      if (pool.exhausted) break;
+      continue;
+    }
     if (!active) continue;
 
     // ---- one condensed-history sub-step (SimDPMLike.cc:273-458) ----
@@ -572,9 +639,9 @@ __global__ void __launch_bounds__(256) ElectronPhase(PhaseArgs a) {
       im = MaterialAt(J, p.ix, p.iy, p.iz);
     }
     if (im < 0) {
-      const float esc = p.e + (positron ? 2.0f * kEMC2f : 0.f);
-      acc += esc;
-      atomicAdd(&J.cnt->escaped, double(esc));
+      const float out = p.e + (positron ? 2.0f * kEMC2f : 0.f);
+      acc += out;
+      esc.Add(jobs, job, double(out));
       done = true;
     } else if (++pst > kMaxElectronSteps) {   // bounded: every step loses energy or moves >= 5e-5 mm
       acc += p.e + (positron ? 2.0f * kEMC2f : 0.f);
@@ -627,7 +694,7 @@ __global__ void __launch_bounds__(256) ElectronPhase(PhaseArgs a) {
           const int im2 = inside ? MaterialAt(J, p.ix, p.iy, p.iz) : -1;
           if (im2 < 0) {
             acc += edep + 2.0f * kEMC2f;
-            atomicAdd(&J.cnt->escaped, double(edep + 2.0f * kEMC2f));
+            esc.Add(jobs, job, double(edep + 2.0f * kEMC2f));
           } else {
             const float cost = 1.0f - 2.0f * rng.U();
             const float sint = sqrtf(fmaxf(0.f, (1.0f - cost) * (1.0f + cost)));
@@ -655,11 +722,11 @@ __global__ void __launch_bounds__(256) ElectronPhase(PhaseArgs a) {
         if (what == 0) {
           if (!MoveToFace(J, p, step, s.axis)) {
             acc += p.e + (positron ? 2.0f * kEMC2f : 0.f);
-            atomicAdd(&J.cnt->escaped, double(p.e + (positron ? 2.0f * kEMC2f : 0.f)));
+            esc.Add(jobs, job, double(p.e + (positron ? 2.0f * kEMC2f : 0.f)));
             done = true;
           } else if (!Settle(J, p, s.sGeom, s.axis)) {
             acc += p.e + (positron ? 2.0f * kEMC2f : 0.f);
-            atomicAdd(&J.cnt->escaped, double(p.e + (positron ? 2.0f * kEMC2f : 0.f)));
+            esc.Add(jobs, job, double(p.e + (positron ? 2.0f * kEMC2f : 0.f)));
             done = true;
           }
         } else {
@@ -763,6 +830,7 @@ __global__ void __launch_bounds__(256) ElectronPhase(PhaseArgs a) {
   }
   // step counters: one atomic per warp
   for (int o = 16; o > 0; o >>= 1) nsteps += __shfl_down_sync(kFull, nsteps, o);
+  esc.Flush(jobs);
   if (lane == 0 && a.njobs > 0) atomicAdd(&a.jobs[0].cnt->steps, nsteps);
 }
 

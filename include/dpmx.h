@@ -108,6 +108,7 @@ typedef struct {
   int use_graph;             /* FP32: capture each batch in a CUDA graph (default 1) */
   int tag_beamlets;          /* FP32: also tally dose per beamlet (influence matrix) */
   int autotune;              /* 1: tune block size / chunk / aggregation on a sample */
+  int profile_phases;        /* FP32: time every phase launch (no graph); see dpmx_result_profile */
   void* stream;              /* cudaStream_t to run on, NULL = library stream */
 } dpmx_run_options;
 
@@ -138,6 +139,11 @@ double dpmx_result_elapsed_ms(const dpmx_result* r);
 long long dpmx_result_launches(const dpmx_result* r);
 /* chosen launch configuration: [block_size, blocks_per_sm, chunk_histories, tally_aggregate] */
 int dpmx_result_config(const dpmx_result* r, long long* cfg4);
+/* phase profile of a run with profile_phases = 1 (zeros otherwise), 10 values:
+ * electron-phase ms, photon-phase ms, electron-phase launches, photon-phase
+ * launches, electron sub-steps, photon steps, electrons transported, photons
+ * transported, histories, total ms */
+int dpmx_result_profile(const dpmx_result* r, double* out10);
 void dpmx_result_free(dpmx_result* r);
 
 /* ---- drop-in for Simulate(...) ---- */
