@@ -100,6 +100,9 @@ def library():
         "dpmx_simulate": (C.c_int, [P, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int, C.c_uint64, C.c_int,
                                     _dp, _dp, C.c_int, C.POINTER(C.c_int)]),
         "dpmx_write_hist": (C.c_int, [P, C.c_char_p, C.c_int, C.c_double, C.c_int, _dp, _dp, C.c_int]),
+        "dpmx_simulate_noalloc": (C.c_int, [P, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int, C.c_uint64,
+                                            C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_int),
+                                            C.c_void_p]),
         "dpmx_sampler_eval": (C.c_int, [P, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, C.c_int]),
         "dpmx_table_eval": (C.c_int, [P, C.c_int, C.c_int, C.c_int, _dp, _dp, C.c_int]),
         "dpmx_simulate_histories": (C.c_int, [P, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int, C.c_uint64,
@@ -133,7 +136,7 @@ def exported_symbols():
             "dpmx_run", "dpmx_result_tally", "dpmx_result_tally_device", "dpmx_result_stats",
             "dpmx_result_elapsed_ms", "dpmx_result_launches", "dpmx_result_config", "dpmx_result_profile",
             "dpmx_result_free",
-            "dpmx_simulate", "dpmx_write_hist", "dpmx_sampler_eval", "dpmx_table_eval", "dpmx_simulate_histories",
+            "dpmx_simulate", "dpmx_simulate_noalloc", "dpmx_write_hist", "dpmx_sampler_eval", "dpmx_table_eval", "dpmx_simulate_histories",
             "dpmx_influence_build", "dpmx_csr_shape", "dpmx_csr_device", "dpmx_csr_spmv", "dpmx_csr_spmv_t",
             "dpmx_csr_download", "dpmx_csr_free"]
 

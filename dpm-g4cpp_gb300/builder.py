@@ -34,6 +34,7 @@ CU_UNITS = {
     "api.cu": [],
     "run.cu": [],
     "influence.cu": [],
+    "noalloc.cu": [],
 }
 CXX_UNITS = ["host_tables.cpp"]
 

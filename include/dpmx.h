@@ -153,6 +153,20 @@ void dpmx_result_free(dpmx_result* r);
 int dpmx_simulate(const dpmx_tables* t, int nprimary, double eprimary, int iselectron, double lbox,
                   int geom_index, uint64_t seed, int precision, double* edep_hist, double* step_hist,
                   int cap, int* hist_len);
+/* The same workload in the FP64 plain form for callers that must not have the
+ * library allocate device memory (a plug-in inside a framework that owns all
+ * device memory through its own pool, or a latency-critical caller for whom a
+ * cudaMalloc would synchronise the device). No counterpart in the reference.
+ * edep, edep2 (may be NULL) and steps are caller-owned DEVICE arrays of `bins`
+ * doubles (depth bins of lbox); bins must cover the geometry's depth bins and
+ * may not exceed 8192. The library's scratch is a fixed 65 KB device array
+ * shared by all calls: calls that overlap on the GPU race and must be
+ * serialised; the first call on a device looks the array up and should come
+ * before any stream capture. Runs on `stream` (NULL: default stream) and
+ * returns after it has finished. */
+int dpmx_simulate_noalloc(const dpmx_tables* t, int nprimary, double eprimary, int iselectron, double lbox,
+                          int geom_index, uint64_t seed, double* edep, double* edep2, double* steps, int bins,
+                          int* hist_len, void* stream);
 /* writes hist.sim exactly as Geom::Write */
 int dpmx_write_hist(const dpmx_tables* t, const char* fname, int geom_index, double lbox, int nprimary,
                     const double* edep_hist, const double* step_hist, int hist_len);
