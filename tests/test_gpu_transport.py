@@ -41,12 +41,17 @@ def oracle_batches(oracle, nb, per, e, ise, geom, seed0):
 
 
 def compare_depth_dose(g, sg, o, so):
-    """fraction of bins above 10% Dmax within combined 2 sigma, mean |rel diff| there"""
+    """For the bins above 10% of Dmax: fraction within combined 2 sigma, the
+    mean |relative difference| in excess of the statistical expectation
+    (E|N(0, s)| = 0.8 s per bin), and the mean signed relative difference."""
     m = min(len(g), len(o))
     g, sg, o, so = g[:m], sg[:m], o[:m], so[:m]
     mask = o > 0.1 * o.max()
-    z = np.abs(g[mask] - o[mask]) / np.sqrt(sg[mask] ** 2 + so[mask] ** 2)
-    return np.mean(z < 2.0), np.mean(np.abs(g[mask] - o[mask]) / o[mask])
+    s = np.sqrt(sg[mask] ** 2 + so[mask] ** 2)
+    z = np.abs(g[mask] - o[mask]) / s
+    rel = (g[mask] - o[mask]) / o[mask]
+    noise = np.mean(0.8 * s / o[mask])
+    return np.mean(z < 2.0), max(0.0, np.mean(np.abs(rel)) - noise), np.mean(rel)
 
 
 @pytest.mark.parametrize("ise", [True, False])
@@ -58,9 +63,10 @@ def test_fp64_depth_dose_statistical(tables_c3, oracle_c3, dpm, ise):
     d, d2, _ = res.tally(0)
     assert res.stats(0).lost == 0
     o, so = oracle_batches(oracle_c3, 10, 10000 if ise else 20000, 15.0, ise, 3, 100)
-    frac, mrel = compare_depth_dose(d / n, batch_sigma(d, d2, 10) / n, o, so)
+    frac, excess, bias = compare_depth_dose(d / n, batch_sigma(d, d2, 10) / n, o, so)
     assert frac >= 0.85, frac
-    assert mrel < 0.01, mrel
+    assert excess < 0.01, excess    # mean |diff| beyond statistics: <= 1 %
+    assert abs(bias) < 0.005, bias  # no systematic offset
 
 
 @pytest.mark.parametrize("ise", [True, False])
@@ -73,9 +79,10 @@ def test_fp32_depth_dose_vs_oracle(tables_c3, oracle_c3, dpm, ise):
     st = res.stats(0)
     assert st.lost == 0 and st.residual_violations == 0, st
     o, so = oracle_batches(oracle_c3, 10, 10000 if ise else 20000, 15.0, ise, 3, 200)
-    frac, mrel = compare_depth_dose(d / n, batch_sigma(d, d2, 10) / n, o, so)
+    frac, excess, bias = compare_depth_dose(d / n, batch_sigma(d, d2, 10) / n, o, so)
     assert frac >= 0.85, frac
-    assert mrel < 0.01, mrel
+    assert excess < 0.01, excess    # mean |diff| beyond statistics: <= 1 %
+    assert abs(bias) < 0.005, bias  # no systematic offset
 
 
 def test_fp32_energy_conservation(tables_wlb, dpm):
