@@ -44,7 +44,8 @@ class _Source(C.Structure):
 
 
 class _Job(C.Structure):
-    _fields_ = [("phantom", C.c_void_p), ("source", _Source), ("histories", C.c_longlong), ("seed", C.c_uint64)]
+    _fields_ = [("phantom", C.c_void_p), ("source", _Source), ("histories", C.c_longlong), ("seed", C.c_uint64),
+                ("first_history", C.c_longlong)]
 
 
 class _Opts(C.Structure):
@@ -269,6 +270,7 @@ class Job:
     source: Source = field(default_factory=Source)
     histories: int = 1000
     seed: int = 12345
+    first_history: int = 0
 
 
 @dataclass
@@ -358,7 +360,7 @@ def run(tables, jobs, precision=FP32_EVENT, batches=10, block_size=0, blocks_per
     arr = (_Job * len(jobs))()
     for i, j in enumerate(jobs):
         arr[i] = _Job(j.phantom.handle.value if hasattr(j.phantom.handle, "value") else j.phantom.handle,
-                      j.source._c(), int(j.histories), int(j.seed))
+                      j.source._c(), int(j.histories), int(j.seed), int(j.first_history))
     o = _Opts()
     L.dpmx_run_options_default(C.byref(o))
     o.precision = precision

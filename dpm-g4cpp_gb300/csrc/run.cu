@@ -79,7 +79,7 @@ std::vector<Chunk> PlanBatch(const dpmx_job* jobs, int njobs, int b, int B, long
       const long long take = std::min(left, chunk - cur.nslots);
       Segment s{};
       s.job = j;
-      s.firstHist = first;
+      s.firstHist = jobs[j].first_history + first;
       s.count = take;
       s.slotBase = cur.nslots;
       if (jobs[j].source.particle == 0) { s.prefix = cur.nP; cur.nP += take; cur.segP.push_back(s); }
@@ -401,11 +401,13 @@ int RunFp64(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
       double* he = histEdep ? histEdep + histOff + lo : nullptr;
       if (ph->kind == 0) {
         SlabGeomD g{ph->geomIndex, ph->lbox, 1.0 / ph->lbox, 0.5 * ph->lbox};
-        CK(LaunchFp64Slab(T->t64, g, density, src, lo, hi - lo, jobs[j].seed, tB, o.d_steps, int(o.tallySize),
+        CK(LaunchFp64Slab(T->t64, g, density, src, jobs[j].first_history + lo, hi - lo, jobs[j].seed, tB, o.d_steps,
+                          int(o.tallySize),
                           maxIz + j, he, cnt + j, blocks, st));
       } else {
         GridGeom g = ph->grid;
-        CK(LaunchFp64Grid(T->t64, g, density, src, lo, hi - lo, jobs[j].seed, tB, he, cnt + j, blocks, st));
+        CK(LaunchFp64Grid(T->t64, g, density, src, jobs[j].first_history + lo, hi - lo, jobs[j].seed, tB, he,
+                          cnt + j, blocks, st));
       }
       CK(LaunchFold(tB, o.d_dose, o.d_dose2, o.tallySize, st));
       nl += 2;
@@ -469,7 +471,8 @@ int CheckJobs(const dpmx_tables* t, const dpmx_job* jobs, int njobs) {
   for (int j = 0; j < njobs; ++j) {
     const dpmx_job& J = jobs[j];
     if (!J.phantom || J.phantom->tables != t) return Fail(DPMX_ERR_ARG, "job phantom missing or built on other tables");
-    if (J.histories < 0 || J.histories > 0xffffffffLL) return Fail(DPMX_ERR_ARG, "histories must be in [0, 2^32)");
+    if (J.histories < 0 || J.first_history < 0 || J.first_history + J.histories > 0xffffffffLL)
+      return Fail(DPMX_ERR_ARG, "history indices must lie in [0, 2^32)");
     const dpmx_source& s = J.source;
     if (s.particle != -1 && s.particle != 0) return Fail(DPMX_ERR_ARG, "source particle must be -1 (e-) or 0 (photon)");
     const double emax = t->h.dedx[0].x.back();

@@ -96,6 +96,9 @@ typedef struct {
   dpmx_source source;
   long long histories;
   uint64_t seed;
+  long long first_history;   /* index of the job's first history: history h always
+                                uses random stream h, so a job split into ranges
+                                (e.g. across GPUs) sums to the unsplit result */
 } dpmx_job;
 
 typedef struct {

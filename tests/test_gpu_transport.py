@@ -31,13 +31,26 @@ def test_fp64_histories_match_oracle(tables_c3, oracle_c3, dpm, ise, e, geom):
 
 
 def oracle_batches(oracle, nb, per, e, ise, geom, seed0):
-    """per-history mean depth dose and its standard error from nb oracle runs"""
+    """per-history mean depth dose, its standard error, and the per-batch
+    arrays (nb x bins) from nb oracle runs of `per` histories"""
     runs = [oracle.simulate_slab(per, e, ise, 1.0, geom, seed0 + k)[0] for k in range(nb)]
     m = max(len(r) for r in runs)
     a = np.zeros((nb, m))
     for k, r in enumerate(runs):
         a[k, :len(r)] = r / per
-    return a.mean(0), a.std(0, ddof=1) / np.sqrt(nb)
+    return a.mean(0), a.std(0, ddof=1) / np.sqrt(nb), a
+
+
+def total_dose_z(g, n_g, batches, per):
+    """z-score of the GPU total dose (bins above 10% Dmax) against the oracle's;
+    the per-history spread measured on the oracle batches gives both sigmas"""
+    o = batches.mean(0)
+    m = min(len(g), len(o))
+    mask = o[:m] > 0.1 * o.max()
+    tot_b = batches[:, :m][:, mask].sum(1)
+    sd_hist = tot_b.std(ddof=1) * np.sqrt(per)
+    s = np.sqrt(sd_hist ** 2 / n_g + tot_b.var(ddof=1) / len(tot_b))
+    return (g[:m][mask].sum() - tot_b.mean()) / s
 
 
 def compare_depth_dose(g, sg, o, so):
@@ -62,11 +75,13 @@ def test_fp64_depth_dose_statistical(tables_c3, oracle_c3, dpm, ise):
     res = dpm.run(tables_c3, [dpm.Job(ph, src, n, 11)], precision=dpm.FP64_PLAIN, batches=10)
     d, d2, _ = res.tally(0)
     assert res.stats(0).lost == 0
-    o, so = oracle_batches(oracle_c3, 10, 10000 if ise else 20000, 15.0, ise, 3, 100)
+    per = 10000 if ise else 20000
+    o, so, ob = oracle_batches(oracle_c3, 10, per, 15.0, ise, 3, 100)
     frac, excess, bias = compare_depth_dose(d / n, batch_sigma(d, d2, 10) / n, o, so)
     assert frac >= 0.85, frac
     assert excess < 0.01, excess    # mean |diff| beyond statistics: <= 1 %
-    assert abs(bias) < 0.005, bias  # no systematic offset
+    z = total_dose_z(d / n, n, ob, per)
+    assert abs(z) < 3.5, (z, bias)  # no systematic offset of the integral dose
 
 
 @pytest.mark.parametrize("ise", [True, False])
@@ -78,11 +93,13 @@ def test_fp32_depth_dose_vs_oracle(tables_c3, oracle_c3, dpm, ise):
     d, d2, steps = res.tally(0)
     st = res.stats(0)
     assert st.lost == 0 and st.residual_violations == 0, st
-    o, so = oracle_batches(oracle_c3, 10, 10000 if ise else 20000, 15.0, ise, 3, 200)
+    per = 10000 if ise else 20000
+    o, so, ob = oracle_batches(oracle_c3, 10, per, 15.0, ise, 3, 200)
     frac, excess, bias = compare_depth_dose(d / n, batch_sigma(d, d2, 10) / n, o, so)
     assert frac >= 0.85, frac
     assert excess < 0.01, excess    # mean |diff| beyond statistics: <= 1 %
-    assert abs(bias) < 0.005, bias  # no systematic offset
+    z = total_dose_z(d / n, n, ob, per)
+    assert abs(z) < 3.5, (z, bias)  # no systematic offset of the integral dose
 
 
 def test_fp32_energy_conservation(tables_wlb, dpm):
