@@ -131,6 +131,10 @@ cudaError_t LaunchSamplerEval32(const DevTables<float>& T, int s, int imat, cons
 cudaError_t LaunchTableEval32(const DevTables<float>& T, int q, int imat, const double* e, double* out, int n,
                               cudaStream_t st);
 int ElectronPhaseSmemBytes(const DevTables<float>& T);
+// block-batched electron phase (256 threads per block, shared-memory slots)
+int BlockPhaseSmemBytes(const DevTables<float>& T);
+cudaError_t PrepareBlockPhase(const DevTables<float>& T);
+cudaError_t LaunchElectronPhaseBlock(const PhaseArgs& a, int blocks, cudaStream_t st);
 
 // ---- influence matrix (influence.cu) ----
 cudaError_t LaunchCountNnz(const double* dense, long long nvox, int nb, double thr, long long* rowCount,

@@ -34,9 +34,10 @@ constexpr int kCtrPerChunk = 2 * kCntStride + 2 * (kGen + 1) + 1;
 
 struct Cfg {
   int threads = 256;
-  int blocksPerSM = 2;
+  int blocksPerSM = 3;
   long long chunk = 1 << 20;
   int aggregate = 0;
+  int eblock = 0;          // electron phase: 0 lane-refill kernel, 1 block-batched kernel
 };
 
 struct DevBuf {       // owned device allocations of one run
@@ -186,6 +187,8 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
     if (int rc = AllocQueue(buf, qp[k], cap)) return rc;
   }
   const int blocks = nsm * cfg.blocksPerSM;
+  const int eblocks = nsm * 2;   // block-batched electron phase: 2 resident blocks per SM
+  if (cfg.eblock) CK(PrepareBlockPhase(T->t32));
   long long nl = 0;
   auto enqueue = [&](cudaStream_t s) -> int {
     size_t segCur = 0, ci = 0;
@@ -238,7 +241,8 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
             CK(cudaEventCreate(&evE.back()));
             CK(cudaEventRecord(evE[evE.size() - 2], s));
           }
-          CK(LaunchElectronPhase(a, blocks, cfg.threads, s));
+          if (cfg.eblock) CK(LaunchElectronPhaseBlock(a, eblocks, s));
+          else CK(LaunchElectronPhase(a, blocks, cfg.threads, s));
           if (profile) CK(cudaEventRecord(evE.back(), s));
           ++nl;
         }
@@ -489,11 +493,12 @@ int CheckJobs(const dpmx_tables* t, const dpmx_job* jobs, int njobs) {
 
 Cfg DefaultCfg(const dpmx_run_options* o, long long totalHist) {
   Cfg c;
-  if (o && o->block_size > 0) c.threads = o->block_size;
+  if (o && o->block_size > 0) c.threads = std::min(256, std::max(32, o->block_size / 32 * 32));
   if (o && o->blocks_per_sm > 0) c.blocksPerSM = o->blocks_per_sm;
   if (o && o->chunk_histories > 0) c.chunk = o->chunk_histories;
   else c.chunk = std::max<long long>(1 << 14, std::min<long long>(1 << 21, totalHist));
   if (o && o->tally_aggregate >= 0) c.aggregate = o->tally_aggregate;
+  if (o && o->electron_kernel >= 0) c.eblock = o->electron_kernel;
   return c;
 }
 
@@ -504,8 +509,10 @@ int Autotune(const dpmx_tables* t, const dpmx_job* jobs, int njobs, const Cfg& b
   const long long sample = std::min<long long>(total, 1 << 18);
   std::vector<dpmx_job> sj(jobs, jobs + njobs);
   for (auto& j : sj) j.histories = std::max<long long>(1, (long long)(double(j.histories) * sample / std::max(1LL, total)));
-  struct Cand { int threads, bps, agg; };
-  const Cand cands[] = {{256, 2, 0}, {256, 2, 1}, {128, 4, 0}, {512, 1, 0}, {256, 3, 0}, {128, 6, 0}};
+  struct Cand { int threads, bps, agg, eblock; };
+  // the phase kernels are compiled for at most 256 threads per block
+  const Cand cands[] = {{256, 3, 0, 0}, {256, 3, 1, 0}, {256, 2, 0, 0}, {128, 6, 0, 0},
+                        {256, 3, 0, 1}, {256, 3, 1, 1}, {256, 2, 0, 1}};
   double bestMs = 1e30;
   *best = base;
   for (const Cand& c : cands) {
@@ -513,6 +520,7 @@ int Autotune(const dpmx_tables* t, const dpmx_job* jobs, int njobs, const Cfg& b
     cfg.threads = c.threads;
     cfg.blocksPerSM = c.bps;
     cfg.aggregate = c.agg;
+    cfg.eblock = c.eblock;
     cfg.chunk = sample;
     std::vector<JobOut> outs;
     if (int rc = PrepareOutputs(sj.data(), njobs, false, outs)) return rc;
@@ -560,7 +568,8 @@ int dpmx_run(const dpmx_tables* t, const dpmx_job* jobs, int njobs, const dpmx_r
       if (!rc)
         rc = RunFp32(t, jobs, njobs, o.batches, cfg, tag, o.use_graph != 0 && !o.profile_phases, st, r->jobs, &r->ms,
                      &r->launches, o.profile_phases ? r->prof : nullptr);
-      r->cfg[0] = cfg.threads; r->cfg[1] = cfg.blocksPerSM; r->cfg[2] = cfg.chunk; r->cfg[3] = cfg.aggregate;
+      r->cfg[0] = cfg.threads; r->cfg[1] = cfg.blocksPerSM; r->cfg[2] = cfg.chunk;
+      r->cfg[3] = cfg.aggregate | (cfg.eblock << 1);
     }
   }
   if (ownStream) cudaStreamDestroy(st);

@@ -834,6 +834,434 @@ __global__ void __launch_bounds__(256) ElectronPhase(PhaseArgs a) {
   if (lane == 0 && a.njobs > 0) atomicAdd(&a.jobs[0].cnt->steps, nsteps);
 }
 
+// ---------------------------------------------------------------------------
+// electron phase, block-batched: kSlots electrons per block live in shared
+// memory; every iteration of the block refills idle slots, advances every
+// active electron by one condensed-history sub-step (all threads), and then
+// runs each kind of interaction over a compacted list of the electrons that
+// reached it, so that the code of one interaction runs with full warps.
+// ---------------------------------------------------------------------------
+constexpr int kSlots = 512;
+constexpr uint32_t kFAxis = 3u, kFHinge = 4u, kFNeedGeom = 8u, kFPositron = 16u, kFAlive = 32u;
+
+struct SlotArrays {     // shared-memory state of the resident electrons
+  uint32_t vox[kSlots];
+  float lx[kSlots], ly[kSlots], lz[kSlots], dx[kSlots], dy[kSlots], dz[kSlots], e[kSlots];
+  float nTr1[kSlots], nTr10[kSlots], nMol[kSlots], invMol[kSlots], nBrem[kSlots], ekin0[kSlots], sGeom[kSlots];
+  uint32_t flags[kSlots];   // axis (2 bits), hinge, needGeom, positron, alive; job << 8
+  uint32_t hist[kSlots], slot[kSlots], ulo[kSlots], uhi[kSlots], ctr[kSlots], pst[kSlots];
+  double acc[kSlots];
+};
+struct SlotLists {
+  uint16_t active[kSlots], idle[kSlots], hinge[kSlots], mscEnd[kSlots], brem[kSlots], moller[kSlots];
+  int nActive, nIdle, nHinge, nMscEnd, nBrem, nMoller, nFill, exhausted;
+  unsigned long long fillBase;
+};
+
+__host__ __device__ constexpr size_t BlockPhaseStaticBytes() { return sizeof(SlotArrays) + sizeof(SlotLists); }
+
+// warp-aggregated push of v onto a shared list
+__device__ __forceinline__ void Push(uint16_t* list, int* n, int v) {
+  cg::coalesced_group g = cg::coalesced_threads();
+  int base = 0;
+  if (g.thread_rank() == 0) base = atomicAdd(n, int(g.size()));
+  base = g.shfl(base, 0);
+  list[base + g.thread_rank()] = uint16_t(v);
+}
+
+__device__ __forceinline__ void LoadSlot(const SlotArrays& S, int k, PState& p, EState& s, uint32_t& fl) {
+  const uint32_t v = S.vox[k];
+  p.ix = int(v & 0x7ffu); p.iy = int((v >> 11) & 0x7ffu); p.iz = int(v >> 22);
+  p.lx = S.lx[k]; p.ly = S.ly[k]; p.lz = S.lz[k];
+  p.dx = S.dx[k]; p.dy = S.dy[k]; p.dz = S.dz[k];
+  p.e = S.e[k];
+  fl = S.flags[k];
+  p.hist = S.hist[k]; p.slot = S.slot[k]; p.ulo = S.ulo[k]; p.uhi = S.uhi[k];
+  p.meta = ((fl >> 8) << 2) | ((fl & kFPositron) ? 2u : 1u);
+  s.nTr1 = S.nTr1[k]; s.nTr10 = S.nTr10[k]; s.nMol = S.nMol[k]; s.invMol = S.invMol[k];
+  s.nBrem = S.nBrem[k]; s.ekin0 = S.ekin0[k]; s.sGeom = S.sGeom[k];
+  s.axis = int(fl & kFAxis);
+  s.hinge = (fl & kFHinge) != 0;
+  s.needGeom = (fl & kFNeedGeom) != 0;
+}
+
+__device__ __forceinline__ void StoreSlot(SlotArrays& S, int k, const PState& p, const EState& s, bool alive) {
+  S.vox[k] = PackVox(p.ix, p.iy, p.iz);
+  S.lx[k] = p.lx; S.ly[k] = p.ly; S.lz[k] = p.lz;
+  S.dx[k] = p.dx; S.dy[k] = p.dy; S.dz[k] = p.dz;
+  S.e[k] = p.e;
+  S.nTr1[k] = s.nTr1; S.nTr10[k] = s.nTr10; S.nMol[k] = s.nMol; S.invMol[k] = s.invMol;
+  S.nBrem[k] = s.nBrem; S.ekin0[k] = s.ekin0; S.sGeom[k] = s.sGeom;
+  S.flags[k] = (uint32_t(s.axis) & kFAxis) | (s.hinge ? kFHinge : 0u) | (s.needGeom ? kFNeedGeom : 0u) |
+               ((p.meta & 3u) == 2u ? kFPositron : 0u) | (alive ? kFAlive : 0u) | ((p.meta >> 2) << 8);
+}
+
+// random stream of slot k (a fresh Philox block per use; the counter advances)
+__device__ __forceinline__ void SlotRng(const SlotArrays& S, int k, const JobF& J, const PState& p, PRng& r) {
+  r.Init(J.k0, J.k1, p.hist, p.ulo, p.uhi);
+  r.ctr = S.ctr[k];
+}
+
+// e+ annihilation at rest: two back-to-back 0.511 MeV photons (SimDPMLike.cc:753-791)
+__device__ __forceinline__ void AnnihilateF(const PhaseArgs& a, const PState& p, PRng& rng, double& acc) {
+  const float cost = 1.0f - 2.0f * rng.U();
+  const float sint = sqrtf(fmaxf(0.f, (1.0f - cost) * (1.0f + cost)));
+  const float phi = 2.0f * kPIf * rng.U();
+  float sn, cs;
+  __sincosf(phi, &sn, &cs);
+  PState g = p;
+  g.e = kEMC2f; g.meta = 0u | (p.meta & ~3u);
+  g.dx = sint * cs; g.dy = sint * sn; g.dz = cost;
+  rng.Child(0, g.ulo, g.uhi);
+  if (!Append(a.outP, a.outPCount, a.overflow, g)) acc += kEMC2f;
+  g.dx = -g.dx; g.dy = -g.dy; g.dz = -g.dz;
+  rng.Child(1, g.ulo, g.uhi);
+  if (!Append(a.outP, a.outPCount, a.overflow, g)) acc += kEMC2f;
+}
+
+// one condensed-history sub-step of slot k. Returns 0 to keep stepping,
+// 1 brem, 2 Moller, 3 MSC hinge, 4 MSC step end, 5 finished.
+__device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, const JobF* jobs, SlotArrays& S,
+                                        int k, EscTally& esc, unsigned long long& nsteps) {
+  const DevTables<float>& T = a.T;
+  PState p;
+  EState s;
+  uint32_t fl;
+  LoadSlot(S, k, p, s, fl);
+  const int job = int(fl >> 8);
+  const JobF& J = jobs[job];
+  const bool positron = (fl & kFPositron) != 0;
+  double acc = S.acc[k];
+  int code = 0;
+  int im = -1;
+  if (s.needGeom) {
+    if (Settle(J, p, s.sGeom, s.axis)) im = MaterialAt(J, p.ix, p.iy, p.iz);
+    s.needGeom = false;
+  } else {
+    im = MaterialAt(J, p.ix, p.iy, p.iz);
+  }
+  const uint32_t pst = S.pst[k] + 1;
+  S.pst[k] = pst;
+  if (im < 0) {
+    const float out = p.e + (positron ? 2.0f * kEMC2f : 0.f);
+    acc += out;
+    esc.Add(jobs, job, double(out));
+    code = 5;
+  } else if (pst > kMaxElectronSteps) {
+    acc += p.e + (positron ? 2.0f * kEMC2f : 0.f);
+    atomicAdd(&J.cnt->lost, 1ull);
+    code = 5;
+  } else {
+    ++nsteps;
+    const float ecut = T.ecut;
+    const float rho = T.density[im];
+    float step = s.sGeom;
+    int what = 0;
+    const float le = __logf(p.e);
+    float dedx = SplineLe(et.dedx[im], p.e, le) * rho;
+    float emid = fmaxf(p.e - 0.5f * step * dedx, ecut);
+    const float lm = __logf(emid);
+    float dTr1 = SplineLe(et.itr1[im], emid, lm) * rho;
+    const float dMol = s.invMol * T.mollerScale[im] * rho;
+    const float dBrem = SplineLe(et.brem[im], emid, lm) * rho;
+    const float sBrem = s.nBrem / dBrem;
+    if (sBrem < step) { step = sBrem; what = 1; }
+    const float sMol = s.nMol / dMol;
+    if (sMol < step) { step = sMol; what = 2; }
+    float sEl = s.nTr1 / dTr1;
+    if (sEl < step) {
+      sEl = s.nTr1 / (SplineLe(et.itr1[im], p.e, le) * rho);
+      emid = fmaxf(p.e - 0.5f * sEl * dedx, ecut);
+      dTr1 = SplineLe(et.itr1[im], emid, __logf(emid)) * rho;
+      sEl = fminf(step, s.nTr1 / dTr1);
+      step = sEl;
+      what = 3;
+    }
+    s.nBrem = (what == 1) ? 0.f : s.nBrem - step * dBrem;
+    s.nMol = (what == 2) ? 0.f : s.nMol - step * dMol;
+    s.nTr1 = (what == 3) ? 0.f : s.nTr1 - step * dTr1;
+    emid = fmaxf(p.e - 0.5f * step * dedx, ecut);
+    dedx = SplineLe(et.dedx[im], emid, __logf(emid)) * rho;
+    const float de = step * dedx;
+    const float ef = p.e - de;
+    if (ef < ecut) {
+      const float edep = p.e;
+      p.e = 0.f;
+      if (!positron) {
+        Score(J, p.ix, p.iy, p.iz, p.hist, edep, a.aggregate);
+        acc += edep;
+      } else {
+        bool inside;
+        if (what == 0) inside = MoveToFace(J, p, step, s.axis);
+        else { p.lx += step * p.dx; p.ly += step * p.dy; p.lz += step * p.dz; inside = true; }
+        const int im2 = inside ? MaterialAt(J, p.ix, p.iy, p.iz) : -1;
+        if (im2 < 0) {
+          acc += edep + 2.0f * kEMC2f;
+          esc.Add(jobs, job, double(edep + 2.0f * kEMC2f));
+        } else {
+          PRng rng;
+          SlotRng(S, k, J, p, rng);
+          AnnihilateF(a, p, rng, acc);
+          Score(J, p.ix, p.iy, p.iz, p.hist, edep, a.aggregate);
+          acc += edep;
+        }
+      }
+      code = 5;
+    } else {
+      p.e = ef;
+      Score(J, p.ix, p.iy, p.iz, p.hist, de, a.aggregate);
+      acc += de;
+      if (what == 0) {
+        if (!MoveToFace(J, p, step, s.axis) || !Settle(J, p, s.sGeom, s.axis)) {
+          const float out = p.e + (positron ? 2.0f * kEMC2f : 0.f);
+          acc += out;
+          esc.Add(jobs, job, double(out));
+          code = 5;
+        }
+      } else {
+        p.lx += step * p.dx; p.ly += step * p.dy; p.lz += step * p.dz;
+        s.needGeom = true;
+        code = (what == 3) ? (s.hinge ? 3 : 4) : what;
+      }
+    }
+  }
+  if (code == 5) {
+    atomicAdd(a.histE + p.slot, acc);
+    S.flags[k] = 0u;
+  } else {
+    S.acc[k] = acc;
+    StoreSlot(S, k, p, s, true);
+  }
+  return code;
+}
+
+// GS angular deflection at the MSC hinge (SimDPMLike.cc:216-226, :731-750)
+__device__ __forceinline__ void EventHinge(const PhaseArgs& a, const JobF* jobs, SlotArrays& S, int k) {
+  PState p;
+  EState s;
+  uint32_t fl;
+  LoadSlot(S, k, p, s, fl);
+  PRng rng;
+  SlotRng(S, k, jobs[fl >> 8], p, rng);
+  const float r2 = rng.U(), r1 = rng.U();
+  const float d = SampleGS(a.T.gs, s.ekin0, r1, r2);
+  const float cost = fmaxf(-1.0f, fminf(1.0f, d));
+  const float sint = sqrtf(fmaxf(0.f, (1.0f - cost) * (1.0f + cost)));
+  const float phi = 2.0f * kPIf * rng.U();
+  float sn, cs;
+  __sincosf(phi, &sn, &cs);
+  float u1 = sint * cs, u2 = sint * sn, u3 = cost;
+  RotateToLab(u1, u2, u3, p.dx, p.dy, p.dz);
+  const float inv = rsqrtf(u1 * u1 + u2 * u2 + u3 * u3);
+  S.dx[k] = u1 * inv; S.dy[k] = u2 * inv; S.dz[k] = u3 * inv;
+  S.nTr1[k] = s.nTr10;
+  S.flags[k] = fl & ~kFHinge;
+  S.ctr[k] = rng.ctr;
+}
+
+// end of an MSC step: new scattering strength and hinge (SimDPMLike.cc:227-237)
+__device__ __forceinline__ void EventMscEnd(const PhaseArgs& a, const ETables& et, const JobF* jobs, SlotArrays& S,
+                                            int k) {
+  const uint32_t fl = S.flags[k];
+  const JobF& J = jobs[fl >> 8];
+  PRng rng;
+  rng.Init(J.k0, J.k1, S.hist[k], S.ulo[k], S.uhi[k]);
+  rng.ctr = S.ctr[k];
+  const float e = S.e[k];
+  const float k1 = SplineLe(et.k1, e, __logf(e));
+  const float n0 = rng.U() * k1;
+  S.ekin0[k] = e;
+  S.nTr10[k] = n0;
+  S.nTr1[k] = k1 - n0;
+  S.flags[k] = fl | kFHinge;
+  S.ctr[k] = rng.ctr;
+}
+
+// bremsstrahlung (SimDPMLike.cc:172-194, :661-695)
+__device__ __forceinline__ void EventBrem(const PhaseArgs& a, const JobF* jobs, SlotArrays& S, SlotLists& L, int k) {
+  PState p;
+  EState s;
+  uint32_t fl;
+  LoadSlot(S, k, p, s, fl);
+  const JobF& J = jobs[fl >> 8];
+  const DevTables<float>& T = a.T;
+  PRng rng;
+  SlotRng(S, k, J, p, rng);
+  double acc = S.acc[k];
+  const int im = MaterialAt(J, p.ix, p.iy, p.iz);
+  if (p.e > T.gcut && im >= 0) {
+    const float r3 = rng.U(), r2 = rng.U(), r1 = rng.U();
+    const float eg = SampleSB(T.sb[im], p.e, r1, r2, r3);
+    const float dum0 = (kEMC2f * 0.7071067812f) / (p.e + kEMC2f);
+    const float cost = fmaxf(-1.0f, fminf(1.0f, 1.0f - dum0 * dum0));
+    const float sint = sqrtf(fmaxf(0.f, (1.0f + cost) * (1.0f - cost)));
+    const float phi = 2.0f * kPIf * rng.U();
+    float sn, cs;
+    __sincosf(phi, &sn, &cs);
+    PState g = p;
+    g.e = eg; g.meta = 0u | (p.meta & ~3u);
+    g.dx = sint * cs; g.dy = sint * sn; g.dz = cost;
+    RotateToLab(g.dx, g.dy, g.dz, p.dx, p.dy, p.dz);
+    rng.Child(0, g.ulo, g.uhi);
+    if (!Append(a.outP, a.outPCount, a.overflow, g)) acc += eg;
+    p.e -= eg;
+  }
+  if (p.e < T.ecut) {
+    Score(J, p.ix, p.iy, p.iz, p.hist, p.e, a.aggregate);
+    acc += p.e;
+    if ((fl & kFPositron) != 0) AnnihilateF(a, p, rng, acc);
+    atomicAdd(a.histE + p.slot, acc);
+    S.flags[k] = 0u;
+    return;
+  }
+  S.e[k] = p.e;
+  S.nBrem[k] = -__logf(rng.U());
+  S.acc[k] = acc;
+  S.ctr[k] = rng.ctr;
+}
+
+// Moller delta electron (SimDPMLike.cc:204-214, :699-728)
+__device__ __forceinline__ void EventMoller(const PhaseArgs& a, const ETables& et, const JobF* jobs, SlotArrays& S,
+                                            int k) {
+  PState p;
+  EState s;
+  uint32_t fl;
+  LoadSlot(S, k, p, s, fl);
+  const JobF& J = jobs[fl >> 8];
+  PRng rng;
+  SlotRng(S, k, J, p, rng);
+  double acc = S.acc[k];
+  if (p.e > 2.0f * a.T.ecut) {
+    const float r3 = rng.U(), r2 = rng.U(), r1 = rng.U();
+    const float se = SampleMoller(a.T.mol, p.e, r1, r2, r3);
+    const float k2 = 2.0f * kEMC2f;
+    const float cost = fminf(1.0f, sqrtf(se * (p.e + k2) / (p.e * (se + k2))));
+    const float sint = sqrtf(fmaxf(0.f, (1.0f + cost) * (1.0f - cost)));
+    const float phi = 2.0f * kPIf * rng.U();
+    float sn, cs;
+    __sincosf(phi, &sn, &cs);
+    PState c = p;
+    c.e = se; c.meta = 1u | (p.meta & ~3u);
+    c.dx = sint * cs; c.dy = sint * sn; c.dz = cost;
+    RotateToLab(c.dx, c.dy, c.dz, p.dx, p.dy, p.dz);
+    rng.Child(0, c.ulo, c.uhi);
+    if (!Append(a.outE, a.outECount, a.overflow, c)) acc += se;
+    p.e -= se;
+  }
+  S.e[k] = p.e;
+  S.nMol[k] = -__logf(rng.U());
+  S.invMol[k] = SplineLe(et.moller, p.e, __logf(p.e));
+  S.acc[k] = acc;
+  S.ctr[k] = rng.ctr;
+}
+
+__global__ void __launch_bounds__(256, 2) ElectronPhaseB(PhaseArgs a) {
+  extern __shared__ __align__(16) unsigned char dyn[];
+  SlotArrays& S = *reinterpret_cast<SlotArrays*>(dyn);
+  SlotLists& L = *reinterpret_cast<SlotLists*>(dyn + sizeof(SlotArrays));
+  float* sdata = reinterpret_cast<float*>(dyn + BlockPhaseStaticBytes());
+  __shared__ ETables et;
+  __shared__ JobF sjobs[16];
+  __shared__ unsigned long long spre[kStripes + 1];
+  const bool fewJobs = a.njobs <= 16;
+  if (fewJobs)
+    for (int j = threadIdx.x; j < a.njobs; j += blockDim.x) sjobs[j] = a.jobs[j];
+  StageElectronTables(a.T, sdata, &et);
+  const unsigned long long nQ = StripePrefix(a.inCount, spre);
+  const JobF* jobs = fewJobs ? sjobs : a.jobs;
+  const unsigned long long total = (unsigned long long)a.nPrimaries + nQ;
+  if (total == 0) return;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  for (int k = tid; k < kSlots; k += nthr) S.flags[k] = 0u;
+  if (tid == 0) L.exhausted = 0;
+  __syncthreads();
+  EscTally esc;
+  unsigned long long nsteps = 0;
+  for (;;) {
+    // active / idle lists
+    if (tid == 0) { L.nActive = 0; L.nIdle = 0; }
+    __syncthreads();
+    for (int k = tid; k < kSlots; k += nthr) {
+      if (S.flags[k] & kFAlive) Push(L.active, &L.nActive, k);
+      else Push(L.idle, &L.nIdle, k);
+    }
+    __syncthreads();
+    // claim work for the idle slots (one atomic per block and iteration)
+    if (tid == 0) {
+      L.nHinge = L.nMscEnd = L.nBrem = L.nMoller = 0;
+      L.nFill = 0;
+      const int want = L.nIdle < 128 ? L.nIdle : 128;
+      if (!L.exhausted && want > 0) {
+        const unsigned long long base = atomicAdd(a.head, (unsigned long long)want);
+        if (base >= total) {
+          L.exhausted = 1;
+        } else {
+          L.fillBase = base;
+          L.nFill = int(total - base < (unsigned long long)want ? total - base : (unsigned long long)want);
+          if (base + want >= total) L.exhausted = 1;
+        }
+      }
+    }
+    __syncthreads();
+    for (int i = tid; i < L.nFill; i += nthr) {
+      const int k = L.idle[i];
+      const unsigned long long item = L.fillBase + i;
+      PState p;
+      PRng rng;
+      if (item < (unsigned long long)a.nPrimaries) {
+        MakePrimary(a, a.segs, (long long)item, p, rng);
+      } else {
+        LoadParticle(a.in, StripedIndex(a.in, spre, item - a.nPrimaries), p);
+        const JobF& J = jobs[p.meta >> 2];
+        rng.Init(J.k0, J.k1, p.hist, p.ulo, p.uhi);
+      }
+      const int job = int(p.meta >> 2);
+      const JobF& J = jobs[job];
+      if (!InBox(J, p.ix, p.iy, p.iz) || MaterialAt(J, p.ix, p.iy, p.iz) < 0) {
+        const double out = p.e + ((p.meta & 3u) == 2u ? 2.0 * kEMC2f : 0.0);
+        esc.Add(jobs, job, out);
+        atomicAdd(a.histE + p.slot, out);
+        continue;
+      }
+      EState s;
+      InitElectron(et, p, rng, s);
+      s.sGeom = 0.f;
+      s.axis = 0;
+      StoreSlot(S, k, p, s, true);
+      S.acc[k] = 0.0;
+      S.ctr[k] = rng.ctr;
+      S.pst[k] = 0;
+      Push(L.active, &L.nActive, k);
+    }
+    __syncthreads();
+    const int nAct = L.nActive, ex = L.exhausted;
+    __syncthreads();
+    if (nAct == 0) {
+      if (ex) break;
+      continue;
+    }
+    // one sub-step for every active electron
+    for (int i = tid; i < nAct; i += nthr) {
+      const int k = L.active[i];
+      const int code = StepSlot(a, et, jobs, S, k, esc, nsteps);
+      if (code == 1) Push(L.brem, &L.nBrem, k);
+      else if (code == 2) Push(L.moller, &L.nMoller, k);
+      else if (code == 3) Push(L.hinge, &L.nHinge, k);
+      else if (code == 4) Push(L.mscEnd, &L.nMscEnd, k);
+    }
+    __syncthreads();
+    // interactions, one kind at a time over compacted lists
+    for (int i = tid; i < L.nHinge; i += nthr) EventHinge(a, jobs, S, L.hinge[i]);
+    for (int i = tid; i < L.nMscEnd; i += nthr) EventMscEnd(a, et, jobs, S, L.mscEnd[i]);
+    for (int i = tid; i < L.nBrem; i += nthr) EventBrem(a, jobs, S, L, L.brem[i]);
+    for (int i = tid; i < L.nMoller; i += nthr) EventMoller(a, et, jobs, S, L.moller[i]);
+    __syncthreads();
+  }
+  esc.Flush(jobs);
+  for (int o = 16; o > 0; o >>= 1) nsteps += __shfl_down_sync(kFull, nsteps, o);
+  if ((tid & 31) == 0 && a.njobs > 0) atomicAdd(&a.jobs[0].cnt->steps, nsteps);
+}
+
 __global__ void FoldKernel(double* t, double* dose, double* dose2, long long n) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const double v = t[i];
@@ -909,6 +1337,19 @@ int ElectronPhaseSmemBytes(const DevTables<float>& T) { return int(T.elecCount *
 
 cudaError_t LaunchPhotonPhase(const PhaseArgs& a, int blocks, int threads, cudaStream_t st) {
   PhotonPhase<<<blocks, threads, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+int BlockPhaseSmemBytes(const DevTables<float>& T) {
+  return int(BlockPhaseStaticBytes() + size_t(T.elecCount) * sizeof(float));
+}
+
+cudaError_t PrepareBlockPhase(const DevTables<float>& T) {
+  return cudaFuncSetAttribute(ElectronPhaseB, cudaFuncAttributeMaxDynamicSharedMemorySize, BlockPhaseSmemBytes(T));
+}
+
+cudaError_t LaunchElectronPhaseBlock(const PhaseArgs& a, int blocks, cudaStream_t st) {
+  ElectronPhaseB<<<blocks, 256, BlockPhaseSmemBytes(a.T), st>>>(a);
   return cudaGetLastError();
 }
 

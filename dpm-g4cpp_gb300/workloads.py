@@ -83,8 +83,8 @@ def differentiation_setup(seed=4, n=128, v=2.0):
     rng = np.random.default_rng(seed)
     m = np.full((n, n, n), WATER, dtype=np.uint8)
     for mat in (BONE, LUNG):
-        size = rng.integers(10, 25, size=3)
-        lo = [int(rng.integers(5, n - 5 - s)) for s in size]
+        size = rng.integers(max(2, n // 13), max(3, n // 5), size=3)   # 10-25 voxels at n = 128
+        lo = [int(rng.integers(n // 25, n - n // 25 - s)) for s in size]
         m[lo[2]:lo[2] + size[2], lo[1]:lo[1] + size[1], lo[0]:lo[0] + size[0]] = mat
     src = Source(particle=0, spectrum=0, e0=6.0, e1=6.0, shape=2, cx=0.0, cy=0.0, fx=5.0, fy=5.0, nbx=20, nby=20)
     x = voxel_centres(n, v, -0.5 * n * v)

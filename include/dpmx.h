@@ -112,6 +112,9 @@ typedef struct {
   int tag_beamlets;          /* FP32: also tally dose per beamlet (influence matrix) */
   int autotune;              /* 1: tune block size / chunk / aggregation on a sample */
   int profile_phases;        /* FP32: time every phase launch (no graph); see dpmx_result_profile */
+  int electron_kernel;       /* FP32 electron phase: -1 default, 0 one electron per lane with
+                                refill, 1 block-batched (shared-memory slots, interactions
+                                processed over compacted per-type lists) */
   void* stream;              /* cudaStream_t to run on, NULL = library stream */
 } dpmx_run_options;
 
@@ -140,7 +143,8 @@ int dpmx_result_stats(const dpmx_result* r, int job, dpmx_job_stats* s);
 /* wall time of the transport (device events) [ms] and kernel launches issued */
 double dpmx_result_elapsed_ms(const dpmx_result* r);
 long long dpmx_result_launches(const dpmx_result* r);
-/* chosen launch configuration: [block_size, blocks_per_sm, chunk_histories, tally_aggregate] */
+/* chosen launch configuration: [block_size, blocks_per_sm, chunk_histories,
+ * tally_aggregate + 2 * electron_kernel] */
 int dpmx_result_config(const dpmx_result* r, long long* cfg4);
 /* phase profile of a run with profile_phases = 1 (zeros otherwise), 10 values:
  * electron-phase ms, photon-phase ms, electron-phase launches, photon-phase
