@@ -1228,6 +1228,12 @@ __global__ void __launch_bounds__(256, 2) ElectronPhaseB(PhaseArgs a) {
       s.sGeom = 0.f;
       s.axis = 0;
       StoreSlot(S, k, p, s, true);
+      // the particle's identity (history, energy-check slot, stream) is set
+      // once here; StoreSlot only writes the state that changes while stepping
+      S.hist[k] = p.hist;
+      S.slot[k] = p.slot;
+      S.ulo[k] = p.ulo;
+      S.uhi[k] = p.uhi;
       S.acc[k] = 0.0;
       S.ctr[k] = rng.ctr;
       S.pst[k] = 0;
