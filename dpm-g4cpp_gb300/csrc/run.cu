@@ -292,12 +292,12 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
   // results: leftovers beyond the last generation and queue overflows are losses
   std::vector<unsigned long long> hc(nchunks * kCtrPerChunk);
   CK(cudaMemcpy(hc.data(), ctr, hc.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
-  unsigned long long lost = 0;
+  unsigned long long lost = 0, leftover = 0, overflowed = 0;
   double nElec = 0, nPhot = 0;
   for (size_t ci = 0; ci < nchunks; ++ci) {
     const unsigned long long* cc = hc.data() + ci * kCtrPerChunk;
-    for (int k = 0; k < kStripes; ++k) lost += cc[kGen * kStripes + k] + cc[kCntStride + kGen * kStripes + k];
-    lost += cc[2 * kCntStride + 2 * (kGen + 1)];
+    for (int k = 0; k < kStripes; ++k) leftover += cc[kGen * kStripes + k] + cc[kCntStride + kGen * kStripes + k];
+    overflowed += cc[2 * kCntStride + 2 * (kGen + 1)];
     for (int g = 0; g < kGen; ++g)
       for (int k = 0; k < kStripes; ++k) {
         nElec += double(cc[g * kStripes + k]);
@@ -343,7 +343,8 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
     CK(cudaMemcpy(outs[j].d_dose, dose + off[j], outs[j].tallySize * sizeof(double), cudaMemcpyDeviceToDevice));
     CK(cudaMemcpy(outs[j].d_dose2, dose2 + off[j], outs[j].tallySize * sizeof(double), cudaMemcpyDeviceToDevice));
   }
-  // the step counter of the electron phase is accumulated on job 0
+  lost = leftover + overflowed;
+  // losses of the queues are reported on job 0
   if (njobs > 0) outs[0].cnt.lost += lost;
   for (int j = 0; j < njobs; ++j) {
     double e = 0.0;
@@ -357,7 +358,10 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
       outs[j].maxIz = mz;
     }
   }
-  if (lost > 0) return Fail(DPMX_ERR_OVERFLOW, "particle queue overflow or generation limit reached");
+  if (lost > 0)
+    return Fail(DPMX_ERR_OVERFLOW, std::to_string(overflowed) + " secondaries dropped on full queues, " +
+                                       std::to_string(leftover) + " particles left after " + std::to_string(kGen) +
+                                       " generations");
   return DPMX_OK;
 }
 

@@ -149,7 +149,10 @@ __device__ __forceinline__ void LoadParticle(const Queue& q, unsigned long long 
 __device__ __forceinline__ bool Append(const Queue& q, unsigned long long* count, unsigned long long* overflow,
                                        const PState& p) {
   cg::coalesced_group g = cg::coalesced_threads();
-  const int stripe = int((blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) & (kStripes - 1));
+  // blocks and warps spread over all stripes (7 is coprime with kStripes, so
+  // the first warp of consecutive blocks, which does most block-stage appends,
+  // still cycles through every stripe)
+  const int stripe = int((blockIdx.x * 7u + (threadIdx.x >> 5)) & (kStripes - 1));
   unsigned long long base = 0;
   if (g.thread_rank() == 0) base = atomicAdd(count + stripe, (unsigned long long)g.size());
   base = g.shfl(base, 0);
