@@ -37,7 +37,7 @@ struct Cfg {
   int blocksPerSM = 3;
   long long chunk = 1 << 20;
   int aggregate = 0;
-  int eblock = 0;          // electron phase: 0 lane-refill kernel, 1 block-batched kernel
+  int eblock = 1;          // electron phase: 0 lane-refill kernel, 1 block-batched kernel
 };
 
 struct DevBuf {       // owned device allocations of one run
