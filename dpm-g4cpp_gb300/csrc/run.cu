@@ -507,7 +507,7 @@ Cfg DefaultCfg(const dpmx_run_options* o, long long totalHist) {
 }
 
 // times a few launch shapes on a sample of the jobs and returns the fastest
-int Autotune(const dpmx_tables* t, const dpmx_job* jobs, int njobs, const Cfg& base, cudaStream_t st, Cfg* best) {
+int Autotune(const dpmx_tables* t, const dpmx_job* jobs, int njobs, const Cfg base, cudaStream_t st, Cfg* best) {
   long long total = 0;
   for (int j = 0; j < njobs; ++j) total += jobs[j].histories;
   const long long sample = std::min<long long>(total, 1 << 18);

@@ -855,21 +855,30 @@ struct SlotArrays {     // shared-memory state of the resident electrons
   uint32_t hist[kSlots], slot[kSlots], ulo[kSlots], uhi[kSlots], ctr[kSlots], pst[kSlots];
   double acc[kSlots];
 };
+// Every slot sits in exactly one of six lists, by what it does next: MSC
+// hinge, MSC step end, brem, Moller, plain sub-step, idle. The lists share
+// three arrays (one kind filled from the front, one from the back) and are
+// double-buffered: an iteration reads one buffer and fills the other. Their
+// counts rotate over three sets, so that the set an iteration reads, the set
+// it fills and the set it clears for the next iteration are never the same
+// and one barrier per iteration suffices.
+enum : int { kLHinge, kLMscEnd, kLBrem, kLMoller, kLStep, kLIdle, kLExhausted, kLCounts = 8 };
 struct SlotLists {
-  uint16_t active[kSlots], idle[kSlots], hinge[kSlots], mscEnd[kSlots], brem[kSlots], moller[kSlots];
-  int nActive, nIdle, nHinge, nMscEnd, nBrem, nMoller, nFill, exhausted;
-  unsigned long long fillBase;
+  uint16_t ev[2][kSlots];    // hinge from the front, MSC step end from the back
+  uint16_t ia[2][kSlots];    // brem from the front, Moller from the back
+  uint16_t run[2][kSlots];   // plain sub-step from the front, idle from the back
+  int cnt[3][kLCounts];
 };
 
 __host__ __device__ constexpr size_t BlockPhaseStaticBytes() { return sizeof(SlotArrays) + sizeof(SlotLists); }
 
-// warp-aggregated push of v onto a shared list
-__device__ __forceinline__ void Push(uint16_t* list, int* n, int v) {
+// warp-aggregated push of v onto a shared list, from its front or its back
+__device__ __forceinline__ void Push(uint16_t* list, int* n, int v, bool back) {
   cg::coalesced_group g = cg::coalesced_threads();
   int base = 0;
   if (g.thread_rank() == 0) base = atomicAdd(n, int(g.size()));
-  base = g.shfl(base, 0);
-  list[base + g.thread_rank()] = uint16_t(v);
+  const int pos = g.shfl(base, 0) + int(g.thread_rank());
+  list[back ? kSlots - 1 - pos : pos] = uint16_t(v);
 }
 
 __device__ __forceinline__ void LoadSlot(const SlotArrays& S, int k, PState& p, EState& s, uint32_t& fl) {
@@ -1080,8 +1089,9 @@ __device__ __forceinline__ void EventMscEnd(const PhaseArgs& a, const ETables& e
   S.ctr[k] = rng.ctr;
 }
 
-// bremsstrahlung (SimDPMLike.cc:172-194, :661-695)
-__device__ __forceinline__ void EventBrem(const PhaseArgs& a, const JobF* jobs, SlotArrays& S, SlotLists& L, int k) {
+// bremsstrahlung (SimDPMLike.cc:172-194, :661-695); false when the electron
+// fell below the tracking cut and finished
+__device__ __forceinline__ bool EventBrem(const PhaseArgs& a, const JobF* jobs, SlotArrays& S, int k) {
   PState p;
   EState s;
   uint32_t fl;
@@ -1115,12 +1125,13 @@ __device__ __forceinline__ void EventBrem(const PhaseArgs& a, const JobF* jobs, 
     if ((fl & kFPositron) != 0) AnnihilateF(a, p, rng, acc);
     atomicAdd(a.histE + p.slot, acc);
     S.flags[k] = 0u;
-    return;
+    return false;
   }
   S.e[k] = p.e;
   S.nBrem[k] = -__logf(rng.U());
   S.acc[k] = acc;
   S.ctr[k] = rng.ctr;
+  return true;
 }
 
 // Moller delta electron (SimDPMLike.cc:204-214, :699-728)
@@ -1158,6 +1169,45 @@ __device__ __forceinline__ void EventMoller(const PhaseArgs& a, const ETables& e
   S.ctr[k] = rng.ctr;
 }
 
+// first sub-step state of a claimed work item (a primary or a queued
+// electron) in slot k; false when it starts outside the phantom
+__device__ __forceinline__ bool RefillSlot(const PhaseArgs& a, const ETables& et, const JobF* jobs,
+                                           const unsigned long long* spre, SlotArrays& S, int k,
+                                           unsigned long long item, EscTally& esc) {
+  PState p;
+  PRng rng;
+  if (item < (unsigned long long)a.nPrimaries) {
+    MakePrimary(a, a.segs, (long long)item, p, rng);
+  } else {
+    LoadParticle(a.in, StripedIndex(a.in, spre, item - a.nPrimaries), p);
+    const JobF& J = jobs[p.meta >> 2];
+    rng.Init(J.k0, J.k1, p.hist, p.ulo, p.uhi);
+  }
+  const int job = int(p.meta >> 2);
+  const JobF& J = jobs[job];
+  if (!InBox(J, p.ix, p.iy, p.iz) || MaterialAt(J, p.ix, p.iy, p.iz) < 0) {
+    const double out = p.e + ((p.meta & 3u) == 2u ? 2.0 * kEMC2f : 0.0);
+    esc.Add(jobs, job, out);
+    atomicAdd(a.histE + p.slot, out);
+    return false;
+  }
+  EState s;
+  InitElectron(et, p, rng, s);
+  s.sGeom = 0.f;
+  s.axis = 0;
+  StoreSlot(S, k, p, s, true);
+  // the particle's identity (history, energy-check slot, stream) is set once
+  // here; StoreSlot only writes the state that changes while stepping
+  S.hist[k] = p.hist;
+  S.slot[k] = p.slot;
+  S.ulo[k] = p.ulo;
+  S.uhi[k] = p.uhi;
+  S.acc[k] = 0.0;
+  S.ctr[k] = rng.ctr;
+  S.pst[k] = 0;
+  return true;
+}
+
 __global__ void __launch_bounds__(256, 2) ElectronPhaseB(PhaseArgs a) {
   extern __shared__ __align__(16) unsigned char dyn[];
   SlotArrays& S = *reinterpret_cast<SlotArrays*>(dyn);
@@ -1175,96 +1225,75 @@ __global__ void __launch_bounds__(256, 2) ElectronPhaseB(PhaseArgs a) {
   const unsigned long long total = (unsigned long long)a.nPrimaries + nQ;
   if (total == 0) return;
   const int tid = threadIdx.x, nthr = blockDim.x;
-  for (int k = tid; k < kSlots; k += nthr) S.flags[k] = 0u;
-  if (tid == 0) L.exhausted = 0;
+  // all slots start idle
+  for (int k = tid; k < kSlots; k += nthr) {
+    S.flags[k] = 0u;
+    L.run[0][kSlots - 1 - k] = uint16_t(k);
+  }
+  for (int c = tid; c < 3 * kLCounts; c += nthr) (&L.cnt[0][0])[c] = (c == kLIdle) ? kSlots : 0;
   __syncthreads();
   EscTally esc;
   unsigned long long nsteps = 0;
+  int cr = 0, lr = 0;   // count set and list buffer read by this iteration
   for (;;) {
-    // active / idle lists
-    if (tid == 0) { L.nActive = 0; L.nIdle = 0; }
-    __syncthreads();
-    for (int k = tid; k < kSlots; k += nthr) {
-      if (S.flags[k] & kFAlive) Push(L.active, &L.nActive, k);
-      else Push(L.idle, &L.nIdle, k);
-    }
-    __syncthreads();
-    // claim work for the idle slots (one atomic per block and iteration)
+    const int cw = cr == 2 ? 0 : cr + 1, cz = cw == 2 ? 0 : cw + 1, lw = lr ^ 1;
+    const int* nr = L.cnt[cr];
+    int* nw = L.cnt[cw];
+    const int e0 = nr[kLHinge], e1 = e0 + nr[kLMscEnd], e2 = e1 + nr[kLBrem], e3 = e2 + nr[kLMoller],
+              e4 = e3 + nr[kLStep];
+    const bool exhausted = nr[kLExhausted] != 0;
+    if (e4 == 0 && exhausted) break;
     if (tid == 0) {
-      L.nHinge = L.nMscEnd = L.nBrem = L.nMoller = 0;
-      L.nFill = 0;
-      const int want = L.nIdle < 128 ? L.nIdle : 128;
-      if (!L.exhausted && want > 0) {
-        const unsigned long long base = atomicAdd(a.head, (unsigned long long)want);
-        if (base >= total) {
-          L.exhausted = 1;
+      for (int c = 0; c < kLCounts; ++c) L.cnt[cz][c] = 0;
+      if (exhausted) nw[kLExhausted] = 1;
+    }
+    // each slot once: its pending interaction or its refill, then one sub-step
+    for (int i = tid; i < kSlots; i += nthr) {
+      int k;
+      bool live = true;
+      if (i < e4) {
+        if (i < e0) {
+          k = L.ev[lr][i];
+          EventHinge(a, jobs, S, k);
+        } else if (i < e1) {
+          k = L.ev[lr][kSlots - 1 - (i - e0)];
+          EventMscEnd(a, et, jobs, S, k);
+        } else if (i < e2) {
+          k = L.ia[lr][i - e1];
+          live = EventBrem(a, jobs, S, k);
+        } else if (i < e3) {
+          k = L.ia[lr][kSlots - 1 - (i - e2)];
+          EventMoller(a, et, jobs, S, k);
         } else {
-          L.fillBase = base;
-          L.nFill = int(total - base < (unsigned long long)want ? total - base : (unsigned long long)want);
-          if (base + want >= total) L.exhausted = 1;
+          k = L.run[lr][i - e3];
+        }
+      } else {
+        k = L.run[lr][kSlots - 1 - (i - e4)];
+        live = false;
+        if (!exhausted) {
+          // one claim on the work counter per warp
+          cg::coalesced_group g = cg::coalesced_threads();
+          unsigned long long base = 0;
+          if (g.thread_rank() == 0) base = atomicAdd(a.head, (unsigned long long)g.size());
+          base = g.shfl(base, 0);
+          const unsigned long long item = base + g.thread_rank();
+          if (base + g.size() >= total) nw[kLExhausted] = 1;
+          if (item < total) live = RefillSlot(a, et, jobs, spre, S, k, item, esc);
         }
       }
-    }
-    __syncthreads();
-    for (int i = tid; i < L.nFill; i += nthr) {
-      const int k = L.idle[i];
-      const unsigned long long item = L.fillBase + i;
-      PState p;
-      PRng rng;
-      if (item < (unsigned long long)a.nPrimaries) {
-        MakePrimary(a, a.segs, (long long)item, p, rng);
-      } else {
-        LoadParticle(a.in, StripedIndex(a.in, spre, item - a.nPrimaries), p);
-        const JobF& J = jobs[p.meta >> 2];
-        rng.Init(J.k0, J.k1, p.hist, p.ulo, p.uhi);
+      const int code = live ? StepSlot(a, et, jobs, S, k, esc, nsteps) : 5;
+      switch (code) {
+        case 0: Push(L.run[lw], &nw[kLStep], k, false); break;
+        case 1: Push(L.ia[lw], &nw[kLBrem], k, false); break;
+        case 2: Push(L.ia[lw], &nw[kLMoller], k, true); break;
+        case 3: Push(L.ev[lw], &nw[kLHinge], k, false); break;
+        case 4: Push(L.ev[lw], &nw[kLMscEnd], k, true); break;
+        default: Push(L.run[lw], &nw[kLIdle], k, true); break;
       }
-      const int job = int(p.meta >> 2);
-      const JobF& J = jobs[job];
-      if (!InBox(J, p.ix, p.iy, p.iz) || MaterialAt(J, p.ix, p.iy, p.iz) < 0) {
-        const double out = p.e + ((p.meta & 3u) == 2u ? 2.0 * kEMC2f : 0.0);
-        esc.Add(jobs, job, out);
-        atomicAdd(a.histE + p.slot, out);
-        continue;
-      }
-      EState s;
-      InitElectron(et, p, rng, s);
-      s.sGeom = 0.f;
-      s.axis = 0;
-      StoreSlot(S, k, p, s, true);
-      // the particle's identity (history, energy-check slot, stream) is set
-      // once here; StoreSlot only writes the state that changes while stepping
-      S.hist[k] = p.hist;
-      S.slot[k] = p.slot;
-      S.ulo[k] = p.ulo;
-      S.uhi[k] = p.uhi;
-      S.acc[k] = 0.0;
-      S.ctr[k] = rng.ctr;
-      S.pst[k] = 0;
-      Push(L.active, &L.nActive, k);
     }
     __syncthreads();
-    const int nAct = L.nActive, ex = L.exhausted;
-    __syncthreads();
-    if (nAct == 0) {
-      if (ex) break;
-      continue;
-    }
-    // one sub-step for every active electron
-    for (int i = tid; i < nAct; i += nthr) {
-      const int k = L.active[i];
-      const int code = StepSlot(a, et, jobs, S, k, esc, nsteps);
-      if (code == 1) Push(L.brem, &L.nBrem, k);
-      else if (code == 2) Push(L.moller, &L.nMoller, k);
-      else if (code == 3) Push(L.hinge, &L.nHinge, k);
-      else if (code == 4) Push(L.mscEnd, &L.nMscEnd, k);
-    }
-    __syncthreads();
-    // interactions, one kind at a time over compacted lists
-    for (int i = tid; i < L.nHinge; i += nthr) EventHinge(a, jobs, S, L.hinge[i]);
-    for (int i = tid; i < L.nMscEnd; i += nthr) EventMscEnd(a, et, jobs, S, L.mscEnd[i]);
-    for (int i = tid; i < L.nBrem; i += nthr) EventBrem(a, jobs, S, L, L.brem[i]);
-    for (int i = tid; i < L.nMoller; i += nthr) EventMoller(a, et, jobs, S, L.moller[i]);
-    __syncthreads();
+    cr = cw;
+    lr = lw;
   }
   esc.Flush(jobs);
   for (int o = 16; o > 0; o >>= 1) nsteps += __shfl_down_sync(kFull, nsteps, o);
@@ -1284,6 +1313,22 @@ __global__ void FoldKernel(double* t, double* dose, double* dose2, long long n) 
 
 __global__ void EnergyCheckKernel(const double* histE, const double* histE0, long long nslots, const Segment* segs,
                                   int nsegs, const JobF* jobs) {
+  // per-thread sums for the current job, flushed when the job changes; the
+  // final flush is reduced over the lanes of a warp that share a job
+  int cur = -1;
+  double se0 = 0.0, mres = 0.0;
+  unsigned long long nh = 0, nv = 0;
+  auto flush = [&](int job) {
+    RunCounters* c = jobs[job].cnt;
+    if (nh) {
+      atomicAdd(&c->primaryEnergy, se0);
+      atomicAdd(&c->histories, nh);
+      atomicMax(&c->maxResidualBits, (unsigned long long)__double_as_longlong(mres));
+      if (nv) atomicAdd(&c->violations, nv);
+    }
+    se0 = mres = 0.0;
+    nh = nv = 0;
+  };
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nslots;
        i += (long long)gridDim.x * blockDim.x) {
     // slots are laid out segment after segment
@@ -1292,14 +1337,25 @@ __global__ void EnergyCheckKernel(const double* histE, const double* histE0, lon
       const int mid = (lo + hi + 1) >> 1;
       if (segs[mid].slotBase <= i) lo = mid; else hi = mid - 1;
     }
-    const JobF& J = jobs[segs[lo].job];
+    const int job = segs[lo].job;
+    if (job != cur) {
+      if (cur >= 0) flush(cur);
+      cur = job;
+    }
     const double e0 = histE0[i];
     const double res = fabs(e0 - histE[i]);
-    atomicAdd(&J.cnt->primaryEnergy, e0);
-    atomicAdd(&J.cnt->histories, 1ull);
-    atomicMax(&J.cnt->maxResidualBits, (unsigned long long)__double_as_longlong(res));
-    if (res > 1.0e-3 * e0) atomicAdd(&J.cnt->violations, 1ull);
+    se0 += e0;
+    ++nh;
+    mres = fmax(mres, res);
+    if (res > 1.0e-3 * e0) ++nv;
   }
+  cg::coalesced_group g = cg::coalesced_threads();
+  cg::coalesced_group peers = cg::labeled_partition(g, cur);
+  se0 = cg::reduce(peers, se0, cg::plus<double>());
+  nh = cg::reduce(peers, nh, cg::plus<unsigned long long>());
+  nv = cg::reduce(peers, nv, cg::plus<unsigned long long>());
+  mres = cg::reduce(peers, mres, cg::greater<double>());
+  if (peers.thread_rank() == 0 && cur >= 0) flush(cur);
 }
 
 __global__ void SamplerKernel32(DevTables<float> T, int s, int imat, const double* e, const double* r, double* out,
