@@ -34,6 +34,12 @@ WORKLOAD = "precision form: 128x128x256 x 2 mm water/lung-slab/bone-cylinder pha
 BYTES_E_STEP = 80 + 1 + 16
 BYTES_P_STEP = 24 + 1
 BYTES_PARTICLE = 2 * 52
+# FP32 work per unit: an electron sub-step is ~100 flops, a Woodcock photon
+# step ~35 (the transport is bounded by FP32/SFU issue and latency, not HBM)
+FLOPS_E_STEP = 100
+FLOPS_P_STEP = 35
+# nominal FP32 rate: 152 SMs x 128 lanes x 2 (FMA) x 2.07 GHz
+FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 
 
 def parse():
@@ -43,7 +49,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--hist", type=float, default=1e7, help="histories per step and GPU")
-    ap.add_argument("--cpu-hist", type=int, default=4000, help="oracle histories per CPU worker and step")
+    ap.add_argument("--cpu-hist", type=int, default=200000, help="oracle histories per CPU worker and step")
     ap.add_argument("--batches", type=int, default=10, help="statistical batches per step")
     return ap.parse_args()
 
@@ -253,22 +259,35 @@ def main():
     # live roofline of the dominant kernel from a profiled run (every phase launch timed)
     r = one(10**6, profile=True)
     pr = r.profile
+    eblock = r.config["electron_kernel"] == 1
     r.close()
     peak, peak_kind = measured_peaks()
     e_bytes = pr["electron_steps"] * BYTES_E_STEP + pr["electrons"] * BYTES_PARTICLE
     p_bytes = pr["photon_steps"] * BYTES_P_STEP + pr["photons"] * BYTES_PARTICLE
     if pr["electron_ms"] >= pr["photon_ms"]:
-        kname, kms, kbytes, nl = "ElectronPhase", pr["electron_ms"], e_bytes, pr["electron_launches"]
+        kname = "ElectronPhaseB" if eblock else "ElectronPhase"
+        kms, kbytes, nl = pr["electron_ms"], e_bytes, pr["electron_launches"]
+        kflops = pr["electron_steps"] * FLOPS_E_STEP
+        kunits = pr["electron_steps"]
     else:
         kname, kms, kbytes, nl = "PhotonPhase", pr["photon_ms"], p_bytes, pr["photon_launches"]
+        kflops = pr["photon_steps"] * FLOPS_P_STEP
+        kunits = pr["photon_steps"]
     achieved = kbytes / (kms * 1e-3) / 1e9
+    # DRAM bytes per launch from an ncu capture, given per unit (sub-step) so
+    # that it scales to this launch size
     traffic = None
     tf = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tf):
         with open(tf) as f:
-            traffic = json.load(f).get(kname)
+            per_unit = json.load(f).get(kname, {}).get("dram_bytes_per_unit")
+        if per_unit:
+            traffic = per_unit * kunits / max(1.0, nl)
+    fp32 = kflops / (kms * 1e-3) / 1e12
     roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+                "fp32_issue": {"achieved": fp32, "peak": FP32_NOMINAL_TFLOPS, "unit": "TFLOP/s",
+                               "frac": fp32 / FP32_NOMINAL_TFLOPS, "peak_source": "nominal"},
                 "algorithmic_bytes_per_launch": kbytes / max(1.0, nl), "avg_launch_ms": kms / max(1.0, nl),
                 "electron_phase_share": pr["electron_ms"] / max(1e-9, pr["total_ms"]),
                 "photon_phase_share": pr["photon_ms"] / max(1e-9, pr["total_ms"]),

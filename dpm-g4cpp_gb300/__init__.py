@@ -98,6 +98,7 @@ def library():
         "dpmx_result_config": (C.c_int, [P, C.POINTER(C.c_longlong)]),
         "dpmx_result_profile": (C.c_int, [P, C.POINTER(C.c_double)]),
         "dpmx_result_free": (None, [P]),
+        "dpmx_scratch_release": (None, []),
         "dpmx_simulate": (C.c_int, [P, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int, C.c_uint64, C.c_int,
                                     _dp, _dp, C.c_int, C.POINTER(C.c_int)]),
         "dpmx_write_hist": (C.c_int, [P, C.c_char_p, C.c_int, C.c_double, C.c_int, _dp, _dp, C.c_int]),
@@ -136,7 +137,7 @@ def exported_symbols():
             "dpmx_phantom_voxels", "dpmx_phantom_free", "dpmx_phantom_tally_size", "dpmx_run_options_default",
             "dpmx_run", "dpmx_result_tally", "dpmx_result_tally_device", "dpmx_result_stats",
             "dpmx_result_elapsed_ms", "dpmx_result_launches", "dpmx_result_config", "dpmx_result_profile",
-            "dpmx_result_free",
+            "dpmx_result_free", "dpmx_scratch_release",
             "dpmx_simulate", "dpmx_simulate_noalloc", "dpmx_write_hist", "dpmx_sampler_eval", "dpmx_table_eval", "dpmx_simulate_histories",
             "dpmx_influence_build", "dpmx_csr_shape", "dpmx_csr_device", "dpmx_csr_spmv", "dpmx_csr_spmv_t",
             "dpmx_csr_download", "dpmx_csr_free"]
@@ -352,6 +353,11 @@ class Result:
             self.close()
         except Exception:
             pass
+
+
+def scratch_release():
+    """Frees the device scratch that finished runs keep for later runs."""
+    library().dpmx_scratch_release()
 
 
 def run(tables, jobs, precision=FP32_EVENT, batches=10, block_size=0, blocks_per_sm=0, chunk_histories=0,

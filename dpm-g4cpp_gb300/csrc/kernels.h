@@ -68,7 +68,8 @@ struct JobF {                  // per-job geometry, source and tally (device vie
   float vx, vy, vz, ivx, ivy, ivz;
   double x0, y0, z0;           // lower corner of voxel (0,0,0) [mm]
   const uint8_t* mat;
-  double* tally;               // batch tally of this job
+  double* tally;               // batch tally of this job: bin i at tally[i * tstride]
+  long long tstride;           // batch slices interleaved per bin
   double* steps;               // scoring-step counts (depth tally only) or null
   double* btally;              // beamlet-tagged tally [beamlet][nvox] or null
   int nbeamlets;
@@ -123,6 +124,13 @@ cudaError_t LaunchPhotonPhase(const PhaseArgs& a, int blocks, int threads, cudaS
 cudaError_t LaunchElectronPhase(const PhaseArgs& a, int blocks, int threads, cudaStream_t st);
 // dose += t, dose2 += t^2, t = 0 over n bins
 cudaError_t LaunchFold(double* t, double* dose, double* dose2, long long n, cudaStream_t st);
+// the same over m batch slices, bin i of slice b at t[i * binStride + b * sliceStride]:
+// dose[i] += sum_b t, dose2[i] += sum_b t^2
+cudaError_t LaunchFoldSlices(double* t, double* dose, double* dose2, long long n, long long binStride,
+                             long long sliceStride, int m, cudaStream_t st);
+// *sum += sum of d[0..n), *lastNz = max(*lastNz, 1 + index of the last non-zero bin)
+cudaError_t LaunchTallySummary(const double* d, long long n, double* sum, unsigned long long* lastNz,
+                               cudaStream_t st);
 // per-slot energy check against the primary energy, per-job counters
 cudaError_t LaunchEnergyCheck(const double* histE, const double* histE0, long long nslots, const Segment* segs,
                               int nsegs, const JobF* jobs, cudaStream_t st);

@@ -3,12 +3,15 @@
 //  * FP64 plain form: per job and statistical batch, one launch of the
 //    one-thread-per-history kernel into a batch tally, then a fold
 //    (dose += t, dose2 += t^2).
-//  * FP32 event form: every batch of every job is cut into chunks of at most
-//    `chunk` histories; a chunk runs kGen generations of (photon phase,
-//    electron phase) over double-buffered queues, then the per-history energy
-//    check. The launches of the whole run (all batches, chunks, generations,
-//    folds) are captured into one CUDA graph and launched once. Empty phases
-//    return at once (their input count is read on the device).
+//  * FP32 event form: the statistical batches of every job score into
+//    separate tally slices (as many as fit a memory budget; more batches run
+//    group after group), so the histories of a group are cut into chunks of
+//    at most `chunk` histories regardless of batch boundaries; a chunk runs
+//    kGen generations of (photon phase, electron phase) over double-buffered
+//    queues, then the per-history energy check. After a group every slice is
+//    folded (dose += t, dose2 += t^2). The launches of the whole run are
+//    captured into one CUDA graph and launched once. Empty phases return at
+//    once (their input count is read on the device).
 //  * Tuning: a short sample of the jobs is timed for a few launch shapes
 //    (threads per block, blocks per SM, warp-aggregated tally) and chunk
 //    sizes, and the fastest is used for the run.
@@ -17,6 +20,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -31,6 +35,9 @@ constexpr int kGen = 32;                              // generations per chunk
 // generation, the two work counters of every generation, and the overflow count
 constexpr int kCntStride = (kGen + 1) * kStripes;
 constexpr int kCtrPerChunk = 2 * kCntStride + 2 * (kGen + 1) + 1;
+constexpr long long kMaxChunk = 1LL << 24;            // default upper bound of histories per chunk
+constexpr int kQueuePerPrimary = 6;                   // queue entries per primary of a chunk and generation
+constexpr bool kInterleaveSlices = false;             // batch slices: per bin (true) or one after another
 
 struct Cfg {
   int threads = 256;
@@ -40,12 +47,89 @@ struct Cfg {
   int eblock = 1;          // electron phase: 0 lane-refill kernel, 1 block-batched kernel
 };
 
-struct DevBuf {       // owned device allocations of one run
+// Device scratch kept across runs. A run of the FP32 form needs GBs of queues,
+// energy-check slots and batch tallies; cudaMalloc / cudaFree of them on every
+// run would cost milliseconds and synchronise the device. A block is lent to
+// one run at a time and returns to the pool when the run ends; idle blocks are
+// released when an allocation fails, or by dpmx_scratch_release.
+class ScratchPool {
+ public:
+  static ScratchPool& Instance() {
+    static ScratchPool* p = new ScratchPool;   // never destroyed: no CUDA calls at process exit
+    return *p;
+  }
+  cudaError_t Get(size_t bytes, void** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    bytes = (std::max<size_t>(bytes, 1) + kGrain - 1) / kGrain * kGrain;
+    {
+      std::lock_guard<std::mutex> g(m_);
+      Block* best = nullptr;
+      for (auto& b : blocks_)
+        if (!b.busy && b.dev == dev && b.bytes >= bytes && b.bytes <= 2 * bytes && (!best || b.bytes < best->bytes))
+          best = &b;
+      if (best) {
+        best->busy = true;
+        *out = best->p;
+        return cudaSuccess;
+      }
+    }
+    void* p = nullptr;
+    e = cudaMalloc(&p, bytes);
+    if (e == cudaErrorMemoryAllocation) {
+      cudaGetLastError();
+      Release(dev);
+      e = cudaMalloc(&p, bytes);
+    }
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> g(m_);
+    blocks_.push_back({dev, p, bytes, true});
+    *out = p;
+    return cudaSuccess;
+  }
+  void Put(void* p) {
+    std::lock_guard<std::mutex> g(m_);
+    for (auto& b : blocks_)
+      if (b.p == p) b.busy = false;
+  }
+  // frees the idle blocks of device dev (all devices when dev < 0)
+  void Release(int dev) {
+    std::vector<Block> f;
+    {
+      std::lock_guard<std::mutex> g(m_);
+      std::vector<Block> keep;
+      for (auto& b : blocks_) ((!b.busy && (dev < 0 || b.dev == dev)) ? f : keep).push_back(b);
+      blocks_.swap(keep);
+    }
+    int cur = 0;
+    cudaGetDevice(&cur);
+    for (auto& b : f) {
+      cudaSetDevice(b.dev);
+      cudaFree(b.p);
+    }
+    cudaSetDevice(cur);
+  }
+
+ private:
+  static constexpr size_t kGrain = size_t(1) << 18;
+  struct Block { int dev; void* p; size_t bytes; bool busy; };
+  std::mutex m_;
+  std::vector<Block> blocks_;
+};
+
+struct DevBuf {       // scratch of one run, lent by the pool
+  cudaStream_t st = nullptr;
   std::vector<void*> v;
-  ~DevBuf() { for (void* p : v) cudaFree(p); }
+  explicit DevBuf(cudaStream_t s) : st(s) {}
+  ~DevBuf() {
+    // nothing of this run may still use a block when it goes back
+    cudaStreamSynchronize(st);
+    for (void* p : v) ScratchPool::Instance().Put(p);
+  }
   template <class T> int Get(T** p, size_t n) {
     void* q = nullptr;
-    CK(cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T)));
+    CK(ScratchPool::Instance().Get(std::max<size_t>(n, 1) * sizeof(T), &q));
     v.push_back(q);
     *p = static_cast<T*>(q);
     return DPMX_OK;
@@ -68,35 +152,37 @@ struct Chunk {
   long long nP = 0, nE = 0, nslots = 0;
 };
 
-// splits batch b (of B) of every job into chunks of at most `chunk` histories
-std::vector<Chunk> PlanBatch(const dpmx_job* jobs, int njobs, int b, int B, long long chunk) {
+// Cuts batches [b0, b1) (of B) of every job into chunks of at most `chunk`
+// histories. Batch b of job j runs as sub-job (b - b0) * njobs + j, which
+// scores into its own tally slice; a chunk may span several batches.
+std::vector<Chunk> PlanGroup(const dpmx_job* jobs, int njobs, int b0, int b1, int B, long long chunk) {
   std::vector<Chunk> out;
   Chunk cur;
-  for (int j = 0; j < njobs; ++j) {
-    const long long N = jobs[j].histories;
-    long long first = N * b / B;
-    long long left = N * (b + 1) / B - first;
-    while (left > 0) {
-      const long long take = std::min(left, chunk - cur.nslots);
-      Segment s{};
-      s.job = j;
-      s.firstHist = jobs[j].first_history + first;
-      s.count = take;
-      s.slotBase = cur.nslots;
-      if (jobs[j].source.particle == 0) { s.prefix = cur.nP; cur.nP += take; cur.segP.push_back(s); }
-      else { s.prefix = cur.nE; cur.nE += take; cur.segE.push_back(s); }
-      cur.segAll.push_back(s);
-      cur.nslots += take;
-      first += take;
-      left -= take;
-      if (cur.nslots == chunk) { out.push_back(cur); cur = Chunk(); }
+  for (int b = b0; b < b1; ++b) {
+    for (int j = 0; j < njobs; ++j) {
+      const long long N = jobs[j].histories;
+      long long first = N * b / B;
+      long long left = N * (b + 1) / B - first;
+      while (left > 0) {
+        const long long take = std::min(left, chunk - cur.nslots);
+        Segment s{};
+        s.job = (b - b0) * njobs + j;
+        s.firstHist = jobs[j].first_history + first;
+        s.count = take;
+        s.slotBase = cur.nslots;
+        if (jobs[j].source.particle == 0) { s.prefix = cur.nP; cur.nP += take; cur.segP.push_back(s); }
+        else { s.prefix = cur.nE; cur.nE += take; cur.segE.push_back(s); }
+        cur.segAll.push_back(s);
+        cur.nslots += take;
+        first += take;
+        left -= take;
+        if (cur.nslots == chunk) { out.push_back(cur); cur = Chunk(); }
+      }
     }
   }
   if (cur.nslots > 0) out.push_back(cur);
   return out;
 }
-
-bool IsPow2Aligned(long long) { return true; }
 
 // ---------------------------------------------------------------------------
 // FP32 event form
@@ -108,23 +194,39 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
   // give the electron / photon phase times; see dpmx_result_profile
   const bool profile = prof != nullptr && !useGraph;
   std::vector<cudaEvent_t> evE, evP;
-  DevBuf buf;
+  DevBuf buf(st);
   const int nsm = NumSMs();
-  // concatenated tallies of all jobs: batch tally, dose, dose2
+  // concatenated tallies of all jobs: batch tally slices (interleaved per
+  // bin, so that the batches of one bin share cache lines), dose, dose2
   std::vector<long long> off(njobs);
   long long total = 0;
   for (int j = 0; j < njobs; ++j) { off[j] = total; total += outs[j].tallySize; }
+  // tally slices: all batches at once when they fit an eighth of the free
+  // memory (at most 16 GB), else groups of as many as fit
+  size_t freeB = 0, totB = 0;
+  CK(cudaMemGetInfo(&freeB, &totB));
+  const double budget = std::min(16.0e9, double(freeB) / 8.0);
+  const int R = int(std::max(1.0, std::min(double(batches), budget / (8.0 * double(std::max(1LL, total))))));
+  const int ngroups = (batches + R - 1) / R;
+  const long long binStride = kInterleaveSlices ? R : 1, sliceStride = kInterleaveSlices ? 1 : total;
   double *tB, *dose, *dose2;
-  if (int rc = buf.Get(&tB, total)) return rc;
+  if (int rc = buf.Get(&tB, size_t(R) * total)) return rc;
   if (int rc = buf.Get(&dose, total)) return rc;
   if (int rc = buf.Get(&dose2, total)) return rc;
-  CK(cudaMemsetAsync(tB, 0, total * sizeof(double), st));
+  CK(cudaMemsetAsync(tB, 0, size_t(R) * total * sizeof(double), st));
   CK(cudaMemsetAsync(dose, 0, total * sizeof(double), st));
   CK(cudaMemsetAsync(dose2, 0, total * sizeof(double), st));
   RunCounters* cnt;
   if (int rc = buf.Get(&cnt, njobs)) return rc;
   CK(cudaMemsetAsync(cnt, 0, njobs * sizeof(RunCounters), st));
-  std::vector<JobF> hj(njobs);
+  // per job: deposited energy and 1 + the last non-zero tally bin
+  double* dsum;
+  unsigned long long* dlast;
+  if (int rc = buf.Get(&dsum, njobs)) return rc;
+  if (int rc = buf.Get(&dlast, njobs)) return rc;
+  // sub-job r * njobs + j: job j scoring into tally slice r
+  const int nsub = R * njobs;
+  std::vector<JobF> hj(nsub);
   for (int j = 0; j < njobs; ++j) {
     const dpmx_phantom* ph = jobs[j].phantom;
     const GridGeom& g = ph->grid;
@@ -137,7 +239,8 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
     J.ivx = float(1.0 / g.vx); J.ivy = float(1.0 / g.vy); J.ivz = float(1.0 / g.vz);
     J.x0 = g.x0; J.y0 = g.y0; J.z0 = g.z0;
     J.mat = g.mat;
-    J.tally = tB + off[j];
+    J.tally = tB + off[j] * binStride;
+    J.tstride = binStride;
     J.steps = outs[j].d_steps;
     J.btally = tag ? outs[j].d_btally : nullptr;
     J.nbeamlets = std::max(1, outs[j].nbeamlets);
@@ -149,19 +252,23 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
     J.k0 = uint32_t(jobs[j].seed);
     J.k1 = uint32_t(jobs[j].seed >> 32) ^ 0x5bd1e995u;
     J.cnt = cnt + j;
+    for (int r = 1; r < R; ++r) {
+      hj[r * njobs + j] = J;
+      hj[r * njobs + j].tally = tB + off[j] * binStride + r * sliceStride;
+    }
   }
   JobF* dj;
-  if (int rc = buf.Get(&dj, njobs)) return rc;
-  CK(cudaMemcpyAsync(dj, hj.data(), njobs * sizeof(JobF), cudaMemcpyHostToDevice, st));
+  if (int rc = buf.Get(&dj, nsub)) return rc;
+  CK(cudaMemcpyAsync(dj, hj.data(), nsub * sizeof(JobF), cudaMemcpyHostToDevice, st));
 
   // plan and segment tables
-  std::vector<std::vector<Chunk>> plan(batches);
+  std::vector<std::vector<Chunk>> plan(ngroups);
   std::vector<Segment> segs;
   size_t nchunks = 0;
   long long maxSlots = 1;
-  for (int b = 0; b < batches; ++b) {
-    plan[b] = PlanBatch(jobs, njobs, b, batches, cfg.chunk);
-    for (auto& c : plan[b]) {
+  for (int gi = 0; gi < ngroups; ++gi) {
+    plan[gi] = PlanGroup(jobs, njobs, gi * R, std::min(batches, (gi + 1) * R), batches, cfg.chunk);
+    for (auto& c : plan[gi]) {
       segs.insert(segs.end(), c.segP.begin(), c.segP.end());
       segs.insert(segs.end(), c.segE.begin(), c.segE.end());
       segs.insert(segs.end(), c.segAll.begin(), c.segAll.end());
@@ -179,8 +286,8 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
   if (int rc = buf.Get(&ctr, nchunks * kCtrPerChunk)) return rc;
   CK(cudaMemsetAsync(ctr, 0, nchunks * kCtrPerChunk * sizeof(unsigned long long), st));
   // queues: double-buffered electrons and photons; a generation holds well
-  // under 8 secondaries of each kind per primary
-  const unsigned long long cap = (unsigned long long)std::max<long long>(maxSlots * 8, 1 << 18);
+  // under kQueuePerPrimary secondaries of each kind per primary
+  const unsigned long long cap = (unsigned long long)std::max<long long>(maxSlots * kQueuePerPrimary, 1 << 18);
   Queue qe[2], qp[2];
   for (int k = 0; k < 2; ++k) {
     if (int rc = AllocQueue(buf, qe[k], cap)) return rc;
@@ -192,8 +299,8 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
   long long nl = 0;
   auto enqueue = [&](cudaStream_t s) -> int {
     size_t segCur = 0, ci = 0;
-    for (int b = 0; b < batches; ++b) {
-      for (auto& c : plan[b]) {
+    for (int gi = 0; gi < ngroups; ++gi) {
+      for (auto& c : plan[gi]) {
         unsigned long long* cc = ctr + ci * kCtrPerChunk;
         unsigned long long* cntE = cc;                       // [gen][stripe]
         unsigned long long* cntP = cc + kCntStride;
@@ -209,7 +316,7 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
           std::memset(&a, 0, sizeof(a));
           a.T = T->t32;
           a.jobs = dj;
-          a.njobs = njobs;
+          a.njobs = nsub;
           a.histE = histE;
           a.histE0 = histE0;
           a.overflow = ovf;
@@ -251,7 +358,19 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
         segCur += c.segP.size() + c.segE.size() + c.segAll.size();
         ++ci;
       }
-      CK(LaunchFold(tB, dose, dose2, total, s));
+      const int nslice = std::min(batches, (gi + 1) * R) - gi * R;
+      if (R == 1) CK(LaunchFold(tB, dose, dose2, total, s));
+      else CK(LaunchFoldSlices(tB, dose, dose2, total, binStride, sliceStride, nslice, s));
+      ++nl;
+    }
+    // results into the per-job buffers, with their sums
+    CK(cudaMemsetAsync(dsum, 0, njobs * sizeof(double), s));
+    CK(cudaMemsetAsync(dlast, 0, njobs * sizeof(unsigned long long), s));
+    for (int j = 0; j < njobs; ++j) {
+      const size_t n = outs[j].tallySize * sizeof(double);
+      CK(cudaMemcpyAsync(outs[j].d_dose, dose + off[j], n, cudaMemcpyDeviceToDevice, s));
+      CK(cudaMemcpyAsync(outs[j].d_dose2, dose2 + off[j], n, cudaMemcpyDeviceToDevice, s));
+      CK(LaunchTallySummary(dose + off[j], outs[j].tallySize, dsum + j, dlast + j, s));
       ++nl;
     }
     return DPMX_OK;
@@ -337,27 +456,19 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
     prof[9] = fms;
   }
   std::vector<RunCounters> hcnt(njobs);
+  std::vector<double> hsum(njobs);
+  std::vector<unsigned long long> hlast(njobs);
   CK(cudaMemcpy(hcnt.data(), cnt, njobs * sizeof(RunCounters), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(hsum.data(), dsum, njobs * sizeof(double), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(hlast.data(), dlast, njobs * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
   for (int j = 0; j < njobs; ++j) {
     outs[j].cnt = hcnt[j];
-    CK(cudaMemcpy(outs[j].d_dose, dose + off[j], outs[j].tallySize * sizeof(double), cudaMemcpyDeviceToDevice));
-    CK(cudaMemcpy(outs[j].d_dose2, dose2 + off[j], outs[j].tallySize * sizeof(double), cudaMemcpyDeviceToDevice));
+    outs[j].cnt.deposited = hsum[j];
+    if (outs[j].slab) outs[j].maxIz = hlast[j] > 0 ? int(hlast[j] - 1) : 0;
   }
   lost = leftover + overflowed;
   // losses of the queues are reported on job 0
   if (njobs > 0) outs[0].cnt.lost += lost;
-  for (int j = 0; j < njobs; ++j) {
-    double e = 0.0;
-    std::vector<double> h(outs[j].tallySize);
-    CK(cudaMemcpy(h.data(), outs[j].d_dose, h.size() * sizeof(double), cudaMemcpyDeviceToHost));
-    for (double v : h) e += v;
-    outs[j].cnt.deposited = e;
-    if (outs[j].slab) {
-      int mz = 0;
-      for (size_t i = 0; i < h.size(); ++i) if (h[i] != 0.0) mz = int(i);
-      outs[j].maxIz = mz;
-    }
-  }
   if (lost > 0)
     return Fail(DPMX_ERR_OVERFLOW, std::to_string(overflowed) + " secondaries dropped on full queues, " +
                                        std::to_string(leftover) + " particles left after " + std::to_string(kGen) +
@@ -370,7 +481,7 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
 // ---------------------------------------------------------------------------
 int RunFp64(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, bool fixedSeedSlab, cudaStream_t st,
             std::vector<JobOut>& outs, double* ms, long long* launches, double* histEdep) {
-  DevBuf buf;
+  DevBuf buf(st);
   const int blocks = NumSMs() * 16;
   double* density;
   if (int rc = buf.Get(&density, kMaxMat)) return rc;
@@ -500,7 +611,12 @@ Cfg DefaultCfg(const dpmx_run_options* o, long long totalHist) {
   if (o && o->block_size > 0) c.threads = std::min(256, std::max(32, o->block_size / 32 * 32));
   if (o && o->blocks_per_sm > 0) c.blocksPerSM = o->blocks_per_sm;
   if (o && o->chunk_histories > 0) c.chunk = o->chunk_histories;
-  else c.chunk = std::max<long long>(1 << 14, std::min<long long>(1 << 21, totalHist));
+  else {
+    // as few chunks as the bound allows, of equal size
+    const long long n = std::max(1LL, totalHist);
+    const long long k = (n + kMaxChunk - 1) / kMaxChunk;
+    c.chunk = std::max<long long>(1 << 14, (n + k - 1) / k);
+  }
   if (o && o->tally_aggregate >= 0) c.aggregate = o->tally_aggregate;
   if (o && o->electron_kernel >= 0) c.eblock = o->electron_kernel;
   return c;
@@ -631,6 +747,8 @@ int dpmx_result_profile(const dpmx_result* r, double* out10) {
 
 void dpmx_result_free(dpmx_result* r) { delete r; }
 
+void dpmx_scratch_release(void) { ScratchPool::Instance().Release(-1); }
+
 int dpmx_simulate(const dpmx_tables* t, int nprimary, double eprimary, int iselectron, double lbox, int geom_index,
                   uint64_t seed, int precision, double* edep_hist, double* step_hist, int cap, int* hist_len) {
   if (!t || nprimary < 0 || !(lbox > 0.0)) return Fail(DPMX_ERR_ARG, "bad simulate arguments");
@@ -696,7 +814,7 @@ int dpmx_sampler_eval(const dpmx_tables* t, int precision, int sampler, int imat
   if (!t || !e || !r || !out || n < 0 || sampler < 0 || sampler > 3) return Fail(DPMX_ERR_ARG, "bad sampler arguments");
   if (imat < 0 || imat >= t->h.nmat) return Fail(DPMX_ERR_ARG, "bad material index");
   if (n == 0) return DPMX_OK;
-  DevBuf b;
+  DevBuf b(nullptr);
   double *de, *dr, *dout;
   if (int rc = b.Get(&de, n)) return rc;
   if (int rc = b.Get(&dr, 3 * size_t(n))) return rc;
@@ -713,7 +831,7 @@ int dpmx_table_eval(const dpmx_tables* t, int precision, int q, int imat, const 
   if (!t || !e || !out || n < 0 || q < 0 || q > 8) return Fail(DPMX_ERR_ARG, "bad table arguments");
   if (imat < 0 || imat >= t->h.nmat) return Fail(DPMX_ERR_ARG, "bad material index");
   if (n == 0) return DPMX_OK;
-  DevBuf b;
+  DevBuf b(nullptr);
   double *de, *dout;
   if (int rc = b.Get(&de, n)) return rc;
   if (int rc = b.Get(&dout, n)) return rc;

@@ -175,7 +175,7 @@ __device__ __forceinline__ bool Append(const Queue& q, unsigned long long* count
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void Score(const JobF& J, int ix, int iy, int iz, uint32_t hist, float e, int agg) {
   const long long idx = J.tallyDepth ? (long long)iz : ((long long)iz * J.ny + iy) * J.nx + ix;
-  double* ptr = J.tally + idx;
+  double* ptr = J.tally + idx * J.tstride;
   const double de = double(e);
   if (agg) {
     cg::coalesced_group g = cg::coalesced_threads();
@@ -343,19 +343,22 @@ struct WorkPool {
 };
 
 // escaped energy summed in the lane and flushed once per job change
+// (keyed by the job's counters: the statistical batches of one job share them,
+// so particles of different batches do not force a flush)
 struct EscTally {
   double e = 0.0;
-  int job = -1;
+  RunCounters* c = nullptr;
   __device__ __forceinline__ void Add(const JobF* jobs, int j, double x) {
-    if (j != job) {
-      if (job >= 0 && e != 0.0) atomicAdd(&jobs[job].cnt->escaped, e);
+    RunCounters* cj = jobs[j].cnt;
+    if (cj != c) {
+      if (c && e != 0.0) atomicAdd(&c->escaped, e);
       e = 0.0;
-      job = j;
+      c = cj;
     }
     e += x;
   }
-  __device__ __forceinline__ void Flush(const JobF* jobs) {
-    if (job >= 0 && e != 0.0) atomicAdd(&jobs[job].cnt->escaped, e);
+  __device__ __forceinline__ void Flush(const JobF*) {
+    if (c && e != 0.0) atomicAdd(&c->escaped, e);
     e = 0.0;
   }
 };
@@ -580,11 +583,11 @@ __global__ void __launch_bounds__(256) ElectronPhase(PhaseArgs a) {
   if (fewJobs)
     for (int j = threadIdx.x; j < a.njobs; j += blockDim.x) sjobs[j] = a.jobs[j];
   __shared__ unsigned long long spre[kStripes + 1];
-  StageElectronTables(a.T, sdata, &et);
   const unsigned long long nQ = StripePrefix(a.inCount, spre);
   const JobF* jobs = fewJobs ? sjobs : a.jobs;
   const unsigned long long total = (unsigned long long)a.nPrimaries + nQ;
-  if (total == 0) return;
+  if (total == 0) return;   // an empty generation skips the table staging
+  StageElectronTables(a.T, sdata, &et);
   const int lane = threadIdx.x & 31;
   const DevTables<float>& T = a.T;
   const float ecut = T.ecut, gcut = T.gcut;
@@ -1219,11 +1222,11 @@ __global__ void __launch_bounds__(256, 2) ElectronPhaseB(PhaseArgs a) {
   const bool fewJobs = a.njobs <= 16;
   if (fewJobs)
     for (int j = threadIdx.x; j < a.njobs; j += blockDim.x) sjobs[j] = a.jobs[j];
-  StageElectronTables(a.T, sdata, &et);
   const unsigned long long nQ = StripePrefix(a.inCount, spre);
   const JobF* jobs = fewJobs ? sjobs : a.jobs;
   const unsigned long long total = (unsigned long long)a.nPrimaries + nQ;
-  if (total == 0) return;
+  if (total == 0) return;   // an empty generation skips the table staging
+  StageElectronTables(a.T, sdata, &et);
   const int tid = threadIdx.x, nthr = blockDim.x;
   // all slots start idle
   for (int k = tid; k < kSlots; k += nthr) {
@@ -1311,15 +1314,60 @@ __global__ void FoldKernel(double* t, double* dose, double* dose2, long long n) 
   }
 }
 
+__global__ void FoldSlicesKernel(double* t, double* dose, double* dose2, long long n, long long binStride,
+                                 long long sliceStride, int m) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double* ti = t + i * binStride;
+    double s = 0.0, s2 = 0.0;
+    bool any = false;
+    for (int b = 0; b < m; ++b) {
+      const double v = ti[b * sliceStride];
+      if (v != 0.0) {
+        s += v;
+        s2 += v * v;
+        ti[b * sliceStride] = 0.0;
+        any = true;
+      }
+    }
+    if (any) {
+      dose[i] += s;
+      dose2[i] += s2;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) TallySummaryKernel(const double* d, long long n, double* sum,
+                                                          unsigned long long* lastNz) {
+  __shared__ double ws[8];
+  __shared__ unsigned long long wl[8];
+  double s = 0.0;
+  unsigned long long last = 0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double v = d[i];
+    s += v;
+    if (v != 0.0) last = (unsigned long long)i + 1;
+  }
+  cg::thread_block_tile<32> w = cg::tiled_partition<32>(cg::this_thread_block());
+  s = cg::reduce(w, s, cg::plus<double>());
+  last = cg::reduce(w, last, cg::greater<unsigned long long>());
+  if (w.thread_rank() == 0) { ws[threadIdx.x >> 5] = s; wl[threadIdx.x >> 5] = last; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 1; k < int(blockDim.x >> 5); ++k) { s += ws[k]; last = last > wl[k] ? last : wl[k]; }
+    atomicAdd(sum, s);
+    atomicMax(lastNz, last);
+  }
+}
+
 __global__ void EnergyCheckKernel(const double* histE, const double* histE0, long long nslots, const Segment* segs,
                                   int nsegs, const JobF* jobs) {
-  // per-thread sums for the current job, flushed when the job changes; the
-  // final flush is reduced over the lanes of a warp that share a job
-  int cur = -1;
+  // per-thread sums for the current job's counters (the batches of a job
+  // share them), flushed when they change; the final flush is reduced over
+  // the lanes of a warp that share the counters
+  RunCounters* cur = nullptr;
   double se0 = 0.0, mres = 0.0;
   unsigned long long nh = 0, nv = 0;
-  auto flush = [&](int job) {
-    RunCounters* c = jobs[job].cnt;
+  auto flush = [&](RunCounters* c) {
     if (nh) {
       atomicAdd(&c->primaryEnergy, se0);
       atomicAdd(&c->histories, nh);
@@ -1337,10 +1385,10 @@ __global__ void EnergyCheckKernel(const double* histE, const double* histE0, lon
       const int mid = (lo + hi + 1) >> 1;
       if (segs[mid].slotBase <= i) lo = mid; else hi = mid - 1;
     }
-    const int job = segs[lo].job;
-    if (job != cur) {
-      if (cur >= 0) flush(cur);
-      cur = job;
+    RunCounters* c = jobs[segs[lo].job].cnt;
+    if (c != cur) {
+      if (cur) flush(cur);
+      cur = c;
     }
     const double e0 = histE0[i];
     const double res = fabs(e0 - histE[i]);
@@ -1350,12 +1398,12 @@ __global__ void EnergyCheckKernel(const double* histE, const double* histE0, lon
     if (res > 1.0e-3 * e0) ++nv;
   }
   cg::coalesced_group g = cg::coalesced_threads();
-  cg::coalesced_group peers = cg::labeled_partition(g, cur);
+  cg::coalesced_group peers = cg::labeled_partition(g, (unsigned long long)cur);
   se0 = cg::reduce(peers, se0, cg::plus<double>());
   nh = cg::reduce(peers, nh, cg::plus<unsigned long long>());
   nv = cg::reduce(peers, nv, cg::plus<unsigned long long>());
   mres = cg::reduce(peers, mres, cg::greater<double>());
-  if (peers.thread_rank() == 0 && cur >= 0) flush(cur);
+  if (peers.thread_rank() == 0 && cur) flush(cur);
 }
 
 __global__ void SamplerKernel32(DevTables<float> T, int s, int imat, const double* e, const double* r, double* out,
@@ -1430,10 +1478,25 @@ cudaError_t LaunchFold(double* t, double* dose, double* dose2, long long n, cuda
   return cudaGetLastError();
 }
 
+cudaError_t LaunchFoldSlices(double* t, double* dose, double* dose2, long long n, long long binStride,
+                             long long sliceStride, int m, cudaStream_t st) {
+  const int blocks = int(std::min<long long>((n + 255) / 256, 152LL * 16));
+  FoldSlicesKernel<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(t, dose, dose2, n, binStride, sliceStride, m);
+  return cudaGetLastError();
+}
+
+cudaError_t LaunchTallySummary(const double* d, long long n, double* sum, unsigned long long* lastNz,
+                               cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const int blocks = int(std::min<long long>((n + 255) / 256, 152LL * 8));
+  TallySummaryKernel<<<blocks, 256, 0, st>>>(d, n, sum, lastNz);
+  return cudaGetLastError();
+}
+
 cudaError_t LaunchEnergyCheck(const double* histE, const double* histE0, long long nslots, const Segment* segs,
                               int nsegs, const JobF* jobs, cudaStream_t st) {
   if (nslots <= 0) return cudaSuccess;
-  const int blocks = int(std::min<long long>((nslots + 255) / 256, 152LL * 16));
+  const int blocks = int(std::min<long long>((nslots + 255) / 256, 152LL * 4));
   EnergyCheckKernel<<<blocks, 256, 0, st>>>(histE, histE0, nslots, segs, nsegs, jobs);
   return cudaGetLastError();
 }

@@ -152,6 +152,9 @@ int dpmx_result_config(const dpmx_result* r, long long* cfg4);
  * transported, histories, total ms */
 int dpmx_result_profile(const dpmx_result* r, double* out10);
 void dpmx_result_free(dpmx_result* r);
+/* Runs keep their device scratch (particle queues, batch tallies) in a pool
+ * for later runs on the same device; this frees the blocks no run is using. */
+void dpmx_scratch_release(void);
 
 /* ---- drop-in for Simulate(...) ---- */
 /* pencil beam from (0,0,-lbox/2) along +z through geometry geom_index; fills
