@@ -60,12 +60,21 @@ struct dpmx_result {
 
 struct dpmx_csr {
   long long rows = 0, cols = 0, nnz = 0;
-  int64_t* rowPtr = nullptr;
+  int64_t* rowPtr = nullptr;   // CSR of A (rows: voxels)
   int32_t* col = nullptr;
   float* val = nullptr;
+  int64_t* colPtr = nullptr;   // the same entries by column (CSR of A^T), for A^T y
+  int32_t* rowT = nullptr;
+  float* valT = nullptr;
+  int splits = 1;              // blocks per column of A^T y
+  double* partial = nullptr;   // [cols][splits] block sums of A^T y
   ~dpmx_csr() {
     cudaFree(rowPtr);
     cudaFree(col);
     cudaFree(val);
+    cudaFree(colPtr);
+    cudaFree(rowT);
+    cudaFree(valT);
+    cudaFree(partial);
   }
 };

@@ -1,11 +1,14 @@
 // Beamlet influence matrix A (rows: voxels, columns: beamlets) built from the
 // beamlet-tagged FP64 tally of an FP32 run, stored as CSR with FP32 values,
-// and the two products of the differentiable dose D = A w:
-//   forward  y = A x     one thread per row, FP64 accumulation
-//   backward x = A^T y   per-block column partial sums in shared memory,
-//                        one FP64 atomic per column and block
-// These are HBM-bound: each product streams the CSR arrays once
-// (4 B value + 4 B column per entry + 8 B row pointer per row).
+// plus the same entries grouped by column (CSR of A^T), and the two products
+// of the differentiable dose D = A w:
+//   forward  y = A x     kRowLanes lanes per row (coalesced row segments),
+//                        x staged in shared memory, FP64 accumulation
+//   backward x = A^T y   CSR of A^T: `splits` blocks per column each reduce a
+//                        slice of the column, then one pass sums the slices
+//                        (no atomics: the result does not depend on timing)
+// Both are HBM-bound: each streams its CSR arrays once (4 B value + 4 B index
+// per entry + 8 B pointer per row) and gathers the dense vector from L2.
 #include <cstring>
 #include <memory>
 
@@ -35,38 +38,100 @@ __global__ void FillCsrKernel(const double* dense, long long nvox, int nb, doubl
   }
 }
 
-__global__ void SpmvKernel(const int64_t* rowPtr, const int32_t* col, const float* val, long long rows, const double* x,
-                           double* y) {
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += (long long)gridDim.x * blockDim.x) {
+constexpr int kRowLanes = 16;      // lanes per row of y = A x
+constexpr int kColChunk = 2048;    // rows per block when grouping entries by column
+
+__global__ void __launch_bounds__(256) SpmvKernel(const int64_t* rowPtr, const int32_t* col, const float* val,
+                                                  long long rows, long long cols, const double* x, double* y,
+                                                  int stageX) {
+  extern __shared__ double xs[];
+  if (stageX) {
+    for (long long c = threadIdx.x; c < cols; c += blockDim.x) xs[c] = x[c];
+    __syncthreads();
+  }
+  const double* xv = stageX ? xs : x;
+  const int sub = threadIdx.x % kRowLanes;
+  const long long first = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / kRowLanes;
+  const long long stride = (long long)gridDim.x * blockDim.x / kRowLanes;
+  for (long long i = first; i < rows; i += stride) {
     double s = 0.0;
     const int64_t e = rowPtr[i + 1];
-    for (int64_t k = rowPtr[i]; k < e; ++k) s += double(__ldg(val + k)) * __ldg(x + __ldg(col + k));
-    y[i] = s;
+    for (int64_t k = rowPtr[i] + sub; k < e; k += kRowLanes) s += double(__ldg(val + k)) * xv[__ldg(col + k)];
+    for (int o = kRowLanes / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, kRowLanes);
+    if (sub == 0) y[i] = s;
   }
 }
 
-__global__ void SpmvTKernel(const int64_t* rowPtr, const int32_t* col, const float* val, long long rows,
-                            long long cols, const double* y, double* x, int useShared) {
-  extern __shared__ double part[];
-  if (useShared) {
-    for (long long c = threadIdx.x; c < cols; c += blockDim.x) part[c] = 0.0;
-    __syncthreads();
+// block (c, s): slice s of column c of A^T y
+__global__ void __launch_bounds__(256) SpmvTSliceKernel(const int64_t* colPtr, const int32_t* rowT, const float* valT,
+                                                        const double* y, int splits, double* partial) {
+  __shared__ double red[8];
+  const int c = blockIdx.x / splits, sl = blockIdx.x % splits;
+  const int64_t b0 = colPtr[c], b1 = colPtr[c + 1];
+  const int64_t len = b1 - b0;
+  const int64_t lo = b0 + len * sl / splits, hi = b0 + len * (sl + 1) / splits;
+  double s = 0.0;
+  for (int64_t k = lo + threadIdx.x; k < hi; k += blockDim.x) s += double(__ldg(valT + k)) * __ldg(y + __ldg(rowT + k));
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < int(blockDim.x >> 5); ++w) s += red[w];
+    partial[blockIdx.x] = s;
   }
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += (long long)gridDim.x * blockDim.x) {
-    const double yi = y[i];
-    if (yi == 0.0) continue;
-    const int64_t e = rowPtr[i + 1];
-    for (int64_t k = rowPtr[i]; k < e; ++k) {
-      const double v = double(__ldg(val + k)) * yi;
-      if (useShared) atomicAdd(part + __ldg(col + k), v);
-      else atomicAdd(x + __ldg(col + k), v);
+}
+
+__global__ void SumSlicesKernel(const double* partial, long long cols, int splits, double* x) {
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < cols; c += (long long)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int k = 0; k < splits; ++k) s += partial[c * splits + k];
+    x[c] = s;
+  }
+}
+
+// entries of column b in rows [chunk * kColChunk, +kColChunk): count
+__global__ void __launch_bounds__(256) ColCountKernel(const double* dense, long long nvox, int nchunks, double thr,
+                                                      long long* cnt) {
+  using BR = cub::BlockReduce<long long, 256>;
+  __shared__ typename BR::TempStorage tmp;
+  const int b = blockIdx.x / nchunks, ch = blockIdx.x % nchunks;
+  const double* d = dense + (long long)b * nvox;
+  long long n = 0;
+  for (int j = 0; j < kColChunk; j += 256) {
+    const long long i = (long long)ch * kColChunk + j + threadIdx.x;
+    if (i < nvox && fabs(d[i]) > thr) ++n;
+  }
+  n = BR(tmp).Sum(n);
+  if (threadIdx.x == 0) cnt[blockIdx.x] = n;
+}
+
+// ... and their row indices and values in row order, from offset off[block]
+__global__ void __launch_bounds__(256) ColFillKernel(const double* dense, long long nvox, int nchunks, double thr,
+                                                     const long long* off, int32_t* rowT, float* valT) {
+  using BS = cub::BlockScan<int, 256>;
+  __shared__ typename BS::TempStorage tmp;
+  const int b = blockIdx.x / nchunks, ch = blockIdx.x % nchunks;
+  const double* d = dense + (long long)b * nvox;
+  long long base = off[blockIdx.x];
+  for (int j = 0; j < kColChunk; j += 256) {
+    const long long i = (long long)ch * kColChunk + j + threadIdx.x;
+    const double v = i < nvox ? d[i] : 0.0;
+    const int f = (i < nvox && fabs(v) > thr) ? 1 : 0;
+    int pos = 0, tot = 0;
+    BS(tmp).ExclusiveSum(f, pos, tot);
+    if (f) {
+      rowT[base + pos] = int32_t(i);
+      valT[base + pos] = float(v);
     }
+    base += tot;
+    __syncthreads();   // the scan storage is reused
   }
-  if (useShared) {
-    __syncthreads();
-    for (long long c = threadIdx.x; c < cols; c += blockDim.x)
-      if (part[c] != 0.0) atomicAdd(x + c, part[c]);
-  }
+}
+
+// column pointers from the per-(column, chunk) offsets
+__global__ void ColPtrKernel(const long long* off, int cols, int nchunks, long long nnz, int64_t* colPtr) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c <= cols; c += gridDim.x * blockDim.x)
+    colPtr[c] = c < cols ? off[(long long)c * nchunks] : nnz;
 }
 
 __global__ void MaxAbsKernel(const double* a, long long n, unsigned long long* out) {
@@ -91,18 +156,21 @@ cudaError_t LaunchFillCsr(const double* dense, long long nvox, int nb, double th
   FillCsrKernel<<<Grid(nvox), 256, 0, st>>>(dense, nvox, nb, thr, rowPtr, col, val);
   return cudaGetLastError();
 }
-cudaError_t LaunchSpmv(const int64_t* rowPtr, const int32_t* col, const float* val, long long rows, const double* x,
-                       double* y, cudaStream_t st) {
-  SpmvKernel<<<Grid(rows), 256, 0, st>>>(rowPtr, col, val, rows, x, y);
+cudaError_t LaunchSpmv(const int64_t* rowPtr, const int32_t* col, const float* val, long long rows, long long cols,
+                       const double* x, double* y, cudaStream_t st) {
+  const int stageX = cols <= 6144 ? 1 : 0;
+  const long long threads = rows * kRowLanes;
+  const int blocks = int(std::max<long long>(1, std::min<long long>((threads + 255) / 256, 152LL * 8)));
+  SpmvKernel<<<blocks, 256, stageX ? cols * sizeof(double) : 0, st>>>(rowPtr, col, val, rows, cols, x, y, stageX);
   return cudaGetLastError();
 }
-cudaError_t LaunchSpmvT(const int64_t* rowPtr, const int32_t* col, const float* val, long long rows, long long cols,
-                        const double* y, double* x, cudaStream_t st) {
-  cudaError_t e = cudaMemsetAsync(x, 0, cols * sizeof(double), st);
+cudaError_t LaunchSpmvT(const dpmx_csr* a, const double* y, double* x, cudaStream_t st) {
+  if (a->cols == 0) return cudaSuccess;
+  SpmvTSliceKernel<<<int(a->cols * a->splits), 256, 0, st>>>(a->colPtr, a->rowT, a->valT, y, a->splits, a->partial);
+  const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  const int useShared = cols <= 4096 ? 1 : 0;
-  const size_t smem = useShared ? size_t(cols) * sizeof(double) : 0;
-  SpmvTKernel<<<std::min(Grid(rows), 152 * 4), 256, smem, st>>>(rowPtr, col, val, rows, cols, y, x, useShared);
+  SumSlicesKernel<<<int(std::min<long long>((a->cols + 255) / 256, 152LL)), 256, 0, st>>>(a->partial, a->cols,
+                                                                                          a->splits, x);
   return cudaGetLastError();
 }
 cudaError_t LaunchMaxAbs(const double* a, long long n, unsigned long long* outBits, cudaStream_t st) {
@@ -154,7 +222,33 @@ int dpmx_influence_build(const dpmx_result* r, int job, double threshold, dpmx_c
   CK(cudaMalloc(&a->col, std::max<long long>(1, nnz) * sizeof(int32_t)));
   CK(cudaMalloc(&a->val, std::max<long long>(1, nnz) * sizeof(float)));
   CK(LaunchFillCsr(o.d_btally, nvox, nb, thr, reinterpret_cast<const long long*>(a->rowPtr), a->col, a->val, 0));
+  // the same entries by column, in row order within a column
+  const int nchunks = int((nvox + kColChunk - 1) / kColChunk);
+  const long long nblk = (long long)nb * nchunks;
+  long long* ccnt = nullptr;
+  long long* coff = nullptr;
+  CK(cudaMalloc(&ccnt, nblk * sizeof(long long)));
+  CK(cudaMalloc(&coff, nblk * sizeof(long long)));
+  ColCountKernel<<<int(nblk), 256>>>(o.d_btally, nvox, nchunks, thr, ccnt);
+  CK(cudaGetLastError());
+  tmpBytes = 0;
+  cub::DeviceScan::ExclusiveSum(nullptr, tmpBytes, ccnt, coff, nblk);
+  CK(cudaMalloc(&tmp, tmpBytes));
+  CK(cub::DeviceScan::ExclusiveSum(tmp, tmpBytes, ccnt, coff, nblk));
+  cudaFree(tmp);
+  CK(cudaMalloc(&a->colPtr, (nb + 1) * sizeof(int64_t)));
+  CK(cudaMalloc(&a->rowT, std::max<long long>(1, nnz) * sizeof(int32_t)));
+  CK(cudaMalloc(&a->valT, std::max<long long>(1, nnz) * sizeof(float)));
+  ColFillKernel<<<int(nblk), 256>>>(o.d_btally, nvox, nchunks, thr, coff, a->rowT, a->valT);
+  CK(cudaGetLastError());
+  ColPtrKernel<<<1, 256>>>(coff, nb, nchunks, nnz, a->colPtr);
+  CK(cudaGetLastError());
+  // enough column slices to fill the GPU with blocks of A^T y
+  a->splits = int(std::max<long long>(1, (4LL * 152 * 4 + nb - 1) / nb));
+  CK(cudaMalloc(&a->partial, (long long)nb * a->splits * sizeof(double)));
   CK(cudaDeviceSynchronize());
+  cudaFree(ccnt);
+  cudaFree(coff);
   *out = a.release();
   return DPMX_OK;
 }
@@ -177,13 +271,13 @@ int dpmx_csr_device(const dpmx_csr* a, const int64_t** row_ptr, const int32_t** 
 
 int dpmx_csr_spmv(const dpmx_csr* a, const double* x, double* y, void* stream) {
   if (!a || !x || !y) return Fail(DPMX_ERR_ARG, "null argument");
-  CK(LaunchSpmv(a->rowPtr, a->col, a->val, a->rows, x, y, static_cast<cudaStream_t>(stream)));
+  CK(LaunchSpmv(a->rowPtr, a->col, a->val, a->rows, a->cols, x, y, static_cast<cudaStream_t>(stream)));
   return DPMX_OK;
 }
 
 int dpmx_csr_spmv_t(const dpmx_csr* a, const double* y, double* x, void* stream) {
   if (!a || !x || !y) return Fail(DPMX_ERR_ARG, "null argument");
-  CK(LaunchSpmvT(a->rowPtr, a->col, a->val, a->rows, a->cols, y, x, static_cast<cudaStream_t>(stream)));
+  CK(LaunchSpmvT(a, y, x, static_cast<cudaStream_t>(stream)));
   return DPMX_OK;
 }
 

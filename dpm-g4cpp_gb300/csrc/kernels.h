@@ -77,6 +77,7 @@ struct JobF {                  // per-job geometry, source and tally (device vie
   float e0, e1, cx, cy, fx, fy;
   uint32_t k0, k1;             // Philox key (job seed)
   RunCounters* cnt;
+  int dbase;                   // first bin of this job in a block's shared depth tally, or -1
 };
 
 struct Segment {               // a run of primaries of one job inside a chunk
@@ -118,7 +119,12 @@ struct PhaseArgs {
   double* histE0;              // per-slot primary energy
   unsigned long long* overflow;
   int aggregate;               // warp-aggregated tally atomics
+  int depthBins;               // > 0: depth tallies summed per block in shared memory first
+  int depthStride;             //      (bins per job; job j at j * depthStride)
 };
+
+// shared-memory depth tally of a block (slab jobs): bins of all jobs of a run
+constexpr int kDepthBins = 1024;
 
 cudaError_t LaunchPhotonPhase(const PhaseArgs& a, int blocks, int threads, cudaStream_t st);
 cudaError_t LaunchElectronPhase(const PhaseArgs& a, int blocks, int threads, cudaStream_t st);
@@ -141,6 +147,7 @@ cudaError_t LaunchTableEval32(const DevTables<float>& T, int q, int imat, const 
 int ElectronPhaseSmemBytes(const DevTables<float>& T);
 // block-batched electron phase (256 threads per block, shared-memory slots)
 int BlockPhaseSmemBytes(const DevTables<float>& T);
+int BlockPhaseBlocksPerSM();
 cudaError_t PrepareBlockPhase(const DevTables<float>& T);
 cudaError_t LaunchElectronPhaseBlock(const PhaseArgs& a, int blocks, cudaStream_t st);
 
@@ -149,10 +156,8 @@ cudaError_t LaunchCountNnz(const double* dense, long long nvox, int nb, double t
                            cudaStream_t st);
 cudaError_t LaunchFillCsr(const double* dense, long long nvox, int nb, double thr, const long long* rowPtr,
                           int32_t* col, float* val, cudaStream_t st);
-cudaError_t LaunchSpmv(const int64_t* rowPtr, const int32_t* col, const float* val, long long rows, const double* x,
-                       double* y, cudaStream_t st);
-cudaError_t LaunchSpmvT(const int64_t* rowPtr, const int32_t* col, const float* val, long long rows, long long cols,
-                        const double* y, double* x, cudaStream_t st);
+cudaError_t LaunchSpmv(const int64_t* rowPtr, const int32_t* col, const float* val, long long rows, long long cols,
+                       const double* x, double* y, cudaStream_t st);
 cudaError_t LaunchMaxAbs(const double* a, long long n, unsigned long long* outBits, cudaStream_t st);
 
 }  // namespace dpmx

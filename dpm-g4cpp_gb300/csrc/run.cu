@@ -257,6 +257,16 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
       hj[r * njobs + j].tally = tB + off[j] * binStride + r * sliceStride;
     }
   }
+  // slab jobs: the depth tallies are summed per block in shared memory first
+  // when the bins of all sub-jobs fit
+  bool allSlab = true;
+  int maxNz = 1;
+  for (int j = 0; j < njobs; ++j) {
+    allSlab = allSlab && outs[j].slab;
+    maxNz = std::max(maxNz, jobs[j].phantom->grid.nz);
+  }
+  const int depthBins = (allSlab && (long long)nsub * maxNz <= kDepthBins) ? nsub * maxNz : 0;
+  for (int k = 0; k < nsub; ++k) hj[k].dbase = depthBins ? k * maxNz : -1;
   JobF* dj;
   if (int rc = buf.Get(&dj, nsub)) return rc;
   CK(cudaMemcpyAsync(dj, hj.data(), nsub * sizeof(JobF), cudaMemcpyHostToDevice, st));
@@ -294,7 +304,7 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
     if (int rc = AllocQueue(buf, qp[k], cap)) return rc;
   }
   const int blocks = nsm * cfg.blocksPerSM;
-  const int eblocks = nsm * 2;   // block-batched electron phase: 2 resident blocks per SM
+  const int eblocks = nsm * BlockPhaseBlocksPerSM();   // block-batched electron phase: one wave
   if (cfg.eblock) CK(PrepareBlockPhase(T->t32));
   long long nl = 0;
   auto enqueue = [&](cudaStream_t s) -> int {
@@ -321,6 +331,8 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
           a.histE0 = histE0;
           a.overflow = ovf;
           a.aggregate = cfg.aggregate;
+          a.depthBins = depthBins;
+          a.depthStride = maxNz;
           // photons of generation g; their electrons join generation g
           a.segs = sP; a.nsegs = int(c.segP.size()); a.nPrimaries = (g == 0) ? c.nP : 0;
           a.in = qp[g & 1]; a.inCount = cntP + g * kStripes;

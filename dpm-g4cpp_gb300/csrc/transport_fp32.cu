@@ -101,6 +101,17 @@ __device__ void StageElectronTables(const DevTables<float>& T, float* sdata, ETa
   __syncthreads();
 }
 
+// the same tables read in place (global memory, cached in L1); one thread
+__device__ void BindElectronTables(const DevTables<float>& T, ETables* et) {
+  for (int m = 0; m < T.nmat; ++m) {
+    et->dedx[m] = T.dedx[m];
+    et->itr1[m] = T.itr1[m];
+    et->brem[m] = T.brem[m];
+  }
+  et->k1 = T.k1;
+  et->moller = T.moller;
+}
+
 // spline value at e whose log (of the unclamped value) is le
 __device__ __forceinline__ float SplineLe(const SplineT<float>& s, float e, float le) {
   const float ec = fminf(s.emaxm, fmaxf(s.emin, e));
@@ -173,10 +184,22 @@ __device__ __forceinline__ bool Append(const Queue& q, unsigned long long* count
 // ---------------------------------------------------------------------------
 // tallies
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void Score(const JobF& J, int ix, int iy, int iz, uint32_t hist, float e, int agg) {
+// a block's shared-memory depth tally (energy and scoring steps per bin), or none
+struct DepthAcc {
+  double* e = nullptr;
+  unsigned* n = nullptr;
+};
+
+__device__ __forceinline__ void Score(const JobF& J, int ix, int iy, int iz, uint32_t hist, float e, int agg,
+                                      const DepthAcc& d = DepthAcc()) {
+  const double de = double(e);
+  if (d.e != nullptr && J.dbase >= 0) {   // depth tally of a slab job: block-local first
+    atomicAdd(d.e + J.dbase + iz, de);
+    atomicAdd(d.n + J.dbase + iz, 1u);
+    return;
+  }
   const long long idx = J.tallyDepth ? (long long)iz : ((long long)iz * J.ny + iy) * J.nx + ix;
   double* ptr = J.tally + idx * J.tstride;
-  const double de = double(e);
   if (agg) {
     cg::coalesced_group g = cg::coalesced_threads();
     cg::coalesced_group peers = cg::labeled_partition(g, (unsigned long long)ptr);
@@ -189,6 +212,35 @@ __device__ __forceinline__ void Score(const JobF& J, int ix, int iy, int iz, uin
   if (J.btally) {
     const long long nvox = (long long)J.nx * J.ny * J.nz;
     atomicAdd(J.btally + (long long)(hist % uint32_t(J.nbeamlets)) * nvox + idx, de);
+  }
+}
+
+// bytes of a depth tally of `bins` bins (energy, then step counts)
+__host__ __device__ constexpr size_t DepthAccBytes(int bins) { return size_t(bins) * (sizeof(double) + sizeof(unsigned)); }
+
+// the block's depth tally at `mem` (dynamic shared memory, 8-byte aligned),
+// zeroed; before the block's first barrier
+__device__ __forceinline__ DepthAcc DepthAccInit(const PhaseArgs& a, unsigned char* mem) {
+  DepthAcc d;
+  if (a.depthBins > 0) {
+    d.e = reinterpret_cast<double*>(mem);
+    d.n = reinterpret_cast<unsigned*>(mem + size_t(a.depthBins) * sizeof(double));
+    for (int b = threadIdx.x; b < a.depthBins; b += blockDim.x) { d.e[b] = 0.0; d.n[b] = 0u; }
+  }
+  return d;
+}
+
+// adds the block's depth tally to the jobs' tallies (whole block, at its end)
+__device__ __forceinline__ void DepthAccFlush(const PhaseArgs& a, const JobF* jobs, const DepthAcc& d) {
+  if (d.e == nullptr) return;
+  __syncthreads();
+  for (int b = threadIdx.x; b < a.depthBins; b += blockDim.x) {
+    const unsigned n = d.n[b];
+    if (n == 0u) continue;
+    const JobF& J = jobs[b / a.depthStride];
+    const int iz = b % a.depthStride;
+    atomicAdd(J.tally + (long long)iz * J.tstride, d.e[b]);
+    if (J.steps) atomicAdd(J.steps + iz, double(n));
   }
 }
 
@@ -375,12 +427,14 @@ __device__ __forceinline__ unsigned long long StripePrefix(const unsigned long l
 }
 
 __global__ void __launch_bounds__(256) PhotonPhase(PhaseArgs a) {
+  extern __shared__ __align__(16) unsigned char pdyn[];   // the depth tally, when used
   __shared__ JobF sjobs[16];
   __shared__ unsigned long long spre[kStripes + 1];
   const bool fewJobs = a.njobs <= 16;
   if (fewJobs) {
     for (int j = threadIdx.x; j < a.njobs; j += blockDim.x) sjobs[j] = a.jobs[j];
   }
+  const DepthAcc dacc = DepthAccInit(a, pdyn);
   const unsigned long long nQ = StripePrefix(a.inCount, spre);
   const JobF* jobs = fewJobs ? sjobs : a.jobs;
   const unsigned long long total = (unsigned long long)a.nPrimaries + nQ;
@@ -463,7 +517,7 @@ __global__ void __launch_bounds__(256) PhotonPhase(PhaseArgs a) {
           float sn, cs;
           __sincosf(phPhi, &sn, &cs);
           if (elE < T.ecut) {
-            Score(J, p.ix, p.iy, p.iz, p.hist, elE, a.aggregate);
+            Score(J, p.ix, p.iy, p.iz, p.hist, elE, a.aggregate, dacc);
             acc += elE;
           } else {
             const float e0 = kappa;
@@ -479,7 +533,7 @@ __global__ void __launch_bounds__(256) PhotonPhase(PhaseArgs a) {
           }
           p.e = phE;
           if (p.e < T.gcut) {
-            Score(J, p.ix, p.iy, p.iz, p.hist, p.e, a.aggregate);
+            Score(J, p.ix, p.iy, p.iz, p.hist, p.e, a.aggregate, dacc);
             acc += p.e;
             done = true;
           } else {
@@ -496,7 +550,7 @@ __global__ void __launch_bounds__(256) PhotonPhase(PhaseArgs a) {
             const float e1 = rng.U() * sum;
             const float e2 = sum - e1;
             if (e2 < T.ecut) {
-              Score(J, p.ix, p.iy, p.iz, p.hist, e2, a.aggregate);
+              Score(J, p.ix, p.iy, p.iz, p.hist, e2, a.aggregate, dacc);
               acc += e2;
             } else {
               PState c = p;
@@ -505,7 +559,7 @@ __global__ void __launch_bounds__(256) PhotonPhase(PhaseArgs a) {
               if (!Append(a.outE, a.outECount, a.overflow, c)) acc += e2;
             }
             if (e1 < T.ecut) {
-              Score(J, p.ix, p.iy, p.iz, p.hist, e1, a.aggregate);
+              Score(J, p.ix, p.iy, p.iz, p.hist, e1, a.aggregate, dacc);
               acc += e1;
               // annihilation at rest (SimDPMLike.cc:753-791)
               const float cost = 1.0f - 2.0f * rng.U();
@@ -530,12 +584,12 @@ __global__ void __launch_bounds__(256) PhotonPhase(PhaseArgs a) {
             done = true;
           } else if (r1 < prob) {
             // below threshold (pair IMFP floor): treated as photoelectric
-            Score(J, p.ix, p.iy, p.iz, p.hist, p.e, a.aggregate);
+            Score(J, p.ix, p.iy, p.iz, p.hist, p.e, a.aggregate, dacc);
             acc += p.e;
             done = true;
           } else {
             // photoelectric absorption
-            Score(J, p.ix, p.iy, p.iz, p.hist, p.e, a.aggregate);
+            Score(J, p.ix, p.iy, p.iz, p.hist, p.e, a.aggregate, dacc);
             acc += p.e;
             done = true;
           }
@@ -548,6 +602,7 @@ __global__ void __launch_bounds__(256) PhotonPhase(PhaseArgs a) {
     }
   }
   esc.Flush(jobs);
+  DepthAccFlush(a, jobs, dacc);
   for (int o = 16; o > 0; o >>= 1) nph += __shfl_down_sync(kFull, nph, o);
   if (lane == 0 && a.njobs > 0) atomicAdd(&a.jobs[0].cnt->photonSteps, nph);
 }
@@ -848,6 +903,9 @@ __global__ void __launch_bounds__(256) ElectronPhase(PhaseArgs a) {
 // reached it, so that the code of one interaction runs with full warps.
 // ---------------------------------------------------------------------------
 constexpr int kSlots = 512;
+constexpr int kBlockMinBlocks = 3;      // resident blocks per SM the kernel is compiled for
+constexpr bool kTablesInSmem = false;  // electron tables staged per block, else read through L1
+constexpr bool kClaimItems = true;     // warps claim 32 items at a time, else a fixed share each
 constexpr uint32_t kFAxis = 3u, kFHinge = 4u, kFNeedGeom = 8u, kFPositron = 16u, kFAlive = 32u;
 
 struct SlotArrays {     // shared-memory state of the resident electrons
@@ -858,30 +916,53 @@ struct SlotArrays {     // shared-memory state of the resident electrons
   uint32_t hist[kSlots], slot[kSlots], ulo[kSlots], uhi[kSlots], ctr[kSlots], pst[kSlots];
   double acc[kSlots];
 };
-// Every slot sits in exactly one of six lists, by what it does next: MSC
-// hinge, MSC step end, brem, Moller, plain sub-step, idle. The lists share
-// three arrays (one kind filled from the front, one from the back) and are
-// double-buffered: an iteration reads one buffer and fills the other. Their
-// counts rotate over three sets, so that the set an iteration reads, the set
-// it fills and the set it clears for the next iteration are never the same
+// The block's slots are split between kGroups independent groups of
+// kGroupThreads threads (four warps), each with its own lists and its own
+// named barrier, so that a group waits only for its own slowest warp.
+constexpr int kGroups = 1, kGroupThreads = 256 / kGroups, kGroupSlots = kSlots / kGroups;
+// Every slot of a group sits in exactly one of six lists, by what it does
+// next: MSC hinge, MSC step end, brem, Moller, plain sub-step, idle. The lists
+// share three arrays (one kind filled from the front, one from the back) and
+// are double-buffered: an iteration reads one buffer and fills the other.
+// Their counts rotate over three sets, so that the set an iteration reads, the
+// set it fills and the set it clears for the next iteration are never the same
 // and one barrier per iteration suffices.
-enum : int { kLHinge, kLMscEnd, kLBrem, kLMoller, kLStep, kLIdle, kLExhausted, kLCounts = 8 };
+// (kLClaim: the iteration's item counter when warps claim items as they go)
+enum : int { kLHinge, kLMscEnd, kLBrem, kLMoller, kLStep, kLIdle, kLExhausted, kLClaim, kLCounts = 8 };
 struct SlotLists {
-  uint16_t ev[2][kSlots];    // hinge from the front, MSC step end from the back
-  uint16_t ia[2][kSlots];    // brem from the front, Moller from the back
-  uint16_t run[2][kSlots];   // plain sub-step from the front, idle from the back
+  uint16_t ev[2][kGroupSlots];    // hinge from the front, MSC step end from the back
+  uint16_t ia[2][kGroupSlots];    // brem from the front, Moller from the back
+  uint16_t run[2][kGroupSlots];   // plain sub-step from the front, idle from the back
   int cnt[3][kLCounts];
 };
 
-__host__ __device__ constexpr size_t BlockPhaseStaticBytes() { return sizeof(SlotArrays) + sizeof(SlotLists); }
+__host__ __device__ constexpr size_t BlockPhaseStaticBytes() {
+  return sizeof(SlotArrays) + kGroups * sizeof(SlotLists);
+}
 
-// warp-aggregated push of v onto a shared list, from its front or its back
+// dynamic shared memory of the block kernel: slots, lists, the electron tables
+// when staged, then the depth tally of `depthBins` bins
+__host__ __device__ inline size_t BlockPhaseSmemBytesFor(const DevTables<float>& T, int depthBins) {
+  const size_t b = BlockPhaseStaticBytes() + (kTablesInSmem ? size_t(T.elecCount) * sizeof(float) : 0);
+  return ((b + 15) & ~size_t(15)) + DepthAccBytes(depthBins);
+}
+
+// warp-aggregated push of v onto a group's list, from its front or its back
 __device__ __forceinline__ void Push(uint16_t* list, int* n, int v, bool back) {
   cg::coalesced_group g = cg::coalesced_threads();
   int base = 0;
   if (g.thread_rank() == 0) base = atomicAdd(n, int(g.size()));
   const int pos = g.shfl(base, 0) + int(g.thread_rank());
-  list[back ? kSlots - 1 - pos : pos] = uint16_t(v);
+  list[back ? kGroupSlots - 1 - pos : pos] = uint16_t(v);
+}
+
+// barrier of the kGroupThreads threads of group g (ids 1 and 2; 0 is
+// __syncthreads). Immediate ids keep the kernel's barrier count low.
+__device__ __forceinline__ void GroupSync(int g) {
+  static_assert(kGroups == 1 || kGroups == 2, "one barrier id per group");
+  if (kGroups == 1) __syncthreads();
+  else if (g == 0) asm volatile("bar.sync 1, %0;" ::"n"(kGroupThreads) : "memory");
+  else asm volatile("bar.sync 2, %0;" ::"n"(kGroupThreads) : "memory");
 }
 
 __device__ __forceinline__ void LoadSlot(const SlotArrays& S, int k, PState& p, EState& s, uint32_t& fl) {
@@ -936,8 +1017,9 @@ __device__ __forceinline__ void AnnihilateF(const PhaseArgs& a, const PState& p,
 
 // one condensed-history sub-step of slot k. Returns 0 to keep stepping,
 // 1 brem, 2 Moller, 3 MSC hinge, 4 MSC step end, 5 finished.
+template <int AGG>
 __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, const JobF* jobs, SlotArrays& S,
-                                        int k, EscTally& esc, unsigned long long& nsteps) {
+                                        int k, EscTally& esc, unsigned long long& nsteps, const DepthAcc& dacc) {
   const DevTables<float>& T = a.T;
   PState p;
   EState s;
@@ -1003,7 +1085,7 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
       const float edep = p.e;
       p.e = 0.f;
       if (!positron) {
-        Score(J, p.ix, p.iy, p.iz, p.hist, edep, a.aggregate);
+        Score(J, p.ix, p.iy, p.iz, p.hist, edep, AGG, dacc);
         acc += edep;
       } else {
         bool inside;
@@ -1017,14 +1099,14 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
           PRng rng;
           SlotRng(S, k, J, p, rng);
           AnnihilateF(a, p, rng, acc);
-          Score(J, p.ix, p.iy, p.iz, p.hist, edep, a.aggregate);
+          Score(J, p.ix, p.iy, p.iz, p.hist, edep, AGG, dacc);
           acc += edep;
         }
       }
       code = 5;
     } else {
       p.e = ef;
-      Score(J, p.ix, p.iy, p.iz, p.hist, de, a.aggregate);
+      Score(J, p.ix, p.iy, p.iz, p.hist, de, AGG, dacc);
       acc += de;
       if (what == 0) {
         if (!MoveToFace(J, p, step, s.axis) || !Settle(J, p, s.sGeom, s.axis)) {
@@ -1094,7 +1176,9 @@ __device__ __forceinline__ void EventMscEnd(const PhaseArgs& a, const ETables& e
 
 // bremsstrahlung (SimDPMLike.cc:172-194, :661-695); false when the electron
 // fell below the tracking cut and finished
-__device__ __forceinline__ bool EventBrem(const PhaseArgs& a, const JobF* jobs, SlotArrays& S, int k) {
+template <int AGG>
+__device__ __forceinline__ bool EventBrem(const PhaseArgs& a, const JobF* jobs, SlotArrays& S, int k,
+                                         const DepthAcc& dacc) {
   PState p;
   EState s;
   uint32_t fl;
@@ -1123,7 +1207,7 @@ __device__ __forceinline__ bool EventBrem(const PhaseArgs& a, const JobF* jobs, 
     p.e -= eg;
   }
   if (p.e < T.ecut) {
-    Score(J, p.ix, p.iy, p.iz, p.hist, p.e, a.aggregate);
+    Score(J, p.ix, p.iy, p.iz, p.hist, p.e, AGG, dacc);
     acc += p.e;
     if ((fl & kFPositron) != 0) AnnihilateF(a, p, rng, acc);
     atomicAdd(a.histE + p.slot, acc);
@@ -1211,10 +1295,11 @@ __device__ __forceinline__ bool RefillSlot(const PhaseArgs& a, const ETables& et
   return true;
 }
 
-__global__ void __launch_bounds__(256, 2) ElectronPhaseB(PhaseArgs a) {
+template <int AGG>
+__global__ void __launch_bounds__(256, kBlockMinBlocks) ElectronPhaseB(PhaseArgs a) {
   extern __shared__ __align__(16) unsigned char dyn[];
   SlotArrays& S = *reinterpret_cast<SlotArrays*>(dyn);
-  SlotLists& L = *reinterpret_cast<SlotLists*>(dyn + sizeof(SlotArrays));
+  SlotLists* Lg = reinterpret_cast<SlotLists*>(dyn + sizeof(SlotArrays));
   float* sdata = reinterpret_cast<float*>(dyn + BlockPhaseStaticBytes());
   __shared__ ETables et;
   __shared__ JobF sjobs[16];
@@ -1222,18 +1307,22 @@ __global__ void __launch_bounds__(256, 2) ElectronPhaseB(PhaseArgs a) {
   const bool fewJobs = a.njobs <= 16;
   if (fewJobs)
     for (int j = threadIdx.x; j < a.njobs; j += blockDim.x) sjobs[j] = a.jobs[j];
+  const DepthAcc dacc = DepthAccInit(a, dyn + BlockPhaseSmemBytesFor(a.T, 0));
   const unsigned long long nQ = StripePrefix(a.inCount, spre);
   const JobF* jobs = fewJobs ? sjobs : a.jobs;
   const unsigned long long total = (unsigned long long)a.nPrimaries + nQ;
   if (total == 0) return;   // an empty generation skips the table staging
-  StageElectronTables(a.T, sdata, &et);
-  const int tid = threadIdx.x, nthr = blockDim.x;
-  // all slots start idle
-  for (int k = tid; k < kSlots; k += nthr) {
-    S.flags[k] = 0u;
-    L.run[0][kSlots - 1 - k] = uint16_t(k);
+  if (kTablesInSmem) StageElectronTables(a.T, sdata, &et);
+  else if (threadIdx.x == 0) BindElectronTables(a.T, &et);   // visible after the barrier below
+  const int tid = threadIdx.x;
+  const int grp = tid / kGroupThreads, gt = tid % kGroupThreads;
+  SlotLists& L = Lg[grp];
+  // all slots of the group start idle
+  for (int k = gt; k < kGroupSlots; k += kGroupThreads) {
+    S.flags[grp * kGroupSlots + k] = 0u;
+    L.run[0][kGroupSlots - 1 - k] = uint16_t(grp * kGroupSlots + k);
   }
-  for (int c = tid; c < 3 * kLCounts; c += nthr) (&L.cnt[0][0])[c] = (c == kLIdle) ? kSlots : 0;
+  for (int c = gt; c < 3 * kLCounts; c += kGroupThreads) (&L.cnt[0][0])[c] = (c == kLIdle) ? kGroupSlots : 0;
   __syncthreads();
   EscTally esc;
   unsigned long long nsteps = 0;
@@ -1246,12 +1335,25 @@ __global__ void __launch_bounds__(256, 2) ElectronPhaseB(PhaseArgs a) {
               e4 = e3 + nr[kLStep];
     const bool exhausted = nr[kLExhausted] != 0;
     if (e4 == 0 && exhausted) break;
-    if (tid == 0) {
+    if (gt == 0) {
       for (int c = 0; c < kLCounts; ++c) L.cnt[cz][c] = 0;
       if (exhausted) nw[kLExhausted] = 1;
     }
     // each slot once: its pending interaction or its refill, then one sub-step
-    for (int i = tid; i < kSlots; i += nthr) {
+    const int lane = tid & 31;
+    int claimed = kClaimItems ? 0 : gt - lane;
+    for (;;) {
+      // the warp's next 32 items: claimed from the iteration's counter (the
+      // warps that finish early take more), or a fixed stride
+      if (kClaimItems) {
+        int b = 0;
+        if (lane == 0) b = atomicAdd(&L.cnt[cr][kLClaim], 32);
+        claimed = __shfl_sync(kFull, b, 0);
+      }
+      if (claimed >= kGroupSlots) break;
+      const int i = claimed + lane;
+      if (!kClaimItems) claimed += kGroupThreads;
+      if (i >= kGroupSlots) continue;
       int k;
       bool live = true;
       if (i < e4) {
@@ -1259,19 +1361,19 @@ __global__ void __launch_bounds__(256, 2) ElectronPhaseB(PhaseArgs a) {
           k = L.ev[lr][i];
           EventHinge(a, jobs, S, k);
         } else if (i < e1) {
-          k = L.ev[lr][kSlots - 1 - (i - e0)];
+          k = L.ev[lr][kGroupSlots - 1 - (i - e0)];
           EventMscEnd(a, et, jobs, S, k);
         } else if (i < e2) {
           k = L.ia[lr][i - e1];
-          live = EventBrem(a, jobs, S, k);
+          live = EventBrem<AGG>(a, jobs, S, k, dacc);
         } else if (i < e3) {
-          k = L.ia[lr][kSlots - 1 - (i - e2)];
+          k = L.ia[lr][kGroupSlots - 1 - (i - e2)];
           EventMoller(a, et, jobs, S, k);
         } else {
           k = L.run[lr][i - e3];
         }
       } else {
-        k = L.run[lr][kSlots - 1 - (i - e4)];
+        k = L.run[lr][kGroupSlots - 1 - (i - e4)];
         live = false;
         if (!exhausted) {
           // one claim on the work counter per warp
@@ -1284,7 +1386,7 @@ __global__ void __launch_bounds__(256, 2) ElectronPhaseB(PhaseArgs a) {
           if (item < total) live = RefillSlot(a, et, jobs, spre, S, k, item, esc);
         }
       }
-      const int code = live ? StepSlot(a, et, jobs, S, k, esc, nsteps) : 5;
+      const int code = live ? StepSlot<AGG>(a, et, jobs, S, k, esc, nsteps, dacc) : 5;
       switch (code) {
         case 0: Push(L.run[lw], &nw[kLStep], k, false); break;
         case 1: Push(L.ia[lw], &nw[kLBrem], k, false); break;
@@ -1294,11 +1396,12 @@ __global__ void __launch_bounds__(256, 2) ElectronPhaseB(PhaseArgs a) {
         default: Push(L.run[lw], &nw[kLIdle], k, true); break;
       }
     }
-    __syncthreads();
+    GroupSync(grp);
     cr = cw;
     lr = lw;
   }
   esc.Flush(jobs);
+  DepthAccFlush(a, jobs, dacc);
   for (int o = 16; o > 0; o >>= 1) nsteps += __shfl_down_sync(kFull, nsteps, o);
   if ((tid & 31) == 0 && a.njobs > 0) atomicAdd(&a.jobs[0].cnt->steps, nsteps);
 }
@@ -1449,20 +1552,25 @@ __global__ void TableKernel32(DevTables<float> T, int q, int imat, const double*
 int ElectronPhaseSmemBytes(const DevTables<float>& T) { return int(T.elecCount * sizeof(float)); }
 
 cudaError_t LaunchPhotonPhase(const PhaseArgs& a, int blocks, int threads, cudaStream_t st) {
-  PhotonPhase<<<blocks, threads, 0, st>>>(a);
+  PhotonPhase<<<blocks, threads, DepthAccBytes(a.depthBins), st>>>(a);
   return cudaGetLastError();
 }
 
-int BlockPhaseSmemBytes(const DevTables<float>& T) {
-  return int(BlockPhaseStaticBytes() + size_t(T.elecCount) * sizeof(float));
-}
+int BlockPhaseSmemBytes(const DevTables<float>& T) { return int(BlockPhaseSmemBytesFor(T, kDepthBins)); }
+
+int BlockPhaseBlocksPerSM() { return kBlockMinBlocks; }
 
 cudaError_t PrepareBlockPhase(const DevTables<float>& T) {
-  return cudaFuncSetAttribute(ElectronPhaseB, cudaFuncAttributeMaxDynamicSharedMemorySize, BlockPhaseSmemBytes(T));
+  const int smem = BlockPhaseSmemBytes(T);
+  cudaError_t e = cudaFuncSetAttribute(ElectronPhaseB<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(ElectronPhaseB<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
 }
 
 cudaError_t LaunchElectronPhaseBlock(const PhaseArgs& a, int blocks, cudaStream_t st) {
-  ElectronPhaseB<<<blocks, 256, BlockPhaseSmemBytes(a.T), st>>>(a);
+  const size_t smem = BlockPhaseSmemBytesFor(a.T, a.depthBins);
+  if (a.aggregate) ElectronPhaseB<1><<<blocks, 256, smem, st>>>(a);
+  else ElectronPhaseB<0><<<blocks, 256, smem, st>>>(a);
   return cudaGetLastError();
 }
 

@@ -10,6 +10,7 @@ import numpy as np
 from . import Job, Phantom, Source
 
 WATER, LUNG, BONE = 0, 1, 2
+AIR = 3          # data/water_lung_bone_air only
 VACUUM = 255
 MEV_TO_J = 1.602176634e-13
 
@@ -94,11 +95,14 @@ def differentiation_setup(seed=4, n=128, v=2.0):
     return m, src, target
 
 
-def full_scale_phantom(seed=99, nx=512, ny=512, nz=256, v=1.0):
+def full_scale_phantom(seed=99, nx=512, ny=512, nz=256, v=1.0, outside=AIR):
     """Synthetic CT-like phantom (512x512x256 x 1 mm): an elliptical water body
     (semi-axes 180 mm in x and 120 mm in z, long axis along y), two lung
-    ellipsoids, a bone spine cylinder along y and a bone rib shell; vacuum
-    outside the body. The beam enters along +z (anterior face)."""
+    ellipsoids, a bone spine cylinder along y and a bone rib shell; air (of the
+    water/lung/bone/air data set) outside the body. The beam enters along +z
+    (anterior face) through the air gap. Vacuum voxels would end every track
+    that reaches them, as in the reference's transport, so they are not used
+    around the body."""
     rng = np.random.default_rng(seed)
     x = voxel_centres(nx, v, -0.5 * nx * v)
     y = voxel_centres(ny, v, -0.5 * ny * v)
@@ -108,7 +112,7 @@ def full_scale_phantom(seed=99, nx=512, ny=512, nz=256, v=1.0):
     ell = (xx / 180.0) ** 2 + ((zz - zc) / 120.0) ** 2
     body = ell < 1.0
     ribs = (ell > 0.80) & (ell < 0.86)
-    sl = np.where(body, WATER, VACUUM).astype(np.uint8)
+    sl = np.where(body, WATER, outside).astype(np.uint8)
     m = np.repeat(sl[:, None, :], ny, axis=1)
     thorax = (y > -120.0 + rng.uniform(-10, 10)) & (y < 120.0 + rng.uniform(-10, 10))
     rib_mask = np.broadcast_to(ribs[:, None, :], m.shape) & thorax[None, :, None]
@@ -117,7 +121,7 @@ def full_scale_phantom(seed=99, nx=512, ny=512, nz=256, v=1.0):
         cx = sx * rng.uniform(60.0, 80.0)
         lung = _ellipsoid(m.shape, v, (cx, rng.uniform(-10, 10), zc), (rng.uniform(45, 55), rng.uniform(90, 110),
                                                                       rng.uniform(60, 75)))
-        m[lung & (m != VACUUM)] = LUNG
+        m[lung & (m != outside)] = LUNG
     spine = (xx ** 2 + (zz - (zc + 85.0)) ** 2) < 15.0 ** 2
     m[np.broadcast_to(spine[:, None, :], m.shape)] = BONE
     return m

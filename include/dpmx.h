@@ -72,8 +72,9 @@ int dpmx_tables_material_name(const dpmx_tables* t, int imat, char* name, int ca
  * depth tally (bins of lbox along +z) */
 int dpmx_phantom_slab(const dpmx_tables* t, int geom_index, double lbox_mm, dpmx_phantom** out);
 /* nx*ny*nz voxels (x fastest) of vx*vy*vz mm, material ids from the host array
- * mat (255 = vacuum); the phantom spans x in [-nx*vx/2, nx*vx/2], y likewise,
- * z in [0, nz*vz]; 3-D tally */
+ * mat (255 = vacuum: as in the reference's transport, SimDPMLike.cc:88-93 and
+ * :282-287, a track that enters a vacuum voxel ends there); the phantom spans
+ * x in [-nx*vx/2, nx*vx/2], y likewise, z in [0, nz*vz]; 3-D tally */
 int dpmx_phantom_voxels(const dpmx_tables* t, int nx, int ny, int nz, double vx, double vy, double vz,
                         const uint8_t* mat, dpmx_phantom** out);
 void dpmx_phantom_free(dpmx_phantom* p);
@@ -205,7 +206,9 @@ int dpmx_csr_shape(const dpmx_csr* a, long long* rows, long long* cols, long lon
 int dpmx_csr_device(const dpmx_csr* a, const int64_t** row_ptr, const int32_t** col, const float** val);
 /* y[rows] = A x[cols]; device pointers, FP64 vectors, FP64 accumulation */
 int dpmx_csr_spmv(const dpmx_csr* a, const double* x, double* y, void* stream);
-/* x[cols] = A^T y[rows]; device pointers */
+/* x[cols] = A^T y[rows]; device pointers. Uses per-matrix scratch: calls on
+ * one matrix must not overlap (same stream, or ordered by the caller). The
+ * result does not depend on scheduling (no atomics). */
 int dpmx_csr_spmv_t(const dpmx_csr* a, const double* y, double* x, void* stream);
 /* host copies of the three CSR arrays (sizes from dpmx_csr_shape) */
 int dpmx_csr_download(const dpmx_csr* a, int64_t* row_ptr, int32_t* col, float* val);
