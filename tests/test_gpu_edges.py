@@ -1,0 +1,104 @@
+"""Edge cases and size-independent properties of the FP32 event form.
+
+* empty and ragged jobs (0 histories, fewer histories than batches);
+* vacuum voxels end every track that reaches them (SimDPMLike.cc:88-93,
+  :282-287, :495-500), so nothing is scored behind a vacuum layer;
+* the block-local depth tally of slab jobs gives the same dose as global
+  atomics (a history's deposits do not depend on the batching);
+* the full-size precision workload (128x128x256 x 2 mm, 1e7 histories):
+  every history conserves energy, nothing is lost, and the FP32 dose agrees
+  with the FP64 plain form within statistics.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_empty_and_ragged_jobs(tables_wlb, dpm):
+    m = np.zeros((16, 16, 16), dtype=np.uint8)
+    ph = dpm.Phantom.voxels(tables_wlb, m, 2.0)
+    src = dpm.Source(particle=0, e0=5.0, e1=5.0, shape=1, fx=10.0, fy=10.0)
+    jobs = [dpm.Job(ph, src, 0, 1), dpm.Job(ph, src, 1, 2), dpm.Job(ph, src, 7, 3), dpm.Job(ph, src, 1000, 4)]
+    r = dpm.run(tables_wlb, jobs, batches=10)
+    d0, q0, _ = r.tally(0)
+    assert not d0.any() and not q0.any()
+    for j, job in enumerate(jobs):
+        st = r.stats(j)
+        assert st.histories == job.histories
+        assert st.lost == 0 and st.residual_violations == 0
+        assert abs(st.edep + st.escaped - st.primary_energy) <= 1e-6 * max(1.0, st.primary_energy)
+    # each job equals the same job run alone
+    for j in (1, 2, 3):
+        alone = dpm.run(tables_wlb, [jobs[j]], batches=10).tally(0)[0]
+        np.testing.assert_allclose(r.tally(j)[0], alone, rtol=1e-10, atol=1e-12 * max(1.0, alone.max()))
+
+
+def test_vacuum_layer_ends_tracks(tables_wlb, dpm):
+    m = np.zeros((40, 16, 16), dtype=np.uint8)
+    ph_water = dpm.Phantom.voxels(tables_wlb, m, 2.0)
+    m[10:12] = 255                      # vacuum layer at z = 20..24 mm
+    ph = dpm.Phantom.voxels(tables_wlb, m, 2.0)
+    src = dpm.Source(particle=-1, e0=10.0, e1=10.0, shape=0)
+    r = dpm.run(tables_wlb, [dpm.Job(ph, src, 20000, 5)], batches=5)
+    w = dpm.run(tables_wlb, [dpm.Job(ph_water, src, 20000, 5)], batches=5)
+    d, dw = r.tally(0)[0], w.tally(0)[0]
+    st = r.stats(0)
+    assert not d[10:12].any()           # nothing is scored in vacuum
+    # no electron crosses the layer: behind it only bremsstrahlung photons
+    # (which can step over it, Woodcock tracking) deposit energy
+    assert d[12:16].sum() < 0.2 * dw[12:16].sum()
+    assert st.lost == 0 and st.residual_violations == 0
+    assert abs(st.edep + st.escaped - st.primary_energy) <= 1e-6 * st.primary_energy
+
+
+def test_all_vacuum_phantom(tables_wlb, dpm):
+    m = np.full((8, 8, 8), 255, dtype=np.uint8)
+    ph = dpm.Phantom.voxels(tables_wlb, m, 2.0)
+    r = dpm.run(tables_wlb, [dpm.Job(ph, dpm.Source(particle=0, e0=3.0, e1=3.0), 500, 6)], batches=2)
+    st = r.stats(0)
+    assert st.edep == 0.0
+    assert abs(st.escaped - 500 * 3.0) < 1e-6
+    assert st.histories == 500
+
+
+def test_block_depth_tally_equals_global(tables_c3, dpm):
+    ph = dpm.Phantom.slab(tables_c3, 3, 1.0)
+    src = dpm.Source(particle=-1, e0=15.0, e1=15.0)
+    # 10 batches x 101 bins fit the block-local depth tally; 20 do not
+    a = dpm.run(tables_c3, [dpm.Job(ph, src, 20000, 77)], batches=10)
+    b = dpm.run(tables_c3, [dpm.Job(ph, src, 20000, 77)], batches=20)
+    da, _, sa = a.tally(0)
+    db, _, sb = b.tally(0)
+    np.testing.assert_allclose(da, db, rtol=1e-10, atol=1e-12 * da.max())
+    np.testing.assert_array_equal(sa, sb)
+
+
+def test_precision_workload_full_size(tables_wlb, dpm):
+    from importlib import import_module
+    wl = import_module("dpm-g4cpp_gb300.workloads")
+    m = wl.precision_phantom()
+    ph = dpm.Phantom.voxels(tables_wlb, m, 2.0)
+    src = wl.precision_source()
+    n32, n64 = 10**7, 10**6
+    r32 = dpm.run(tables_wlb, [dpm.Job(ph, src, n32, 7)], batches=10)
+    st = r32.stats(0)
+    assert st.lost == 0 and st.residual_violations == 0 and st.histories == n32
+    assert abs(st.edep + st.escaped - st.primary_energy) < 1e-6 * st.primary_energy
+    r64 = dpm.run(tables_wlb, [dpm.Job(ph, src, n64, 8)], precision=dpm.FP64_PLAIN, batches=10)
+    d32, q32, _ = r32.tally(0)
+    d64, q64, _ = r64.tally(0)
+    # depth-dose profiles (summed over x, y) per history, with batch errors
+    def profile(d, q, n):
+        pz = d.sum(axis=(1, 2)) / n
+        # the batch sums of a profile bin are not kept; bound its error by the
+        # sum of the voxel errors (an overestimate, so the test stays fair)
+        sz = np.sqrt(np.maximum(q * 10 - d * d, 0.0) / 9).sum(axis=(1, 2)) / n
+        return pz, sz
+    p32, s32 = profile(d32, q32, n32)
+    p64, s64 = profile(d64, q64, n64)
+    mask = p64 > 0.1 * p64.max()
+    rel = (p32[mask] - p64[mask]) / p64[mask]
+    assert np.abs(rel).mean() < 0.01, np.abs(rel).mean()
+    assert (np.abs(p32[mask] - p64[mask]) <= 2 * np.sqrt(s32[mask] ** 2 + s64[mask] ** 2)).mean() >= 0.95
+    assert abs(d32.sum() / n32 / (d64.sum() / n64) - 1.0) < 0.005
