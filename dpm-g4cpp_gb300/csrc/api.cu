@@ -88,8 +88,13 @@ void PutSplines(const std::vector<const Curve*>& curves, std::vector<SplineT<R>*
 
 template <class R>
 void PutLinear(const Curve& c, LinearT<R>& s, Image<R>& img, Fixup& fx, double emin, double emax) {
+  // FP64 keeps the file's grid points (the reference interpolates between
+  // them); FP32 keeps the values only and places them on the uniform grid
   std::vector<R> v;
-  for (size_t i = 0; i < c.x.size(); ++i) { v.push_back(R(c.x[i])); v.push_back(R(c.y[i])); }
+  for (size_t i = 0; i < c.x.size(); ++i) {
+    if (sizeof(R) == sizeof(double)) v.push_back(R(c.x[i]));
+    v.push_back(R(c.y[i]));
+  }
   fx.Add(reinterpret_cast<const void**>(&s.p), img.Put(v.data(), v.size() * sizeof(R)));
   s.n = int(c.x.size());
   s.xmin = R(c.x[0]);
@@ -138,13 +143,15 @@ int BuildImage(const HostTables& h, DevTables<R>& T, void** dptr) {
   PutSplines<R>({&h.k1}, {&T.k1}, img, fx, h.k1.x.front(), h.k1.x.back(), f3, n3);
   PutSplines<R>({&h.moller}, {&T.moller}, img, fx, h.moller.x.front(), h.moller.x.back(), f4, n4);
   const size_t elecEnd = f4 + n4 * sizeof(R);
-  // photon linear tables
+  // photon linear tables, contiguous
+  const size_t photBegin = (img.bytes.size() + 255) & ~size_t(255);
   PutLinear<R>(h.imfpMax, T.imfpMax, img, fx, h.imfpMax.x.front(), h.imfpMax.x.back());
   for (int m = 0; m < h.nmat; ++m) {
     PutLinear<R>(h.tot[m], T.tot[m], img, fx, h.tot[0].x.front(), h.tot[0].x.back());
     PutLinear<R>(h.comp[m], T.comp[m], img, fx, h.comp[0].x.front(), h.comp[0].x.back());
     PutLinear<R>(h.pair[m], T.pair[m], img, fx, h.pair[0].x.front(), h.pair[0].x.back());
   }
+  const size_t photEnd = img.bytes.size();
   // sampling tables
   std::vector<double> knE, molE;
   for (auto& t : h.kn) knE.push_back(t.e);
@@ -171,6 +178,8 @@ int BuildImage(const HostTables& h, DevTables<R>& T, void** dptr) {
   }
   fx.Add(reinterpret_cast<const void**>(&T.elecBase), f0);
   T.elecCount = int((elecEnd - f0) / sizeof(R));
+  fx.Add(reinterpret_cast<const void**>(&T.photBase), photBegin);
+  T.photCount = int((photEnd - photBegin) / sizeof(R));
   void* d = nullptr;
   CK(cudaMalloc(&d, img.bytes.size()));
   CK(cudaMemcpy(d, img.bytes.data(), img.bytes.size(), cudaMemcpyHostToDevice));

@@ -96,14 +96,15 @@ __device__ __forceinline__ double LinearGet(const LinearT<double>& s, double e) 
   const double* q = s.p + 2 * il;
   return mmax(1.0E-20, (q[3] - q[1]) * (e - q[0]) / (q[2] - q[0]) + q[1]);
 }
-// FP32 form: uniform grid, multiply by the inverse spacing instead of dividing
+// FP32 form: values on the uniform grid x_i = xmin + i / invDelta; the
+// position inside the interval comes from the grid, not from stored points
 __device__ __forceinline__ float LinearGet(const LinearT<float>& s, float e) {
   e = mmin(s.emaxm, mmax(s.emin, e));
-  int il = int((e - s.xmin) * s.invDelta);
+  const float t = (e - s.xmin) * s.invDelta;
+  int il = int(t);
   il = il < 0 ? 0 : (il > s.n - 2 ? s.n - 2 : il);
-  const float2 a = __ldg(reinterpret_cast<const float2*>(s.p) + il);
-  const float2 b = __ldg(reinterpret_cast<const float2*>(s.p) + il + 1);
-  return mmax(1.0E-20f, (b.y - a.y) * (e - a.x) * s.invDelta + a.y);
+  const float y0 = s.p[il], y1 = s.p[il + 1];
+  return mmax(1.0E-20f, (y1 - y0) * (t - float(il)) + y0);
 }
 
 // ---------------------------------------------------------------------------

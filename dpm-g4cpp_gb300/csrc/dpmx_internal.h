@@ -26,7 +26,7 @@ struct SplineT {       // natural cubic spline on a log-uniform grid: n x {x,y,b
   R logMin, invLogDelta, emin, emaxm;   // emaxm = emax - 1e-6 (loader clamp)
 };
 template <class R>
-struct LinearT {       // linear interpolation on a uniform grid: n x {x,y}
+struct LinearT {       // linear interpolation on a uniform grid: n x {x,y} (FP64), n x y (FP32)
   const R* p;
   int n;
   R xmin, invDelta, emin, emaxm;
@@ -62,6 +62,8 @@ struct DevTables {
   GSSetT<R> gs;
   const R* elecBase;   // electron spline data are contiguous from here ...
   int elecCount;       // ... for this many values (shared-memory staging)
+  const R* photBase;   // the photon linear tables likewise
+  int photCount;
 };
 
 // ---------------------------------------------------------------------------

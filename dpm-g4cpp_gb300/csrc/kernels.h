@@ -126,6 +126,7 @@ struct PhaseArgs {
 // shared-memory depth tally of a block (slab jobs): bins of all jobs of a run
 constexpr int kDepthBins = 1024;
 
+cudaError_t PreparePhotonPhase(const DevTables<float>& T);   // shared-memory limit, once per run
 cudaError_t LaunchPhotonPhase(const PhaseArgs& a, int blocks, int threads, cudaStream_t st);
 cudaError_t LaunchElectronPhase(const PhaseArgs& a, int blocks, int threads, cudaStream_t st);
 // dose += t, dose2 += t^2, t = 0 over n bins

@@ -306,6 +306,7 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
   const int blocks = nsm * cfg.blocksPerSM;
   const int eblocks = nsm * BlockPhaseBlocksPerSM();   // block-batched electron phase: one wave
   if (cfg.eblock) CK(PrepareBlockPhase(T->t32));
+  CK(PreparePhotonPhase(T->t32));
   long long nl = 0;
   auto enqueue = [&](cudaStream_t s) -> int {
     size_t segCur = 0, ci = 0;

@@ -75,6 +75,12 @@ struct PRng {
   }
 };
 
+// photon linear tables, staged in shared memory or read in place
+constexpr bool kPhotonTablesInSmem = false;   // no measured gain: the photon phase waits on the phantom
+struct PTables {
+  LinearT<float> imfpMax, tot[kMaxMat], comp[kMaxMat], pair[kMaxMat];
+};
+
 // shared-memory copies of the electron spline tables
 struct ETables {
   SplineT<float> dedx[kMaxMat], itr1[kMaxMat], brem[kMaxMat], k1, moller;
@@ -99,6 +105,32 @@ __device__ void StageElectronTables(const DevTables<float>& T, float* sdata, ETa
     et->moller = Rebase(T.moller, T.elecBase, sdata);
   }
   __syncthreads();
+}
+
+__device__ __forceinline__ LinearT<float> RebaseL(const LinearT<float>& s, const float* gbase, float* sbase) {
+  LinearT<float> r = s;
+  r.p = sbase + (s.p - gbase);
+  return r;
+}
+
+// the photon tables of T into shared memory at sdata (whole block; no barrier:
+// the caller's next barrier publishes them), or their global addresses
+__device__ void StagePhotonTables(const DevTables<float>& T, bool stage, float* sdata, PTables* pt) {
+  if (stage)
+    for (int i = threadIdx.x; i < T.photCount; i += blockDim.x) sdata[i] = T.photBase[i];
+  if (threadIdx.x == 0) {
+    pt->imfpMax = stage ? RebaseL(T.imfpMax, T.photBase, sdata) : T.imfpMax;
+    for (int m = 0; m < T.nmat; ++m) {
+      pt->tot[m] = stage ? RebaseL(T.tot[m], T.photBase, sdata) : T.tot[m];
+      pt->comp[m] = stage ? RebaseL(T.comp[m], T.photBase, sdata) : T.comp[m];
+      pt->pair[m] = stage ? RebaseL(T.pair[m], T.photBase, sdata) : T.pair[m];
+    }
+  }
+}
+
+// bytes of dynamic shared memory the photon phase stages its tables in
+__host__ __device__ inline size_t PhotonTableBytes(const DevTables<float>& T) {
+  return kPhotonTablesInSmem ? ((size_t(T.photCount) * sizeof(float) + 15) & ~size_t(15)) : 0;
 }
 
 // the same tables read in place (global memory, cached in L1); one thread
@@ -427,18 +459,21 @@ __device__ __forceinline__ unsigned long long StripePrefix(const unsigned long l
 }
 
 __global__ void __launch_bounds__(256) PhotonPhase(PhaseArgs a) {
-  extern __shared__ __align__(16) unsigned char pdyn[];   // the depth tally, when used
+  extern __shared__ __align__(16) unsigned char pdyn[];   // photon tables, then the depth tally
   __shared__ JobF sjobs[16];
   __shared__ unsigned long long spre[kStripes + 1];
+  __shared__ PTables pt;
   const bool fewJobs = a.njobs <= 16;
   if (fewJobs) {
     for (int j = threadIdx.x; j < a.njobs; j += blockDim.x) sjobs[j] = a.jobs[j];
   }
-  const DepthAcc dacc = DepthAccInit(a, pdyn);
   const unsigned long long nQ = StripePrefix(a.inCount, spre);
   const JobF* jobs = fewJobs ? sjobs : a.jobs;
   const unsigned long long total = (unsigned long long)a.nPrimaries + nQ;
-  if (total == 0) return;
+  if (total == 0) return;   // an empty generation skips the table staging
+  StagePhotonTables(a.T, kPhotonTablesInSmem, reinterpret_cast<float*>(pdyn), &pt);
+  const DepthAcc dacc = DepthAccInit(a, pdyn + PhotonTableBytes(a.T));
+  __syncthreads();
   const int lane = threadIdx.x & 31;
   const DevTables<float>& T = a.T;
 
@@ -491,7 +526,7 @@ __global__ void __launch_bounds__(256) PhotonPhase(PhaseArgs a) {
       continue;
     }
     ++nph;
-    const float lmax = 1.0f / LinearGet(T.imfpMax, p.e);
+    const float lmax = 1.0f / LinearGet(pt.imfpMax, p.e);
     const float step = -lmax * __logf(rng.U());
     int im = -1;
     if (Fly(J, p, step)) im = MaterialAt(J, p.ix, p.iy, p.iz);
@@ -502,9 +537,9 @@ __global__ void __launch_bounds__(256) PhotonPhase(PhaseArgs a) {
     } else {
       const float rho = T.density[im];
       const float r1 = rng.U();
-      float prob = 1.0f - LinearGet(T.tot[im], p.e) * rho * lmax;
+      float prob = 1.0f - LinearGet(pt.tot[im], p.e) * rho * lmax;
       if (r1 >= prob) {
-        prob += LinearGet(T.comp[im], p.e) * rho * lmax;
+        prob += LinearGet(pt.comp[im], p.e) * rho * lmax;
         if (r1 < prob) {
           // Compton (SimDPMLike.cc:512-570)
           const float a3 = rng.U(), a2 = rng.U(), a1 = rng.U();
@@ -543,7 +578,7 @@ __global__ void __launch_bounds__(256) PhotonPhase(PhaseArgs a) {
             p.dx = u1; p.dy = u2; p.dz = u3;
           }
         } else {
-          prob += LinearGet(T.pair[im], p.e) * rho * lmax;
+          prob += LinearGet(pt.pair[im], p.e) * rho * lmax;
           if (r1 < prob && p.e > 2.0f * kEMC2f) {
             // pair production (SimDPMLike.cc:573-627)
             const float sum = p.e - 2.0f * kEMC2f;
@@ -992,6 +1027,32 @@ __device__ __forceinline__ void StoreSlot(SlotArrays& S, int k, const PState& p,
                ((p.meta & 3u) == 2u ? kFPositron : 0u) | (alive ? kFAlive : 0u) | ((p.meta >> 2) << 8);
 }
 
+// the part of slot k a plain sub-step reads (direction, the MSC hinge state
+// and the Moller IMFP stay as they are), and the part it writes back
+__device__ __forceinline__ void LoadStepState(const SlotArrays& S, int k, PState& p, EState& s, uint32_t& fl) {
+  const uint32_t v = S.vox[k];
+  p.ix = int(v & 0x7ffu); p.iy = int((v >> 11) & 0x7ffu); p.iz = int(v >> 22);
+  p.lx = S.lx[k]; p.ly = S.ly[k]; p.lz = S.lz[k];
+  p.dx = S.dx[k]; p.dy = S.dy[k]; p.dz = S.dz[k];
+  p.e = S.e[k];
+  fl = S.flags[k];
+  p.hist = S.hist[k]; p.slot = S.slot[k]; p.ulo = S.ulo[k]; p.uhi = S.uhi[k];
+  p.meta = ((fl >> 8) << 2) | ((fl & kFPositron) ? 2u : 1u);
+  s.nTr1 = S.nTr1[k]; s.nMol = S.nMol[k]; s.invMol = S.invMol[k]; s.nBrem = S.nBrem[k]; s.sGeom = S.sGeom[k];
+  s.axis = int(fl & kFAxis);
+  s.hinge = (fl & kFHinge) != 0;
+  s.needGeom = (fl & kFNeedGeom) != 0;
+}
+
+__device__ __forceinline__ void StoreStepState(SlotArrays& S, int k, const PState& p, const EState& s,
+                                               uint32_t fl) {
+  S.vox[k] = PackVox(p.ix, p.iy, p.iz);
+  S.lx[k] = p.lx; S.ly[k] = p.ly; S.lz[k] = p.lz;
+  S.e[k] = p.e;
+  S.nTr1[k] = s.nTr1; S.nMol[k] = s.nMol; S.nBrem[k] = s.nBrem; S.sGeom[k] = s.sGeom;
+  S.flags[k] = (fl & ~(kFAxis | kFNeedGeom)) | (uint32_t(s.axis) & kFAxis) | (s.needGeom ? kFNeedGeom : 0u);
+}
+
 // random stream of slot k (a fresh Philox block per use; the counter advances)
 __device__ __forceinline__ void SlotRng(const SlotArrays& S, int k, const JobF& J, const PState& p, PRng& r) {
   r.Init(J.k0, J.k1, p.hist, p.ulo, p.uhi);
@@ -1024,7 +1085,7 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
   PState p;
   EState s;
   uint32_t fl;
-  LoadSlot(S, k, p, s, fl);
+  LoadStepState(S, k, p, s, fl);
   const int job = int(fl >> 8);
   const JobF& J = jobs[job];
   const bool positron = (fl & kFPositron) != 0;
@@ -1127,7 +1188,7 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
     S.flags[k] = 0u;
   } else {
     S.acc[k] = acc;
-    StoreSlot(S, k, p, s, true);
+    StoreStepState(S, k, p, s, fl);
   }
   return code;
 }
@@ -1551,8 +1612,13 @@ __global__ void TableKernel32(DevTables<float> T, int q, int imat, const double*
 
 int ElectronPhaseSmemBytes(const DevTables<float>& T) { return int(T.elecCount * sizeof(float)); }
 
+cudaError_t PreparePhotonPhase(const DevTables<float>& T) {
+  return cudaFuncSetAttribute(PhotonPhase, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              int(PhotonTableBytes(T) + DepthAccBytes(kDepthBins)));
+}
+
 cudaError_t LaunchPhotonPhase(const PhaseArgs& a, int blocks, int threads, cudaStream_t st) {
-  PhotonPhase<<<blocks, threads, DepthAccBytes(a.depthBins), st>>>(a);
+  PhotonPhase<<<blocks, threads, PhotonTableBytes(a.T) + DepthAccBytes(a.depthBins), st>>>(a);
   return cudaGetLastError();
 }
 
