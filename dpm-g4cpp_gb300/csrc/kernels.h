@@ -118,6 +118,7 @@ struct PhaseArgs {
   double* histE;               // per-slot energy accounted (deposit + escape)
   double* histE0;              // per-slot primary energy
   unsigned long long* overflow;
+  unsigned long long* fault;   // blocks that abandoned a bounded wait (results incomplete)
   int aggregate;               // warp-aggregated tally atomics
   int depthBins;               // > 0: depth tallies summed per block in shared memory first
   int depthStride;             //      (bins per job; job j at j * depthStride)

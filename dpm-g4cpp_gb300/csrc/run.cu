@@ -32,9 +32,10 @@ namespace {
 
 constexpr int kGen = 32;                              // generations per chunk
 // per chunk: striped counts of the electron and photon queues of every
-// generation, the two work counters of every generation, and the overflow count
+// generation, the two work counters of every generation, the overflow count
+// and the count of blocks that abandoned a bounded wait
 constexpr int kCntStride = (kGen + 1) * kStripes;
-constexpr int kCtrPerChunk = 2 * kCntStride + 2 * (kGen + 1) + 1;
+constexpr int kCtrPerChunk = 2 * kCntStride + 2 * (kGen + 1) + 2;
 constexpr long long kMaxChunk = 1LL << 24;            // default upper bound of histories per chunk
 constexpr int kQueuePerPrimary = 6;                   // queue entries per primary of a chunk and generation
 constexpr bool kInterleaveSlices = false;             // batch slices: per bin (true) or one after another
@@ -318,6 +319,7 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
         unsigned long long* headE = cc + 2 * kCntStride;     // [gen]
         unsigned long long* headP = headE + (kGen + 1);
         unsigned long long* ovf = headP + (kGen + 1);
+        unsigned long long* fault = ovf + 1;
         const Segment* sP = dsegs + segCur;
         const Segment* sE = sP + c.segP.size();
         const Segment* sA = sE + c.segE.size();
@@ -331,6 +333,7 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
           a.histE = histE;
           a.histE0 = histE0;
           a.overflow = ovf;
+          a.fault = fault;
           a.aggregate = cfg.aggregate;
           a.depthBins = depthBins;
           a.depthStride = maxNz;
@@ -424,12 +427,13 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
   // results: leftovers beyond the last generation and queue overflows are losses
   std::vector<unsigned long long> hc(nchunks * kCtrPerChunk);
   CK(cudaMemcpy(hc.data(), ctr, hc.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
-  unsigned long long lost = 0, leftover = 0, overflowed = 0;
+  unsigned long long lost = 0, leftover = 0, overflowed = 0, faults = 0;
   double nElec = 0, nPhot = 0;
   for (size_t ci = 0; ci < nchunks; ++ci) {
     const unsigned long long* cc = hc.data() + ci * kCtrPerChunk;
     for (int k = 0; k < kStripes; ++k) leftover += cc[kGen * kStripes + k] + cc[kCntStride + kGen * kStripes + k];
     overflowed += cc[2 * kCntStride + 2 * (kGen + 1)];
+    faults += cc[2 * kCntStride + 2 * (kGen + 1) + 1];
     for (int g = 0; g < kGen; ++g)
       for (int k = 0; k < kStripes; ++k) {
         nElec += double(cc[g * kStripes + k]);
@@ -479,6 +483,8 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
     outs[j].cnt.deposited = hsum[j];
     if (outs[j].slab) outs[j].maxIz = hlast[j] > 0 ? int(hlast[j] - 1) : 0;
   }
+  if (faults > 0)
+    return Fail(DPMX_ERR_CUDA, std::to_string(faults) + " blocks of the electron phase gave up a wait; run incomplete");
   lost = leftover + overflowed;
   // losses of the queues are reported on job 0
   if (njobs > 0) outs[0].cnt.lost += lost;

@@ -940,7 +940,6 @@ __global__ void __launch_bounds__(256) ElectronPhase(PhaseArgs a) {
 constexpr int kSlots = 512;
 constexpr int kBlockMinBlocks = 3;      // resident blocks per SM the kernel is compiled for
 constexpr bool kTablesInSmem = false;  // electron tables staged per block, else read through L1
-constexpr bool kClaimItems = true;     // warps claim 32 items at a time, else a fixed share each
 constexpr uint32_t kFAxis = 3u, kFHinge = 4u, kFNeedGeom = 8u, kFPositron = 16u, kFAlive = 32u;
 
 struct SlotArrays {     // shared-memory state of the resident electrons
@@ -951,28 +950,33 @@ struct SlotArrays {     // shared-memory state of the resident electrons
   uint32_t hist[kSlots], slot[kSlots], ulo[kSlots], uhi[kSlots], ctr[kSlots], pst[kSlots];
   double acc[kSlots];
 };
-// The block's slots are split between kGroups independent groups of
-// kGroupThreads threads (four warps), each with its own lists and its own
-// named barrier, so that a group waits only for its own slowest warp.
-constexpr int kGroups = 1, kGroupThreads = 256 / kGroups, kGroupSlots = kSlots / kGroups;
-// Every slot of a group sits in exactly one of six lists, by what it does
+// The block's slots form kSets sets with their own lists. With two sets the
+// warps alternate between them: when a warp has no more items of one set's
+// iteration it signals that set's split-phase barrier and goes on to the other
+// set, and waits for the first set's iteration to complete only when it comes
+// back to it, so the wait for the slowest warp of an iteration overlaps with
+// work. With one set the iteration ends at a block barrier.
+constexpr int kSets = 1;   // two sets measured slower: shorter lists, less uniform warps
+constexpr int kSetSlots = kSlots / kSets;
+constexpr long long kWaitCycles = 4LL << 30;   // bound of one wait (~2 s): then the block gives up
+// Every slot of a set sits in exactly one of six lists, by what it does
 // next: MSC hinge, MSC step end, brem, Moller, plain sub-step, idle. The lists
 // share three arrays (one kind filled from the front, one from the back) and
 // are double-buffered: an iteration reads one buffer and fills the other.
 // Their counts rotate over three sets, so that the set an iteration reads, the
 // set it fills and the set it clears for the next iteration are never the same
 // and one barrier per iteration suffices.
-// (kLClaim: the iteration's item counter when warps claim items as they go)
+// (kLClaim: the iteration's item counter, from which warps claim items)
 enum : int { kLHinge, kLMscEnd, kLBrem, kLMoller, kLStep, kLIdle, kLExhausted, kLClaim, kLCounts = 8 };
 struct SlotLists {
-  uint16_t ev[2][kGroupSlots];    // hinge from the front, MSC step end from the back
-  uint16_t ia[2][kGroupSlots];    // brem from the front, Moller from the back
-  uint16_t run[2][kGroupSlots];   // plain sub-step from the front, idle from the back
+  uint16_t ev[2][kSetSlots];    // hinge from the front, MSC step end from the back
+  uint16_t ia[2][kSetSlots];    // brem from the front, Moller from the back
+  uint16_t run[2][kSetSlots];   // plain sub-step from the front, idle from the back
   int cnt[3][kLCounts];
 };
 
 __host__ __device__ constexpr size_t BlockPhaseStaticBytes() {
-  return sizeof(SlotArrays) + kGroups * sizeof(SlotLists);
+  return sizeof(SlotArrays) + kSets * sizeof(SlotLists);
 }
 
 // dynamic shared memory of the block kernel: slots, lists, the electron tables
@@ -982,22 +986,45 @@ __host__ __device__ inline size_t BlockPhaseSmemBytesFor(const DevTables<float>&
   return ((b + 15) & ~size_t(15)) + DepthAccBytes(depthBins);
 }
 
-// warp-aggregated push of v onto a group's list, from its front or its back
+// warp-aggregated push of v onto a set's list, from its front or its back
 __device__ __forceinline__ void Push(uint16_t* list, int* n, int v, bool back) {
   cg::coalesced_group g = cg::coalesced_threads();
   int base = 0;
   if (g.thread_rank() == 0) base = atomicAdd(n, int(g.size()));
   const int pos = g.shfl(base, 0) + int(g.thread_rank());
-  list[back ? kGroupSlots - 1 - pos : pos] = uint16_t(v);
+  list[back ? kSetSlots - 1 - pos : pos] = uint16_t(v);
 }
 
-// barrier of the kGroupThreads threads of group g (ids 1 and 2; 0 is
-// __syncthreads). Immediate ids keep the kernel's barrier count low.
-__device__ __forceinline__ void GroupSync(int g) {
-  static_assert(kGroups == 1 || kGroups == 2, "one barrier id per group");
-  if (kGroups == 1) __syncthreads();
-  else if (g == 0) asm volatile("bar.sync 1, %0;" ::"n"(kGroupThreads) : "memory");
-  else asm volatile("bar.sync 2, %0;" ::"n"(kGroupThreads) : "memory");
+// split-phase barrier of a slot set: an mbarrier in shared memory that
+// completes a phase when every warp of the block has arrived once
+__device__ __forceinline__ void SetBarrierInit(uint64_t* bar, int warps) {
+  asm volatile("mbarrier.init.shared.b64 [%0], %1;" ::"r"(uint32_t(__cvta_generic_to_shared(bar))), "r"(warps)
+               : "memory");
+}
+// one arrival per warp (lane 0, after the warp's writes to the set)
+__device__ __forceinline__ void SetBarrierArrive(uint64_t* bar) {
+  __syncwarp();
+  if ((threadIdx.x & 31) == 0)
+    asm volatile("{ .reg .b64 st; mbarrier.arrive.shared.b64 st, [%0]; }" ::"r"(
+                     uint32_t(__cvta_generic_to_shared(bar)))
+                 : "memory");
+  __syncwarp();
+}
+// waits until phase `phase` of the barrier has completed; false after
+// kWaitCycles (the caller then abandons the phase and reports it)
+__device__ __forceinline__ bool SetBarrierWait(uint64_t* bar, int phase) {
+  const uint32_t addr = uint32_t(__cvta_generic_to_shared(bar));
+  const long long t0 = clock64();
+  for (;;) {
+    uint32_t ok = 0;
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+        : "=r"(ok)
+        : "r"(addr), "r"(uint32_t(phase & 1))
+        : "memory");
+    if (ok) return true;
+    if (clock64() - t0 > kWaitCycles) return false;
+  }
 }
 
 __device__ __forceinline__ void LoadSlot(const SlotArrays& S, int k, PState& p, EState& s, uint32_t& fl) {
@@ -1375,92 +1402,109 @@ __global__ void __launch_bounds__(256, kBlockMinBlocks) ElectronPhaseB(PhaseArgs
   if (total == 0) return;   // an empty generation skips the table staging
   if (kTablesInSmem) StageElectronTables(a.T, sdata, &et);
   else if (threadIdx.x == 0) BindElectronTables(a.T, &et);   // visible after the barrier below
-  const int tid = threadIdx.x;
-  const int grp = tid / kGroupThreads, gt = tid % kGroupThreads;
-  SlotLists& L = Lg[grp];
-  // all slots of the group start idle
-  for (int k = gt; k < kGroupSlots; k += kGroupThreads) {
-    S.flags[grp * kGroupSlots + k] = 0u;
-    L.run[0][kGroupSlots - 1 - k] = uint16_t(grp * kGroupSlots + k);
+  const int tid = threadIdx.x, lane = tid & 31;
+  __shared__ __align__(8) uint64_t setBar[kSets];
+  // all slots start idle
+  for (int k = tid; k < kSlots; k += blockDim.x) {
+    S.flags[k] = 0u;
+    Lg[k / kSetSlots].run[0][kSetSlots - 1 - k % kSetSlots] = uint16_t(k);
   }
-  for (int c = gt; c < 3 * kLCounts; c += kGroupThreads) (&L.cnt[0][0])[c] = (c == kLIdle) ? kGroupSlots : 0;
+  for (int c = tid; c < kSets * 3 * kLCounts; c += blockDim.x) {
+    const int j = c % (3 * kLCounts);
+    (&Lg[c / (3 * kLCounts)].cnt[0][0])[j] = (j == kLIdle) ? kSetSlots : 0;
+  }
+  if (kSets > 1 && tid == 0)
+    for (int st = 0; st < kSets; ++st) SetBarrierInit(&setBar[st], int(blockDim.x >> 5));
   __syncthreads();
   EscTally esc;
   unsigned long long nsteps = 0;
-  int cr = 0, lr = 0;   // count set and list buffer read by this iteration
-  for (;;) {
-    const int cw = cr == 2 ? 0 : cr + 1, cz = cw == 2 ? 0 : cw + 1, lw = lr ^ 1;
-    const int* nr = L.cnt[cr];
-    int* nw = L.cnt[cw];
-    const int e0 = nr[kLHinge], e1 = e0 + nr[kLMscEnd], e2 = e1 + nr[kLBrem], e3 = e2 + nr[kLMoller],
-              e4 = e3 + nr[kLStep];
-    const bool exhausted = nr[kLExhausted] != 0;
-    if (e4 == 0 && exhausted) break;
-    if (gt == 0) {
-      for (int c = 0; c < kLCounts; ++c) L.cnt[cz][c] = 0;
-      if (exhausted) nw[kLExhausted] = 1;
-    }
-    // each slot once: its pending interaction or its refill, then one sub-step
-    const int lane = tid & 31;
-    int claimed = kClaimItems ? 0 : gt - lane;
-    for (;;) {
-      // the warp's next 32 items: claimed from the iteration's counter (the
-      // warps that finish early take more), or a fixed stride
-      if (kClaimItems) {
+  // per set: iteration (its list buffer is it & 1), count set read, still running
+  int it0 = 0, it1 = 0, cr0 = 0, cr1 = 0;
+  bool run0 = true, run1 = kSets > 1, gaveUp = false;
+  while ((run0 || run1) && !gaveUp) {
+#pragma unroll 1
+    for (int st = 0; st < kSets; ++st) {
+      if (!(st ? run1 : run0)) continue;
+      const int itS = st ? it1 : it0;
+      // the set's previous iteration must be complete on every warp
+      if (kSets > 1 && itS > 0 && !SetBarrierWait(&setBar[st], itS - 1)) {
+        gaveUp = true;
+        break;
+      }
+      SlotLists& L = Lg[st];
+      const int lr = itS & 1, lw = lr ^ 1;
+      const int cr = st ? cr1 : cr0, cw = cr == 2 ? 0 : cr + 1, cz = cw == 2 ? 0 : cw + 1;
+      const int* nr = L.cnt[cr];
+      int* nw = L.cnt[cw];
+      const int e0 = nr[kLHinge], e1 = e0 + nr[kLMscEnd], e2 = e1 + nr[kLBrem], e3 = e2 + nr[kLMoller],
+                e4 = e3 + nr[kLStep];
+      const bool exhausted = nr[kLExhausted] != 0;
+      if (e4 == 0 && exhausted) {   // the same decision on every warp (same counts)
+        if (st) run1 = false; else run0 = false;
+        continue;
+      }
+      if (tid == 0) {
+        for (int c = 0; c < kLCounts; ++c) L.cnt[cz][c] = 0;
+        if (exhausted) nw[kLExhausted] = 1;
+      }
+      // each slot once: its pending interaction or its refill, then one
+      // sub-step; a warp claims 32 items at a time, so warps that finish
+      // early take more
+      for (;;) {
         int b = 0;
         if (lane == 0) b = atomicAdd(&L.cnt[cr][kLClaim], 32);
-        claimed = __shfl_sync(kFull, b, 0);
-      }
-      if (claimed >= kGroupSlots) break;
-      const int i = claimed + lane;
-      if (!kClaimItems) claimed += kGroupThreads;
-      if (i >= kGroupSlots) continue;
-      int k;
-      bool live = true;
-      if (i < e4) {
-        if (i < e0) {
-          k = L.ev[lr][i];
-          EventHinge(a, jobs, S, k);
-        } else if (i < e1) {
-          k = L.ev[lr][kGroupSlots - 1 - (i - e0)];
-          EventMscEnd(a, et, jobs, S, k);
-        } else if (i < e2) {
-          k = L.ia[lr][i - e1];
-          live = EventBrem<AGG>(a, jobs, S, k, dacc);
-        } else if (i < e3) {
-          k = L.ia[lr][kGroupSlots - 1 - (i - e2)];
-          EventMoller(a, et, jobs, S, k);
+        const int claimed = __shfl_sync(kFull, b, 0);
+        if (claimed >= kSetSlots) break;
+        const int i = claimed + lane;
+        int k;
+        bool live = true;
+        if (i < e4) {
+          if (i < e0) {
+            k = L.ev[lr][i];
+            EventHinge(a, jobs, S, k);
+          } else if (i < e1) {
+            k = L.ev[lr][kSetSlots - 1 - (i - e0)];
+            EventMscEnd(a, et, jobs, S, k);
+          } else if (i < e2) {
+            k = L.ia[lr][i - e1];
+            live = EventBrem<AGG>(a, jobs, S, k, dacc);
+          } else if (i < e3) {
+            k = L.ia[lr][kSetSlots - 1 - (i - e2)];
+            EventMoller(a, et, jobs, S, k);
+          } else {
+            k = L.run[lr][i - e3];
+          }
         } else {
-          k = L.run[lr][i - e3];
+          k = L.run[lr][kSetSlots - 1 - (i - e4)];
+          live = false;
+          if (!exhausted) {
+            // one claim on the work counter per warp
+            cg::coalesced_group g = cg::coalesced_threads();
+            unsigned long long base = 0;
+            if (g.thread_rank() == 0) base = atomicAdd(a.head, (unsigned long long)g.size());
+            base = g.shfl(base, 0);
+            const unsigned long long item = base + g.thread_rank();
+            if (base + g.size() >= total) nw[kLExhausted] = 1;
+            if (item < total) live = RefillSlot(a, et, jobs, spre, S, k, item, esc);
+          }
         }
-      } else {
-        k = L.run[lr][kGroupSlots - 1 - (i - e4)];
-        live = false;
-        if (!exhausted) {
-          // one claim on the work counter per warp
-          cg::coalesced_group g = cg::coalesced_threads();
-          unsigned long long base = 0;
-          if (g.thread_rank() == 0) base = atomicAdd(a.head, (unsigned long long)g.size());
-          base = g.shfl(base, 0);
-          const unsigned long long item = base + g.thread_rank();
-          if (base + g.size() >= total) nw[kLExhausted] = 1;
-          if (item < total) live = RefillSlot(a, et, jobs, spre, S, k, item, esc);
+        const int code = live ? StepSlot<AGG>(a, et, jobs, S, k, esc, nsteps, dacc) : 5;
+        switch (code) {
+          case 0: Push(L.run[lw], &nw[kLStep], k, false); break;
+          case 1: Push(L.ia[lw], &nw[kLBrem], k, false); break;
+          case 2: Push(L.ia[lw], &nw[kLMoller], k, true); break;
+          case 3: Push(L.ev[lw], &nw[kLHinge], k, false); break;
+          case 4: Push(L.ev[lw], &nw[kLMscEnd], k, true); break;
+          default: Push(L.run[lw], &nw[kLIdle], k, true); break;
         }
       }
-      const int code = live ? StepSlot<AGG>(a, et, jobs, S, k, esc, nsteps, dacc) : 5;
-      switch (code) {
-        case 0: Push(L.run[lw], &nw[kLStep], k, false); break;
-        case 1: Push(L.ia[lw], &nw[kLBrem], k, false); break;
-        case 2: Push(L.ia[lw], &nw[kLMoller], k, true); break;
-        case 3: Push(L.ev[lw], &nw[kLHinge], k, false); break;
-        case 4: Push(L.ev[lw], &nw[kLMscEnd], k, true); break;
-        default: Push(L.run[lw], &nw[kLIdle], k, true); break;
-      }
+      if (kSets > 1) SetBarrierArrive(&setBar[st]);
+      else __syncthreads();
+      if (st) { cr1 = cw; ++it1; } else { cr0 = cw; ++it0; }
     }
-    GroupSync(grp);
-    cr = cw;
-    lr = lw;
   }
+  // a block that gave up a wait leaves its electrons unfinished: reported
+  if (gaveUp && lane == 0) atomicAdd(a.fault, 1ull);
   esc.Flush(jobs);
   DepthAccFlush(a, jobs, dacc);
   for (int o = 16; o > 0; o >>= 1) nsteps += __shfl_down_sync(kFull, nsteps, o);
