@@ -240,15 +240,19 @@ def main():
     value = world * H * a.steps / (ms_max * 1e-3)
 
     # e2e through the public API with host buffers: per step the phantom goes
-    # host->device from pinned memory and the dose + dose^2 come back
+    # host->device from pinned memory and the dose + dose^2 come back into
+    # pinned host arrays
     pinned = torch.from_numpy(mat.reshape(-1)).pin_memory().numpy().reshape(mat.shape)
+    nbins = int(mat.size)
+    out_d = torch.empty(nbins, dtype=torch.float64).pin_memory().numpy()
+    out_d2 = torch.empty(nbins, dtype=torch.float64).pin_memory().numpy()
     e2e_steps = max(1, min(3, a.steps))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for k in range(e2e_steps):
         p2 = dpm.Phantom.voxels(tables, pinned, 2.0)
         r = dpm.run(tables, [dpm.Job(p2, src, H, seed_of(100 + k))], batches=a.batches)
-        d, d2, _ = r.tally(0)
+        d, d2, _ = r.tally(0, out=(out_d, out_d2, None))
         r.close()
         p2.close()
     torch.cuda.synchronize()

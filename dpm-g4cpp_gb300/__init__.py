@@ -291,17 +291,28 @@ class Result:
         self._h = handle
         self._jobs = jobs
 
-    def tally(self, j=0):
-        """(dose, dose2, steps) of job j as numpy arrays shaped like the phantom tally."""
+    def tally(self, j=0, out=None):
+        """(dose, dose2, steps) of job j as numpy arrays shaped like the phantom tally.
+
+        out: optional (dose, dose2, steps) float64 arrays of tally_size elements
+        to copy into (for instance views of pinned host memory, which copy
+        faster); steps may be None."""
         ph = self._jobs[j].phantom
         n = ph.tally_size
-        d = np.zeros(n)
-        d2 = np.zeros(n)
-        s = np.zeros(n)
-        _check(library().dpmx_result_tally(self._h, j, d.ctypes.data, d2.ctypes.data, s.ctypes.data))
+        if out is None:
+            d, d2, s = np.zeros(n), np.zeros(n), np.zeros(n)
+        else:
+            d, d2, s = out
+            for x in (d, d2) + ((s,) if s is not None else ()):
+                if x.dtype != np.float64 or x.size != n or not x.flags["C_CONTIGUOUS"]:
+                    raise DpmxError(ERR_ARG, "tally output arrays must be contiguous float64 of tally_size")
+        _check(library().dpmx_result_tally(self._h, j, d.ctypes.data, d2.ctypes.data,
+                                           s.ctypes.data if s is not None else None))
+        if s is None:
+            s = np.zeros(0)
         shp = ph.shape
         if len(shp) == 3:
-            return d.reshape(shp), d2.reshape(shp), s.reshape(shp)
+            return d.reshape(shp), d2.reshape(shp), (s.reshape(shp) if s.size else s)
         return d, d2, s
 
     def tally_device_ptr(self, j=0):

@@ -27,6 +27,10 @@ int HistLen(int maxIz);
     }                                                                                          \
   } while (0)
 
+struct JobOut;
+// returns a job's device buffers (dose and dose^2 to the scratch pool, the rest freed)
+void ReleaseJobOut(JobOut& o);
+
 struct JobOut {
   long long tallySize = 0;
   int slab = 0;              // depth tally of a slab preset
@@ -49,12 +53,7 @@ struct dpmx_result {
   long long cfg[4] = {0, 0, 0, 0};
   double prof[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   ~dpmx_result() {
-    for (auto& j : jobs) {
-      cudaFree(j.d_dose);
-      cudaFree(j.d_dose2);
-      cudaFree(j.d_steps);
-      cudaFree(j.d_btally);
-    }
+    for (auto& j : jobs) dpmx::ReleaseJobOut(j);
   }
 };
 

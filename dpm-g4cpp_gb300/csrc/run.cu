@@ -584,10 +584,12 @@ int PrepareOutputs(const dpmx_job* jobs, int njobs, bool tag, std::vector<JobOut
     o.tallySize = ph->tallySize;
     o.slab = ph->kind == 0;
     o.nvox = (long long)ph->grid.nx * ph->grid.ny * ph->grid.nz;
-    CK(cudaMalloc(&o.d_dose, o.tallySize * sizeof(double)));
-    CK(cudaMalloc(&o.d_dose2, o.tallySize * sizeof(double)));
-    CK(cudaMemset(o.d_dose, 0, o.tallySize * sizeof(double)));
-    CK(cudaMemset(o.d_dose2, 0, o.tallySize * sizeof(double)));
+    // dose and dose^2 come from the scratch pool; every run writes them whole
+    void* p = nullptr;
+    CK(ScratchPool::Instance().Get(o.tallySize * sizeof(double), &p));
+    o.d_dose = static_cast<double*>(p);
+    CK(ScratchPool::Instance().Get(o.tallySize * sizeof(double), &p));
+    o.d_dose2 = static_cast<double*>(p);
     if (o.slab) {
       CK(cudaMalloc(&o.d_steps, o.tallySize * sizeof(double)));
       CK(cudaMemset(o.d_steps, 0, o.tallySize * sizeof(double)));
@@ -666,7 +668,7 @@ int Autotune(const dpmx_tables* t, const dpmx_job* jobs, int njobs, const Cfg ba
     double ms = 0;
     long long nl = 0;
     const int rc = RunFp32(t, sj.data(), njobs, 1, cfg, false, false, st, outs, &ms, &nl);
-    for (auto& o : outs) { cudaFree(o.d_dose); cudaFree(o.d_dose2); cudaFree(o.d_steps); cudaFree(o.d_btally); }
+    for (auto& o : outs) ReleaseJobOut(o);
     if (rc) return rc;
     if (ms < bestMs) { bestMs = ms; *best = cfg; }
   }
@@ -675,6 +677,18 @@ int Autotune(const dpmx_tables* t, const dpmx_job* jobs, int njobs, const Cfg ba
 }
 
 }  // namespace
+
+namespace dpmx {
+void ReleaseJobOut(JobOut& o) {
+  // nothing may still write the pooled buffers when they go back
+  cudaDeviceSynchronize();
+  if (o.d_dose) ScratchPool::Instance().Put(o.d_dose);
+  if (o.d_dose2) ScratchPool::Instance().Put(o.d_dose2);
+  cudaFree(o.d_steps);
+  cudaFree(o.d_btally);
+  o.d_dose = o.d_dose2 = o.d_steps = o.d_btally = nullptr;
+}
+}  // namespace dpmx
 
 // ===========================================================================
 // C ABI
@@ -890,7 +904,7 @@ int dpmx_simulate_histories(const dpmx_tables* t, int nprimary, double eprimary,
     }
   }
   cudaFree(d_he);
-  for (auto& o : outs) { cudaFree(o.d_dose); cudaFree(o.d_dose2); cudaFree(o.d_steps); cudaFree(o.d_btally); }
+  for (auto& o : outs) ReleaseJobOut(o);
   dpmx_phantom_free(ph);
   return rc;
 }
