@@ -17,6 +17,7 @@ transport runs on the GPU; importing the package without the built library
 raises at the first call.
 """
 import ctypes as C
+import math
 import os
 from dataclasses import dataclass, field
 
@@ -27,6 +28,9 @@ LIB_PATH = os.path.join(_HERE, "lib", "libdpmx.so")
 
 FP64_PLAIN = 0
 FP32_EVENT = 1
+DOSE_RAW = 0      # 3-D dose [Gy per history] + relative uncertainty (voxel phantoms)
+DOSE_DEPTH = 1    # hist.sim-format depth profile (any phantom)
+MODEL_BREM, MODEL_MOLLER, MODEL_MSC = 0, 1, 2
 
 OK, ERR_FILE, ERR_PARSE, ERR_CUDA, ERR_ARG, ERR_OVERFLOW, ERR_NOMEM = 0, -1, -2, -3, -4, -5, -6
 
@@ -99,6 +103,9 @@ def library():
         "dpmx_result_profile": (C.c_int, [P, C.POINTER(C.c_double)]),
         "dpmx_result_free": (None, [P]),
         "dpmx_scratch_release": (None, []),
+        "dpmx_result_write": (C.c_int, [P, C.c_int, C.c_char_p, C.c_int]),
+        "dpmx_model_histogram": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_double, C.c_longlong, C.c_uint64,
+                                           C.c_int, _dp, _dp]),
         "dpmx_simulate": (C.c_int, [P, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int, C.c_uint64, C.c_int,
                                     _dp, _dp, C.c_int, C.POINTER(C.c_int)]),
         "dpmx_write_hist": (C.c_int, [P, C.c_char_p, C.c_int, C.c_double, C.c_int, _dp, _dp, C.c_int]),
@@ -137,7 +144,7 @@ def exported_symbols():
             "dpmx_phantom_voxels", "dpmx_phantom_free", "dpmx_phantom_tally_size", "dpmx_run_options_default",
             "dpmx_run", "dpmx_result_tally", "dpmx_result_tally_device", "dpmx_result_stats",
             "dpmx_result_elapsed_ms", "dpmx_result_launches", "dpmx_result_config", "dpmx_result_profile",
-            "dpmx_result_free", "dpmx_scratch_release",
+            "dpmx_result_free", "dpmx_scratch_release", "dpmx_result_write", "dpmx_model_histogram",
             "dpmx_simulate", "dpmx_simulate_noalloc", "dpmx_write_hist", "dpmx_sampler_eval", "dpmx_table_eval", "dpmx_simulate_histories",
             "dpmx_influence_build", "dpmx_csr_shape", "dpmx_csr_device", "dpmx_csr_spmv", "dpmx_csr_spmv_t",
             "dpmx_csr_download", "dpmx_csr_free"]
@@ -195,6 +202,17 @@ class Tables:
         out = np.zeros_like(e)
         _check(library().dpmx_sampler_eval(self._h, precision, sampler, imat, e, r, out, len(e)))
         return out
+
+    def model_histogram(self, model, e0, n, imat=0, seed=1, hbins=101, precision=FP64_PLAIN):
+        """(x, hist_x, cos, hist_cos): the reference's model-validation histograms
+        (testAPI) of n interactions sampled on the GPU; counts, not normalised."""
+        hx = np.zeros(hbins)
+        hc = np.zeros(hbins)
+        _check(library().dpmx_model_histogram(self._h, precision, model, imat, float(e0), int(n), int(seed), hbins,
+                                              hx, hc))
+        xmin = math.log10(self.gamma_cut / e0)
+        hdel = (0.1 - xmin) / (hbins - 1)
+        return xmin + (np.arange(hbins) + 0.5) * hdel, hx, -1.0 + np.arange(hbins) * 2.0 / (hbins - 1), hc
 
     def eval_table(self, quantity, energies, imat=0, precision=FP64_PLAIN):
         e = np.ascontiguousarray(energies, dtype=np.float64)
@@ -315,6 +333,10 @@ class Result:
             return d.reshape(shp), d2.reshape(shp), (s.reshape(shp) if s.size else s)
         return d, d2, s
 
+    def write(self, path, j=0, fmt=DOSE_DEPTH):
+        """Writes job j's dose: DOSE_RAW (binary, see read_dose_raw) or DOSE_DEPTH (hist.sim text)."""
+        _check(library().dpmx_result_write(self._h, j, str(path).encode(), fmt))
+
     def tally_device_ptr(self, j=0):
         return library().dpmx_result_tally_device(self._h, j)
 
@@ -364,6 +386,25 @@ class Result:
             self.close()
         except Exception:
             pass
+
+
+def read_dose_raw(path):
+    """Reads a DOSE_RAW file: (dose [Gy per history], relative 1-sigma
+    uncertainty, header dict), arrays shaped (nz, ny, nx)."""
+    with open(path, "rb") as f:
+        if f.read(8) != b"DPMXDOSE":
+            raise DpmxError(ERR_PARSE, "%s is not a raw dose file" % path)
+        version, nx, ny, nz = np.frombuffer(f.read(16), dtype="<i4")
+        if version != 1:
+            raise DpmxError(ERR_PARSE, "raw dose version %d not supported" % version)
+        vx, vy, vz, x0, y0, z0 = np.frombuffer(f.read(48), dtype="<f8")
+        hist, batches = np.frombuffer(f.read(16), dtype="<i8")
+        n = int(nx) * int(ny) * int(nz)
+        dose = np.frombuffer(f.read(8 * n), dtype="<f8").reshape(nz, ny, nx)
+        rel = np.frombuffer(f.read(8 * n), dtype="<f8").reshape(nz, ny, nx)
+    head = dict(nx=int(nx), ny=int(ny), nz=int(nz), voxel_mm=(vx, vy, vz), origin_mm=(x0, y0, z0),
+                histories=int(hist), batches=int(batches))
+    return dose, rel, head
 
 
 def scratch_release():

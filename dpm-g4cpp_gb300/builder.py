@@ -35,6 +35,7 @@ CU_UNITS = {
     "run.cu": [],
     "influence.cu": [],
     "noalloc.cu": [],
+    "validation.cu": [],
 }
 CXX_UNITS = ["host_tables.cpp"]
 

@@ -291,6 +291,8 @@ int dpmx_phantom_slab(const dpmx_tables* t, int geom_index, double lbox, dpmx_ph
   for (int iz = 0; iz < nz; ++iz)
     if (SlabMaterialAt(geom_index, invL, iz) >= t->h.nmat)
       return Fail(DPMX_ERR_ARG, "the data set has fewer materials than the slab geometry needs");
+  auto rho = std::make_shared<std::vector<float>>(size_t(nz) + 16, 0.0f);
+  for (int iz = 0; iz < nz + 16; ++iz) (*rho)[iz] = float(SlabDensityAt(t, geom_index, invL, iz));
   std::unique_ptr<dpmx_phantom> p(new dpmx_phantom());
   p->tables = t;
   p->kind = 0;
@@ -310,6 +312,7 @@ int dpmx_phantom_slab(const dpmx_tables* t, int geom_index, double lbox, dpmx_ph
   g.tallyDepth = 1;
   g.matByDepth = 1;
   p->tallySize = nz + 16;
+  p->binDensity = rho;
   *out = p.release();
   return DPMX_OK;
 }
@@ -323,6 +326,10 @@ int dpmx_phantom_voxels(const dpmx_tables* t, int nx, int ny, int nz, double vx,
   const size_t n = size_t(nx) * ny * nz;
   for (size_t i = 0; i < n; ++i)
     if (mat[i] != kVacuum && mat[i] >= t->h.nmat) return Fail(DPMX_ERR_ARG, "material id beyond the data set");
+  float lut[256] = {0.0f};
+  for (int m = 0; m < t->h.nmat; ++m) lut[m] = float(t->h.density[m]);
+  auto rho = std::make_shared<std::vector<float>>(n);
+  for (size_t i = 0; i < n; ++i) (*rho)[i] = lut[mat[i]];
   std::unique_ptr<dpmx_phantom> p(new dpmx_phantom());
   p->tables = t;
   p->kind = 1;
@@ -338,6 +345,7 @@ int dpmx_phantom_voxels(const dpmx_tables* t, int nx, int ny, int nz, double vx,
   g.tallyDepth = 0;
   g.matByDepth = 0;
   p->tallySize = (long long)n;
+  p->binDensity = rho;
   *out = p.release();
   return DPMX_OK;
 }

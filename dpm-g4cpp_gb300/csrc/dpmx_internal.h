@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -144,4 +145,7 @@ struct dpmx_phantom {
   dpmx::GridGeom grid{};    // voxel box (slab presets are materialised too)
   uint8_t* d_mat = nullptr;
   long long tallySize = 0;
+  // host copies for the dose outputs: density of every tally bin [g/cm3]
+  // (0 for vacuum), shared with the results that outlive the phantom
+  std::shared_ptr<const std::vector<float>> binDensity;
 };

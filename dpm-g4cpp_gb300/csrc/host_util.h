@@ -42,6 +42,9 @@ struct JobOut {
   long long nvox = 0;
   int maxIz = 0;
   RunCounters cnt{};
+  GridGeom grid{};                                      // for the dose outputs
+  double lbox = 1.0;
+  std::shared_ptr<const std::vector<float>> binDensity;
 };
 
 }  // namespace dpmx
@@ -51,6 +54,7 @@ struct dpmx_result {
   double ms = 0.0;
   long long launches = 0;
   long long cfg[4] = {0, 0, 0, 0};
+  int batches = 1;
   double prof[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   ~dpmx_result() {
     for (auto& j : jobs) dpmx::ReleaseJobOut(j);

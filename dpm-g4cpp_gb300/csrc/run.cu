@@ -584,6 +584,9 @@ int PrepareOutputs(const dpmx_job* jobs, int njobs, bool tag, std::vector<JobOut
     o.tallySize = ph->tallySize;
     o.slab = ph->kind == 0;
     o.nvox = (long long)ph->grid.nx * ph->grid.ny * ph->grid.nz;
+    o.grid = ph->grid;
+    o.lbox = ph->lbox;
+    o.binDensity = ph->binDensity;
     // dose and dose^2 come from the scratch pool; every run writes them whole
     void* p = nullptr;
     CK(ScratchPool::Instance().Get(o.tallySize * sizeof(double), &p));
@@ -707,6 +710,7 @@ int dpmx_run(const dpmx_tables* t, const dpmx_job* jobs, int njobs, const dpmx_r
   bool ownStream = false;
   if (!st) { CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)); ownStream = true; }
   std::unique_ptr<dpmx_result> r(new dpmx_result());
+  r->batches = o.batches;
   const bool tag = o.tag_beamlets && o.precision == DPMX_FP32_EVENT;
   int rc = PrepareOutputs(jobs, njobs, tag, r->jobs);
   if (!rc) {
@@ -781,6 +785,81 @@ int dpmx_result_profile(const dpmx_result* r, double* out10) {
 void dpmx_result_free(dpmx_result* r) { delete r; }
 
 void dpmx_scratch_release(void) { ScratchPool::Instance().Release(-1); }
+
+int dpmx_result_write(const dpmx_result* r, int job, const char* path, int format) {
+  if (!r || !path || job < 0 || job >= int(r->jobs.size())) return Fail(DPMX_ERR_ARG, "bad result, job or path");
+  if (format != DPMX_DOSE_RAW && format != DPMX_DOSE_DEPTH) return Fail(DPMX_ERR_ARG, "unknown dose format");
+  const JobOut& o = r->jobs[job];
+  if (format == DPMX_DOSE_RAW && o.slab) return Fail(DPMX_ERR_ARG, "raw 3-D output needs a voxel phantom");
+  const long long n = o.tallySize;
+  std::vector<double> d(n), d2(n), st;
+  CK(cudaMemcpy(d.data(), o.d_dose, n * sizeof(double), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(d2.data(), o.d_dose2, n * sizeof(double), cudaMemcpyDeviceToHost));
+  if (o.slab && o.d_steps) {
+    st.resize(n);
+    CK(cudaMemcpy(st.data(), o.d_steps, n * sizeof(double), cudaMemcpyDeviceToHost));
+  }
+  const double hist = double(o.cnt.histories);
+  if (!(hist > 0)) return Fail(DPMX_ERR_ARG, "the job ran no histories");
+  const std::vector<float>& rho = *o.binDensity;
+  FILE* f = std::fopen(path, format == DPMX_DOSE_RAW ? "wb" : "w");
+  if (!f) return Fail(DPMX_ERR_FILE, std::string("file ") + path + " could not be created");
+  bool ok = true;
+  if (format == DPMX_DOSE_RAW) {
+    // header, then dose [Gy per history] and its relative 1-sigma uncertainty
+    // (from the statistical batches) per voxel, x fastest
+    const GridGeom& g = o.grid;
+    const char magic[8] = {'D', 'P', 'M', 'X', 'D', 'O', 'S', 'E'};
+    const int32_t head[4] = {1, g.nx, g.ny, g.nz};
+    const double geo[6] = {g.vx, g.vy, g.vz, g.x0, g.y0, g.z0};
+    const int64_t hb[2] = {int64_t(o.cnt.histories), int64_t(r->batches)};
+    ok = std::fwrite(magic, 1, 8, f) == 8 && std::fwrite(head, 4, 4, f) == 4 && std::fwrite(geo, 8, 6, f) == 6 &&
+         std::fwrite(hb, 8, 2, f) == 2;
+    const double mevToJ = 1.602176634e-13, volCm3 = g.vx * g.vy * g.vz * 1.0e-3;
+    const int B = r->batches;
+    std::vector<double> dose(n), rel(n);
+    for (long long i = 0; i < n; ++i) {
+      const double massKg = double(rho[i]) * volCm3 * 1.0e-3;
+      dose[i] = massKg > 0.0 ? d[i] * mevToJ / massKg / hist : 0.0;
+      // batch sums t_b: sum_b t_b = d, sum_b t_b^2 = d2; error of the mean of B batches
+      const double var = B > 1 ? std::max(0.0, (d2[i] - d[i] * d[i] / B) / (B - 1)) * B : 0.0;
+      rel[i] = d[i] > 0.0 ? std::sqrt(var) / d[i] : 0.0;
+    }
+    ok = ok && std::fwrite(dose.data(), 8, n, f) == size_t(n) && std::fwrite(rel.data(), 8, n, f) == size_t(n);
+  } else {
+    // Geom::Write's columns (Geom.cc:167-192) for any phantom: the energy of a
+    // depth slice per primary over the slice's mean density times its
+    // thickness [MeV cm2/g], and the scoring steps per primary (slab presets)
+    const GridGeom& g = o.grid;
+    const int nz = o.slab ? int(n) : g.nz;
+    const double dz = o.slab ? o.lbox : g.vz;
+    std::vector<double> ez(nz, 0.0), rz(nz, 0.0), sz(nz, 0.0);
+    if (o.slab) {
+      for (int i = 0; i < nz; ++i) { ez[i] = d[i]; rz[i] = rho[i]; sz[i] = st.empty() ? 0.0 : st[i]; }
+    } else {
+      const long long plane = (long long)g.nx * g.ny;
+      for (int iz = 0; iz < nz; ++iz) {
+        double e = 0.0, r0 = 0.0;
+        for (long long k = 0; k < plane; ++k) { e += d[iz * plane + k]; r0 += rho[iz * plane + k]; }
+        ez[iz] = e;
+        rz[iz] = r0 / double(plane);
+      }
+    }
+    int len = nz;
+    if (o.slab) len = std::min(nz, HistLen(o.maxIz));
+    double sum = 0.0;
+    for (int i = 0; i < nz; ++i) sum += ez[i];
+    std::fprintf(f, "# === Mean energy deposit in the target: %13.4e  [MeV/event]\n", sum / hist);
+    std::fprintf(f, "# === Energy deposit as a function of the depth: \n");
+    std::fprintf(f, "# === Index       Depth [cm]    Edep [MeV cm2/g]  #Simulation-Steps \n");
+    const double norm = 1.0 / (hist * dz * 0.1);
+    for (int i = 0; i < len; ++i)
+      std::fprintf(f, " %10d    %13.4e    %13.4e    %13.4e\n", i, (i + 0.5) * dz * 0.1,
+                   rz[i] > 0.0 ? ez[i] * norm / rz[i] : 0.0, sz[i] / hist);
+  }
+  ok = (std::fclose(f) == 0) && ok;
+  return ok ? DPMX_OK : Fail(DPMX_ERR_FILE, std::string("writing ") + path + " failed");
+}
 
 int dpmx_simulate(const dpmx_tables* t, int nprimary, double eprimary, int iselectron, double lbox, int geom_index,
                   uint64_t seed, int precision, double* edep_hist, double* step_hist, int cap, int* hist_len) {

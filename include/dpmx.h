@@ -153,6 +153,18 @@ int dpmx_result_config(const dpmx_result* r, long long* cfg4);
  * transported, histories, total ms */
 int dpmx_result_profile(const dpmx_result* r, double* out10);
 void dpmx_result_free(dpmx_result* r);
+/* dose outputs of a job:
+ *  DPMX_DOSE_RAW   voxel phantoms: "DPMXDOSE", int32 {version 1, nx, ny, nz},
+ *                  float64 {vx, vy, vz, x0, y0, z0} [mm], int64 {histories,
+ *                  batches}, then float64 dose [Gy per history] and float64
+ *                  relative 1-sigma uncertainty per voxel (x fastest)
+ *  DPMX_DOSE_DEPTH the hist.sim text of Geom::Write (Geom.cc:167-192) for any
+ *                  phantom: per depth slice the energy per primary over the
+ *                  slice's mean density and thickness [MeV cm2/g], and the
+ *                  scoring steps per primary (slab presets; 0 for voxels) */
+#define DPMX_DOSE_RAW 0
+#define DPMX_DOSE_DEPTH 1
+int dpmx_result_write(const dpmx_result* r, int job, const char* path, int format);
 /* Runs keep their device scratch (particle queues, batch tallies) in a pool
  * for later runs on the same device; this frees the blocks no run is using. */
 void dpmx_scratch_release(void);
@@ -196,6 +208,19 @@ int dpmx_table_eval(const dpmx_tables* t, int precision, int quantity, int imat,
  * histogram; history h uses the per-history random stream with index h */
 int dpmx_simulate_histories(const dpmx_tables* t, int nprimary, double eprimary, int iselectron, double lbox,
                             int geom_index, uint64_t seed, double* hist_edep, double* edep_hist, int cap);
+
+/* ---- model validation (the reference's modelValidationTests, testAPI.cc) ---- */
+#define DPMX_MODEL_BREM 0
+#define DPMX_MODEL_MOLLER 1
+#define DPMX_MODEL_MSC 2
+/* n interactions of `model` for a primary of energy e0 [MeV] along +z in
+ * material imat, sampled on the GPU (a Philox stream per sample, key `seed`),
+ * histogrammed as testAPI does: hist_x[hbins] counts x = log10(k/e0) on
+ * [log10(gamma cut/e0), 0.1] (hbins - 1 intervals; k the secondary's energy,
+ * the primary's for MSC), hist_cos[hbins] counts the direction cosine of the
+ * secondary (the primary for MSC) in bin (int)(cost*(hbins/2) + hbins/2) */
+int dpmx_model_histogram(const dpmx_tables* t, int precision, int model, int imat, double e0, long long n,
+                         uint64_t seed, int hbins, double* hist_x, double* hist_cos);
 
 /* ---- influence matrix (beamlet-tagged run with tag_beamlets = 1) ---- */
 /* builds A (rows: voxels, cols: beamlets, FP32 values from the FP64 tally,
