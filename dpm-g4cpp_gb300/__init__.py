@@ -90,6 +90,10 @@ def library():
         "dpmx_phantom_slab": (C.c_int, [P, C.c_int, C.c_double, C.POINTER(P)]),
         "dpmx_phantom_voxels": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                                           np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS"), C.POINTER(P)]),
+        "dpmx_phantom_voxels_density": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                                  np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS"),
+                                                  np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS"),
+                                                  C.POINTER(P)]),
         "dpmx_phantom_free": (None, [P]),
         "dpmx_phantom_tally_size": (C.c_longlong, [P]),
         "dpmx_run_options_default": (None, [C.POINTER(_Opts)]),
@@ -141,7 +145,7 @@ def exported_symbols():
     """Names the C ABI exports (declared in include/dpmx.h)."""
     return ["dpmx_last_error", "dpmx_version", "dpmx_tables_load", "dpmx_tables_free", "dpmx_tables_num_materials",
             "dpmx_tables_param", "dpmx_tables_density", "dpmx_tables_material_name", "dpmx_phantom_slab",
-            "dpmx_phantom_voxels", "dpmx_phantom_free", "dpmx_phantom_tally_size", "dpmx_run_options_default",
+            "dpmx_phantom_voxels", "dpmx_phantom_voxels_density", "dpmx_phantom_free", "dpmx_phantom_tally_size", "dpmx_run_options_default",
             "dpmx_run", "dpmx_result_tally", "dpmx_result_tally_device", "dpmx_result_stats",
             "dpmx_result_elapsed_ms", "dpmx_result_launches", "dpmx_result_config", "dpmx_result_profile",
             "dpmx_result_free", "dpmx_scratch_release", "dpmx_result_write", "dpmx_model_histogram",
@@ -234,14 +238,23 @@ class Phantom:
         return cls(tables, h, (library().dpmx_phantom_tally_size(h),))
 
     @classmethod
-    def voxels(cls, tables, mat, voxel_size):
-        """mat: uint8 array of shape (nz, ny, nx) (x fastest), 255 = vacuum; voxel_size mm (scalar or 3)."""
+    def voxels(cls, tables, mat, voxel_size, density=None):
+        """mat: uint8 array of shape (nz, ny, nx) (x fastest), 255 = vacuum; voxel_size mm (scalar or 3);
+        density: optional float32 array like mat [g/cm3] (per-voxel density; the material id keeps
+        the composition)."""
         m = np.ascontiguousarray(mat, dtype=np.uint8)
         nz, ny, nx = m.shape
         v = np.broadcast_to(np.asarray(voxel_size, dtype=np.float64), (3,))
         h = C.c_void_p()
-        _check(library().dpmx_phantom_voxels(tables.handle, nx, ny, nz, float(v[0]), float(v[1]), float(v[2]),
-                                              m.reshape(-1), C.byref(h)))
+        if density is None:
+            _check(library().dpmx_phantom_voxels(tables.handle, nx, ny, nz, float(v[0]), float(v[1]), float(v[2]),
+                                                  m.reshape(-1), C.byref(h)))
+        else:
+            r = np.ascontiguousarray(density, dtype=np.float32)
+            if r.shape != m.shape:
+                raise DpmxError(ERR_ARG, "density must have the shape of mat")
+            _check(library().dpmx_phantom_voxels_density(tables.handle, nx, ny, nz, float(v[0]), float(v[1]),
+                                                          float(v[2]), m.reshape(-1), r.reshape(-1), C.byref(h)))
         return cls(tables, h, (nz, ny, nx))
 
     @property

@@ -311,6 +311,8 @@ int dpmx_phantom_slab(const dpmx_tables* t, int geom_index, double lbox, dpmx_ph
   g.mat = p->d_mat;
   g.tallyDepth = 1;
   g.matByDepth = 1;
+  g.rho = nullptr;
+  g.wscale = 1.0;
   p->tallySize = nz + 16;
   p->binDensity = rho;
   *out = p.release();
@@ -344,15 +346,45 @@ int dpmx_phantom_voxels(const dpmx_tables* t, int nx, int ny, int nz, double vx,
   g.mat = p->d_mat;
   g.tallyDepth = 0;
   g.matByDepth = 0;
+  g.rho = nullptr;
+  g.wscale = 1.0;
   p->tallySize = (long long)n;
   p->binDensity = rho;
   *out = p.release();
   return DPMX_OK;
 }
 
+int dpmx_phantom_voxels_density(const dpmx_tables* t, int nx, int ny, int nz, double vx, double vy, double vz,
+                                const uint8_t* mat, const float* density, dpmx_phantom** out) {
+  if (!density) return Fail(DPMX_ERR_ARG, "null density array");
+  dpmx_phantom* p = nullptr;
+  if (int rc = dpmx_phantom_voxels(t, nx, ny, nz, vx, vy, vz, mat, &p)) return rc;
+  std::unique_ptr<dpmx_phantom, void (*)(dpmx_phantom*)> guard(p, dpmx_phantom_free);
+  const size_t n = size_t(nx) * ny * nz;
+  // the Woodcock majorant of the photon tables holds for the nominal
+  // densities; denser voxels scale it (SimDPMLike.cc:471-474 uses it as is)
+  double ws = 1.0;
+  auto rho = std::make_shared<std::vector<float>>(n);
+  for (size_t i = 0; i < n; ++i) {
+    if (mat[i] == kVacuum) { (*rho)[i] = 0.0f; continue; }
+    const float r = density[i];
+    if (!(r > 0.0f) || !(r < 1.0e4f)) return Fail(DPMX_ERR_ARG, "voxel densities must be positive and finite");
+    (*rho)[i] = r;
+    ws = std::max(ws, double(r) / t->h.density[mat[i]]);
+  }
+  CK(cudaMalloc(&p->d_rho, n * sizeof(float)));
+  CK(cudaMemcpy(p->d_rho, rho->data(), n * sizeof(float), cudaMemcpyHostToDevice));
+  p->grid.rho = p->d_rho;
+  p->grid.wscale = ws;
+  p->binDensity = rho;
+  *out = guard.release();
+  return DPMX_OK;
+}
+
 void dpmx_phantom_free(dpmx_phantom* p) {
   if (!p) return;
   cudaFree(p->d_mat);
+  cudaFree(p->d_rho);
   delete p;
 }
 

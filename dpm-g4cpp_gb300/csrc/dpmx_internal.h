@@ -112,6 +112,8 @@ struct GridGeom {          // voxel box; world = the box
   const uint8_t* mat;      // nx*ny*nz material ids (kVacuum outside any material)
   int tallyDepth;          // 1: tally by iz only (slab workload), 0: 3-D
   int matByDepth;          // 1: mat has nz entries, indexed by iz (slab presets)
+  const float* rho;        // per-voxel density [g/cm3] or null (the material's nominal density)
+  double wscale;           // >= 1: max over voxels of density / nominal density (Woodcock majorant)
 };
 
 struct SlabGeomD {         // the reference's pre-defined slab geometry (Geom.cc)
@@ -144,6 +146,7 @@ struct dpmx_phantom {
   double lbox = 1.0;
   dpmx::GridGeom grid{};    // voxel box (slab presets are materialised too)
   uint8_t* d_mat = nullptr;
+  float* d_rho = nullptr;   // per-voxel densities (dpmx_phantom_voxels_density) or null
   long long tallySize = 0;
   // host copies for the dose outputs: density of every tally bin [g/cm3]
   // (0 for vacuum), shared with the results that outlive the phantom

@@ -78,6 +78,8 @@ struct JobF {                  // per-job geometry, source and tally (device vie
   uint32_t k0, k1;             // Philox key (job seed)
   RunCounters* cnt;
   int dbase;                   // first bin of this job in a block's shared depth tally, or -1
+  const float* rho;            // per-voxel density [g/cm3] or null
+  float wscale;                // Woodcock majorant scale (>= 1)
 };
 
 struct Segment {               // a run of primaries of one job inside a chunk

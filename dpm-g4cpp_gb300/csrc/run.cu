@@ -240,6 +240,8 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
     J.ivx = float(1.0 / g.vx); J.ivy = float(1.0 / g.vy); J.ivz = float(1.0 / g.vz);
     J.x0 = g.x0; J.y0 = g.y0; J.z0 = g.z0;
     J.mat = g.mat;
+    J.rho = g.rho;
+    J.wscale = float(g.wscale);
     J.tally = tB + off[j] * binStride;
     J.tstride = binStride;
     J.steps = outs[j].d_steps;

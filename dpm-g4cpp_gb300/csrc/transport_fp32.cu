@@ -276,6 +276,11 @@ __device__ __forceinline__ void DepthAccFlush(const PhaseArgs& a, const JobF* jo
   }
 }
 
+// density of voxel (ix, iy, iz) of material im (Geom::GetVoxelMaterialDensity)
+__device__ __forceinline__ float VoxelRho(const JobF& J, const DevTables<float>& T, int ix, int iy, int iz, int im) {
+  return J.rho ? __ldg(J.rho + ((long long)iz * J.ny + iy) * J.nx + ix) : T.density[im];
+}
+
 __device__ __forceinline__ bool InBox(const JobF& J, int ix, int iy, int iz) {
   return (unsigned)ix < (unsigned)J.nx && (unsigned)iy < (unsigned)J.ny && (unsigned)iz < (unsigned)J.nz;
 }
@@ -526,7 +531,7 @@ __global__ void __launch_bounds__(256) PhotonPhase(PhaseArgs a) {
       continue;
     }
     ++nph;
-    const float lmax = 1.0f / LinearGet(pt.imfpMax, p.e);
+    const float lmax = 1.0f / (LinearGet(pt.imfpMax, p.e) * J.wscale);
     const float step = -lmax * __logf(rng.U());
     int im = -1;
     if (Fly(J, p, step)) im = MaterialAt(J, p.ix, p.iy, p.iz);
@@ -535,7 +540,7 @@ __global__ void __launch_bounds__(256) PhotonPhase(PhaseArgs a) {
       esc.Add(jobs, job, double(p.e));
       done = true;
     } else {
-      const float rho = T.density[im];
+      const float rho = VoxelRho(J, T, p.ix, p.iy, p.iz, im);
       const float r1 = rng.U();
       float prob = 1.0f - LinearGet(pt.tot[im], p.e) * rho * lmax;
       if (r1 >= prob) {
@@ -745,7 +750,7 @@ __global__ void __launch_bounds__(256) ElectronPhase(PhaseArgs a) {
       done = true;
     } else {
       ++nsteps;
-      const float rho = T.density[im];
+      const float rho = VoxelRho(J, T, p.ix, p.iy, p.iz, im);
       float step = s.sGeom;
       int what = 0;
       const float le = __logf(p.e);
@@ -1139,7 +1144,7 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
   } else {
     ++nsteps;
     const float ecut = T.ecut;
-    const float rho = T.density[im];
+    const float rho = VoxelRho(J, T, p.ix, p.iy, p.iz, im);
     float step = s.sGeom;
     int what = 0;
     const float le = __logf(p.e);

@@ -64,6 +64,8 @@ struct SlabGeo {
     }
   }
   __device__ double Density(int im) const { return im > -1 ? density[im] : 1.0E-40; }
+  __device__ double DensityAt(const int*, int im) const { return Density(im); }
+  __device__ double Wscale() const { return 1.0; }
   __device__ void Score(double e, const int* i) const {
     const int iz = i[2];
     if (iz >= 0 && iz < cap) {
@@ -118,6 +120,12 @@ struct GridGeo {
     return m == kVacuum ? -1 : int(m);
   }
   __device__ double Density(int im) const { return im > -1 ? density[im] : 1.0E-40; }
+  // Geom::GetVoxelMaterialDensity(iVoxel) (Geom.hh:89-92) with per-voxel densities
+  __device__ double DensityAt(const int* i, int im) const {
+    if (g.rho && im > -1) return double(g.rho[(size_t(i[2]) * g.ny + i[1]) * g.nx + i[0]]);
+    return Density(im);
+  }
+  __device__ double Wscale() const { return g.wscale; }
   __device__ void Score(double e, const int* i) const {
     if (Inside(i)) atomicAdd(tally + (size_t(i[2]) * g.ny + i[1]) * g.nx + i[0], e);
   }
@@ -227,7 +235,7 @@ struct HistorySim {
       t.mat = im;
       ++steps;
       const double scal = T.mollerScale[im];
-      const double rho = geom.Density(im);
+      const double rho = geom.DensityAt(t.box, im);
       double dedx = SplineGet(T.dedx[im], t.ekin) * rho;
       double emid = fmax(t.ekin - 0.5 * step * dedx, T.ecut);
       double dTr1 = SplineGet(T.itr1[im], emid) * rho;
@@ -285,14 +293,14 @@ struct HistorySim {
     const double kPI = 3.1415926535897932, kEMC2 = 0.510991, kInvEMC2 = 1.0 / kEMC2;
     for (int guard = 0; t.ekin > 0.0; ++guard) {
       if (guard > 1000000) { ++lost; escaped += t.ekin; t.ekin = 0.0; return; }
-      const double lmax = 1.0 / LinearGet(T.imfpMax, t.ekin);
+      const double lmax = 1.0 / (LinearGet(T.imfpMax, t.ekin) * geom.Wscale());
       const double step = -lmax * log(rng.U());
       t.pos[0] += t.dir[0] * step; t.pos[1] += t.dir[1] * step; t.pos[2] += t.dir[2] * step;
       if (geom.DistanceToBoundary(t.pos, t.dir, t.box) < 0) { Escape(t); t.ekin = 0.0; return; }
       const int im = geom.MaterialIndex(t.box);
       if (im < 0) { Escape(t); t.ekin = 0.0; return; }
       t.mat = im;
-      const double rho = geom.Density(im);
+      const double rho = geom.DensityAt(t.box, im);
       const double tot = LinearGet(T.tot[im], t.ekin) * rho;
       const double r1 = rng.U();
       double prob = 1.0 - tot * lmax;

@@ -77,6 +77,12 @@ int dpmx_phantom_slab(const dpmx_tables* t, int geom_index, double lbox_mm, dpmx
  * x in [-nx*vx/2, nx*vx/2], y likewise, z in [0, nz*vz]; 3-D tally */
 int dpmx_phantom_voxels(const dpmx_tables* t, int nx, int ny, int nz, double vx, double vy, double vz,
                         const uint8_t* mat, dpmx_phantom** out);
+/* the same with a density per voxel [g/cm3] (the material id keeps the
+ * composition): Geom::GetVoxelMaterialDensity(iVoxel) (Geom.hh:75-92) as the
+ * reference designed it for fractional densities; the photon majorant is
+ * scaled by the largest density / nominal density ratio */
+int dpmx_phantom_voxels_density(const dpmx_tables* t, int nx, int ny, int nz, double vx, double vy, double vz,
+                                const uint8_t* mat, const float* density, dpmx_phantom** out);
 void dpmx_phantom_free(dpmx_phantom* p);
 /* number of tally bins of a phantom (slab: depth bins; voxels: nx*ny*nz) */
 long long dpmx_phantom_tally_size(const dpmx_phantom* p);

@@ -60,7 +60,7 @@ def lib():
                                             np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS"), C.c_int, C.c_int,
                                             C.c_double, C.c_double, C.c_int, C.c_double, C.c_double, C.c_double,
                                             C.c_double, C.c_int, C.c_int, C.c_longlong, C.c_longlong, C.c_uint64, _dp,
-                                            _dp, _dp]
+                                            _dp, _dp, C.c_void_p]
         _lib = L
     return _lib
 
@@ -108,10 +108,12 @@ class Oracle:
                                               ed, st, cap, he, stats)
         return ed[:m], st[:m], he[:n], stats
 
-    def simulate_voxel(self, mat, voxel_size, source, nhist, seed, first=0):
-        """Voxel phantom (nz, ny, nx) uint8 with a source (dict like the product's
-        Source); returns (dose[nz,ny,nx], per-history energy, stats)."""
+    def simulate_voxel(self, mat, voxel_size, source, nhist, seed, first=0, density=None):
+        """Voxel phantom (nz, ny, nx) uint8 (optionally with float32 densities
+        per voxel) with a source (dict like the product's Source); returns
+        (dose[nz,ny,nx], per-history energy, stats)."""
         m = np.ascontiguousarray(mat, dtype=np.uint8)
+        rho = None if density is None else np.ascontiguousarray(density, dtype=np.float32).reshape(-1)
         nz, ny, nx = m.shape
         v = np.broadcast_to(np.asarray(voxel_size, dtype=np.float64), (3,))
         dose = np.zeros(m.size)
@@ -120,7 +122,8 @@ class Oracle:
         s = source
         lib().oracle_simulate_voxel(self._h, nx, ny, nz, float(v[0]), float(v[1]), float(v[2]), m.reshape(-1),
                                     s["particle"], s["spectrum"], s["e0"], s["e1"], s["shape"], s["cx"], s["cy"],
-                                    s["fx"], s["fy"], s["nbx"], s["nby"], first, nhist, seed, dose, he, stats)
+                                    s["fx"], s["fy"], s["nbx"], s["nby"], first, nhist, seed, dose, he, stats,
+                                    None if rho is None else rho.ctypes.data)
         return dose.reshape(nz, ny, nx), he[:nhist], stats
 
 

@@ -541,6 +541,8 @@ struct SlabGeom {
     }
   }
   double Density(int imat) const { return imat > -1 ? T->density[imat] : 1.0E-40; }
+  double DensityAt(const int*, int imat) const { return Density(imat); }
+  double Wscale() const { return 1.0; }
   void Score(double e, const int* i) {
     const int iz = i[2];
     if (iz >= 0) {
@@ -563,6 +565,8 @@ struct VoxelGeom {
   const Tables* T;
   double* dose;      // [nvox] energy deposit
   double* tag;       // optional per-history accumulator (energy check)
+  const float* rho = nullptr;   // per-voxel density or null
+  double wscale = 1.0;          // Woodcock majorant scale for densities above nominal
   static constexpr double kTol = 1.0E-4;
   double DistanceToBoundary(double* r, const double* v, int* i) const {
     const double kHalfTol = 0.5 * kTol;
@@ -594,11 +598,20 @@ struct VoxelGeom {
     }
   }
   bool Inside(const int* i) const { return i[0] >= 0 && i[0] < nx && i[1] >= 0 && i[1] < ny && i[2] >= 0 && i[2] < nz; }
+  // material 255 is vacuum: index -1 (SimDPMLike.cc:88-93)
   int MaterialIndex(const int* i) const {
     if (!Inside(i)) return -1;
-    return mat[(size_t(i[2]) * ny + i[1]) * nx + i[0]];
+    const uint8_t m = mat[(size_t(i[2]) * ny + i[1]) * nx + i[0]];
+    return m == 255 ? -1 : int(m);
   }
   double Density(int imat) const { return imat > -1 ? T->density[imat] : 1.0E-40; }
+  // Geom::GetVoxelMaterialDensity(iVoxel) (Geom.hh:89-92), with per-voxel
+  // densities when given
+  double DensityAt(const int* i, int imat) const {
+    if (rho && imat > -1) return double(rho[(size_t(i[2]) * ny + i[1]) * nx + i[0]]);
+    return Density(imat);
+  }
+  double Wscale() const { return wscale; }
   void Score(double e, const int* i) {
     if (Inside(i)) dose[(size_t(i[2]) * ny + i[1]) * nx + i[0]] += e;
   }
@@ -718,7 +731,7 @@ struct Sim {
       t.mat = im;
       ++st.steps;
       const double scal = T.mollerScale[im];
-      const double rho = geom.Density(im);
+      const double rho = geom.DensityAt(t.box, im);
       double dedx = T.dedx[im].Get(t.ekin) * rho;
       double emid = std::max(t.ekin - 0.5 * step * dedx, T.ecut);
       double dTr1 = T.itr1[im].Get(emid) * rho;
@@ -780,14 +793,14 @@ struct Sim {
   void KeepTrackingPhoton(Track& t) {
     const double kInvEMC2 = 1.0 / kEMC2;
     while (t.ekin > 0.0) {
-      const double lmax = 1.0 / T.imfpMax.Get(t.ekin);
+      const double lmax = 1.0 / (T.imfpMax.Get(t.ekin) * geom.Wscale());
       const double step = -lmax * std::log(rng.U());
       t.pos[0] += t.dir[0] * step; t.pos[1] += t.dir[1] * step; t.pos[2] += t.dir[2] * step;
       if (geom.DistanceToBoundary(t.pos, t.dir, t.box) < 0) { Escape(t); t.ekin = 0.0; return; }
       const int im = geom.MaterialIndex(t.box);
       if (im < 0) { Escape(t); t.ekin = 0.0; return; }
       t.mat = im;
-      const double rho = geom.Density(im);
+      const double rho = geom.DensityAt(t.box, im);
       const double tot = T.imfpTot[im].Get(t.ekin) * rho;
       const double r1 = rng.U();
       double prob = 1.0 - tot * lmax;
@@ -1053,9 +1066,16 @@ int oracle_simulate_slab_philox(void* h, long long first, int nprimary, double e
 int oracle_simulate_voxel(void* h, int nx, int ny, int nz, double vx, double vy, double vz, const uint8_t* mat,
                           int particle, int spectrum, double e0, double e1, int shape, double cx, double cy,
                           double fx, double fy, int nbx, int nby, long long first, long long nhist, uint64_t seed,
-                          double* dose, double* hist_edep, double* stats) {
+                          double* dose, double* hist_edep, double* stats, const float* rho) {
   auto* T = static_cast<Tables*>(h);
   VoxelGeom g{nx, ny, nz, -0.5 * nx * vx, -0.5 * ny * vy, 0.0, vx, vy, vz, 1.0 / vx, 1.0 / vy, 1.0 / vz, mat, T, dose, nullptr};
+  if (rho) {
+    // the same majorant scale as the library: max density / nominal density
+    g.rho = rho;
+    const size_t n = size_t(nx) * ny * nz;
+    for (size_t i = 0; i < n; ++i)
+      if (mat[i] != 255) g.wscale = std::max(g.wscale, double(rho[i]) / T->density[mat[i]]);
+  }
   PhiloxRng rng(seed);
   Sim<VoxelGeom, PhiloxRng> sim(*T, g, rng);
   Source s{particle, spectrum, e0, e1, shape, cx, cy, fx, fy, nbx, nby};
