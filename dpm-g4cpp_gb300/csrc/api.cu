@@ -397,6 +397,7 @@ void dpmx_run_options_default(dpmx_run_options* o) {
   o->batches = 10;
   o->tally_aggregate = -1;
   o->electron_kernel = -1;
+  o->photon_kernel = -1;
   o->use_graph = 1;
 }
 

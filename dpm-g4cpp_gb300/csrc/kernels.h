@@ -131,6 +131,9 @@ constexpr int kDepthBins = 1024;
 
 cudaError_t PreparePhotonPhase(const DevTables<float>& T);   // shared-memory limit, once per run
 cudaError_t LaunchPhotonPhase(const PhaseArgs& a, int blocks, int threads, cudaStream_t st);
+// block-batched photon phase (256 threads per block, shared-memory slots)
+int PhotonBlockBlocksPerSM();
+cudaError_t LaunchPhotonPhaseBlock(const PhaseArgs& a, int blocks, cudaStream_t st);
 cudaError_t LaunchElectronPhase(const PhaseArgs& a, int blocks, int threads, cudaStream_t st);
 // dose += t, dose2 += t^2, t = 0 over n bins
 cudaError_t LaunchFold(double* t, double* dose, double* dose2, long long n, cudaStream_t st);

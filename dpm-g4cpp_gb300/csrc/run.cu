@@ -46,6 +46,7 @@ struct Cfg {
   long long chunk = 1 << 20;
   int aggregate = 0;
   int eblock = 1;          // electron phase: 0 lane-refill kernel, 1 block-batched kernel
+  int pblock = 1;          // photon phase: 0 one photon per lane, 1 block-batched kernel
 };
 
 // Device scratch kept across runs. A run of the FP32 form needs GBs of queues,
@@ -351,7 +352,8 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
             CK(cudaEventCreate(&evP.back()));
             CK(cudaEventRecord(evP[evP.size() - 2], s));
           }
-          CK(LaunchPhotonPhase(a, blocks, cfg.threads, s));
+          if (cfg.pblock) CK(LaunchPhotonPhaseBlock(a, nsm * PhotonBlockBlocksPerSM(), s));
+          else CK(LaunchPhotonPhase(a, blocks, cfg.threads, s));
           if (profile) CK(cudaEventRecord(evP.back(), s));
           ++nl;
           // electrons of generation g; their secondaries form generation g+1
@@ -632,8 +634,11 @@ int CheckJobs(const dpmx_tables* t, const dpmx_job* jobs, int njobs) {
   return DPMX_OK;
 }
 
-Cfg DefaultCfg(const dpmx_run_options* o, long long totalHist) {
+Cfg DefaultCfg(const dpmx_run_options* o, long long totalHist, bool photonSources) {
   Cfg c;
+  // the block-batched photon phase pays off when photons are many (photon
+  // beams); with electron beams the photons are few bremsstrahlung secondaries
+  c.pblock = photonSources ? 1 : 0;
   if (o && o->block_size > 0) c.threads = std::min(256, std::max(32, o->block_size / 32 * 32));
   if (o && o->blocks_per_sm > 0) c.blocksPerSM = o->blocks_per_sm;
   if (o && o->chunk_histories > 0) c.chunk = o->chunk_histories;
@@ -645,6 +650,7 @@ Cfg DefaultCfg(const dpmx_run_options* o, long long totalHist) {
   }
   if (o && o->tally_aggregate >= 0) c.aggregate = o->tally_aggregate;
   if (o && o->electron_kernel >= 0) c.eblock = o->electron_kernel;
+  if (o && o->photon_kernel >= 0) c.pblock = o->photon_kernel;
   return c;
 }
 
@@ -721,14 +727,18 @@ int dpmx_run(const dpmx_tables* t, const dpmx_job* jobs, int njobs, const dpmx_r
       r->cfg[0] = 128; r->cfg[1] = 16; r->cfg[2] = 0; r->cfg[3] = 0;
     } else {
       long long total = 0;
-      for (int j = 0; j < njobs; ++j) total += jobs[j].histories;
-      Cfg cfg = DefaultCfg(&o, total);
+      bool photons = false;
+      for (int j = 0; j < njobs; ++j) {
+        total += jobs[j].histories;
+        photons = photons || (jobs[j].source.particle == 0 && jobs[j].histories > 0);
+      }
+      Cfg cfg = DefaultCfg(&o, total, photons);
       if (o.autotune) rc = Autotune(t, jobs, njobs, cfg, st, &cfg);
       if (!rc)
         rc = RunFp32(t, jobs, njobs, o.batches, cfg, tag, o.use_graph != 0 && !o.profile_phases, st, r->jobs, &r->ms,
                      &r->launches, o.profile_phases ? r->prof : nullptr);
       r->cfg[0] = cfg.threads; r->cfg[1] = cfg.blocksPerSM; r->cfg[2] = cfg.chunk;
-      r->cfg[3] = cfg.aggregate | (cfg.eblock << 1);
+      r->cfg[3] = cfg.aggregate | (cfg.eblock << 1) | (cfg.pblock << 2);
     }
   }
   if (ownStream) cudaStreamDestroy(st);

@@ -491,6 +491,8 @@ __global__ void __launch_bounds__(256) PhotonPhase(PhaseArgs a) {
   double acc = 0.0;
   unsigned pst = 0;
   unsigned long long nph = 0;
+  float lmax = 0.f, lmaxE = -1.f;   // Woodcock mean free path, kept while energy and job do not change
+  int lmaxJob = -1;
   for (;;) {
     const unsigned need = __ballot_sync(kFull, !active);
     const unsigned long long my = pool.Take(need, !active, a.head, lane);
@@ -531,7 +533,11 @@ __global__ void __launch_bounds__(256) PhotonPhase(PhaseArgs a) {
       continue;
     }
     ++nph;
-    const float lmax = 1.0f / (LinearGet(pt.imfpMax, p.e) * J.wscale);
+    if (p.e != lmaxE || job != lmaxJob) {
+      lmax = 1.0f / (LinearGet(pt.imfpMax, p.e) * J.wscale);
+      lmaxE = p.e;
+      lmaxJob = job;
+    }
     const float step = -lmax * __logf(rng.U());
     int im = -1;
     if (Fly(J, p, step)) im = MaterialAt(J, p.ix, p.iy, p.iz);
@@ -1516,6 +1522,333 @@ __global__ void __launch_bounds__(256, kBlockMinBlocks) ElectronPhaseB(PhaseArgs
   if ((tid & 31) == 0 && a.njobs > 0) atomicAdd(&a.jobs[0].cnt->steps, nsteps);
 }
 
+// ---------------------------------------------------------------------------
+// photon phase, block-batched: kPSlots photons per block live in shared
+// memory with their random-number state; every iteration each slot runs its
+// pending interaction (Compton or pair, over a compacted list) or its refill,
+// then one Woodcock step. The uniforms are drawn in the order of PhotonPhase,
+// so both kernels give the same histories.
+// ---------------------------------------------------------------------------
+constexpr int kPSlots = 512;
+constexpr int kPBlockMinBlocks = 4;
+
+struct PSlotArrays {
+  uint32_t vox[kPSlots];
+  float lx[kPSlots], ly[kPSlots], lz[kPSlots], dx[kPSlots], dy[kPSlots], dz[kPSlots], e[kPSlots];
+  uint32_t meta[kPSlots], hist[kPSlots], slot[kPSlots], ulo[kPSlots], uhi[kPSlots], pst[kPSlots];
+  uint32_t ctr[kPSlots], have[kPSlots], w0[kPSlots], w1[kPSlots], w2[kPSlots], w3[kPSlots];
+  double acc[kPSlots];
+};
+// lists: Compton from the front and pair from the back of cp; plain steps from
+// the front and idle slots from the back of run; counts rotate as for electrons
+enum : int { kQComp, kQPair, kQStep, kQIdle, kQExhausted, kQClaim, kQCounts = 8 };
+struct PSlotLists {
+  uint16_t cp[2][kPSlots];
+  uint16_t run[2][kPSlots];
+  int cnt[3][kQCounts];
+};
+
+__host__ __device__ constexpr size_t PhotonBlockStaticBytes() { return sizeof(PSlotArrays) + sizeof(PSlotLists); }
+
+__device__ __forceinline__ void PushP(uint16_t* list, int* n, int v, bool back) {
+  cg::coalesced_group g = cg::coalesced_threads();
+  int base = 0;
+  if (g.thread_rank() == 0) base = atomicAdd(n, int(g.size()));
+  const int pos = g.shfl(base, 0) + int(g.thread_rank());
+  list[back ? kPSlots - 1 - pos : pos] = uint16_t(v);
+}
+
+__device__ __forceinline__ void LoadPhoton(const PSlotArrays& S, int k, const JobF* jobs, PState& p, PRng& rng) {
+  const uint32_t v = S.vox[k];
+  p.ix = int(v & 0x7ffu); p.iy = int((v >> 11) & 0x7ffu); p.iz = int(v >> 22);
+  p.lx = S.lx[k]; p.ly = S.ly[k]; p.lz = S.lz[k];
+  p.dx = S.dx[k]; p.dy = S.dy[k]; p.dz = S.dz[k];
+  p.e = S.e[k];
+  p.meta = S.meta[k]; p.hist = S.hist[k]; p.slot = S.slot[k]; p.ulo = S.ulo[k]; p.uhi = S.uhi[k];
+  const JobF& J = jobs[p.meta >> 2];
+  rng.Init(J.k0, J.k1, p.hist, p.ulo, p.uhi);
+  rng.ctr = S.ctr[k];
+  rng.have = int(S.have[k]);
+  rng.w = make_uint4(S.w0[k], S.w1[k], S.w2[k], S.w3[k]);
+}
+
+__device__ __forceinline__ void StorePhoton(PSlotArrays& S, int k, const PState& p, const PRng& rng) {
+  S.vox[k] = PackVox(p.ix, p.iy, p.iz);
+  S.lx[k] = p.lx; S.ly[k] = p.ly; S.lz[k] = p.lz;
+  S.dx[k] = p.dx; S.dy[k] = p.dy; S.dz[k] = p.dz;
+  S.e[k] = p.e;
+  S.ctr[k] = rng.ctr; S.have[k] = uint32_t(rng.have);
+  S.w0[k] = rng.w.x; S.w1[k] = rng.w.y; S.w2[k] = rng.w.z; S.w3[k] = rng.w.w;
+}
+
+// one Woodcock step of slot k (SimDPMLike.cc:471-508): 0 delta step, 1 Compton,
+// 2 pair, 3 finished (escaped, absorbed, or over the step cap)
+template <int AGG>
+__device__ __forceinline__ int PhotonStepSlot(const PhaseArgs& a, const PTables& pt, const JobF* jobs, PSlotArrays& S,
+                                              int k, EscTally& esc, unsigned long long& nph, const DepthAcc& dacc) {
+  const DevTables<float>& T = a.T;
+  PState p;
+  PRng rng;
+  LoadPhoton(S, k, jobs, p, rng);
+  const int job = int(p.meta >> 2);
+  const JobF& J = jobs[job];
+  double acc = S.acc[k];
+  int code = 0;
+  const uint32_t pst = S.pst[k] + 1;
+  S.pst[k] = pst;
+  if (pst > kMaxPhotonSteps) {   // cannot happen for finite cross sections; bounded anyway
+    acc += p.e;
+    atomicAdd(&J.cnt->lost, 1ull);
+    code = 3;
+  } else {
+    ++nph;
+    const float lmax = 1.0f / (LinearGet(pt.imfpMax, p.e) * J.wscale);
+    const float step = -lmax * __logf(rng.U());
+    int im = -1;
+    if (Fly(J, p, step)) im = MaterialAt(J, p.ix, p.iy, p.iz);
+    if (im < 0) {
+      acc += p.e;
+      esc.Add(jobs, job, double(p.e));
+      code = 3;
+    } else {
+      const float rho = VoxelRho(J, T, p.ix, p.iy, p.iz, im);
+      const float r1 = rng.U();
+      float prob = 1.0f - LinearGet(pt.tot[im], p.e) * rho * lmax;
+      if (r1 >= prob) {
+        prob += LinearGet(pt.comp[im], p.e) * rho * lmax;
+        if (r1 < prob) {
+          code = 1;
+        } else {
+          prob += LinearGet(pt.pair[im], p.e) * rho * lmax;
+          if (r1 < prob && p.e > 2.0f * kEMC2f) {
+            code = 2;
+          } else {
+            // photoelectric absorption (also below the pair threshold)
+            Score(J, p.ix, p.iy, p.iz, p.hist, p.e, AGG, dacc);
+            acc += p.e;
+            code = 3;
+          }
+        }
+      }
+    }
+  }
+  if (code == 3) {
+    atomicAdd(a.histE + p.slot, acc);
+  } else {
+    S.acc[k] = acc;
+    StorePhoton(S, k, p, rng);
+  }
+  return code;
+}
+
+// Compton scattering at the slot's position (SimDPMLike.cc:512-570); false
+// when the scattered photon falls below the cut and is absorbed
+template <int AGG>
+__device__ __forceinline__ bool PhotonComptonSlot(const PhaseArgs& a, const JobF* jobs, PSlotArrays& S, int k,
+                                                  const DepthAcc& dacc) {
+  const DevTables<float>& T = a.T;
+  PState p;
+  PRng rng;
+  LoadPhoton(S, k, jobs, p, rng);
+  const JobF& J = jobs[p.meta >> 2];
+  double acc = S.acc[k];
+  const float a3 = rng.U(), a2 = rng.U(), a1 = rng.U();
+  const float eps = SampleKN(T.kn, p.e, a1, a2, a3);
+  const float kappa = p.e * (1.0f / kEMC2f);
+  const float phCost = 1.0f - (1.0f - eps) / (eps * kappa);
+  const float phE = eps * p.e;
+  const float phPhi = 2.0f * kPIf * rng.U();
+  const float elE = p.e - phE;
+  float sn, cs;
+  __sincosf(phPhi, &sn, &cs);
+  if (elE < T.ecut) {
+    Score(J, p.ix, p.iy, p.iz, p.hist, elE, AGG, dacc);
+    acc += elE;
+  } else {
+    const float e0 = kappa;
+    const float elCost = (1.0f + e0) * sqrtf((1.0f - eps) / (e0 * (2.0f + e0 * (1.0f - eps))));
+    const float sint = sqrtf(fmaxf(0.f, (1.0f + elCost) * (1.0f - elCost)));
+    PState c = p;
+    c.dx = -sint * cs; c.dy = -sint * sn; c.dz = elCost;   // phi + pi
+    RotateToLab(c.dx, c.dy, c.dz, p.dx, p.dy, p.dz);
+    c.e = elE;
+    c.meta = 1u | (p.meta & ~3u);
+    rng.Child(0, c.ulo, c.uhi);
+    if (!Append(a.outE, a.outECount, a.overflow, c)) acc += elE;
+  }
+  p.e = phE;
+  if (p.e < T.gcut) {
+    Score(J, p.ix, p.iy, p.iz, p.hist, p.e, AGG, dacc);
+    acc += p.e;
+    atomicAdd(a.histE + p.slot, acc);
+    return false;
+  }
+  const float phSint = sqrtf(fmaxf(0.f, (1.0f - phCost) * (1.0f + phCost)));
+  float u1 = phSint * cs, u2 = phSint * sn, u3 = phCost;
+  RotateToLab(u1, u2, u3, p.dx, p.dy, p.dz);
+  p.dx = u1; p.dy = u2; p.dz = u3;
+  S.acc[k] = acc;
+  StorePhoton(S, k, p, rng);
+  return true;
+}
+
+// pair production at the slot's position (SimDPMLike.cc:573-627); the photon ends
+template <int AGG>
+__device__ __forceinline__ void PhotonPairSlot(const PhaseArgs& a, const JobF* jobs, PSlotArrays& S, int k,
+                                               const DepthAcc& dacc) {
+  const DevTables<float>& T = a.T;
+  PState p;
+  PRng rng;
+  LoadPhoton(S, k, jobs, p, rng);
+  const JobF& J = jobs[p.meta >> 2];
+  double acc = S.acc[k];
+  const float sum = p.e - 2.0f * kEMC2f;
+  const float e1 = rng.U() * sum;
+  const float e2 = sum - e1;
+  if (e2 < T.ecut) {
+    Score(J, p.ix, p.iy, p.iz, p.hist, e2, AGG, dacc);
+    acc += e2;
+  } else {
+    PState c = p;
+    c.e = e2; c.meta = 1u | (p.meta & ~3u);
+    rng.Child(0, c.ulo, c.uhi);
+    if (!Append(a.outE, a.outECount, a.overflow, c)) acc += e2;
+  }
+  if (e1 < T.ecut) {
+    Score(J, p.ix, p.iy, p.iz, p.hist, e1, AGG, dacc);
+    acc += e1;
+    // annihilation at rest (SimDPMLike.cc:753-791)
+    const float cost = 1.0f - 2.0f * rng.U();
+    const float sint = sqrtf(fmaxf(0.f, (1.0f - cost) * (1.0f + cost)));
+    const float phi = 2.0f * kPIf * rng.U();
+    float s2, c2;
+    __sincosf(phi, &s2, &c2);
+    PState g = p;
+    g.e = kEMC2f; g.meta = 0u | (p.meta & ~3u);
+    g.dx = sint * c2; g.dy = sint * s2; g.dz = cost;
+    rng.Child(0, g.ulo, g.uhi);
+    if (!Append(a.outP, a.outPCount, a.overflow, g)) acc += kEMC2f;
+    g.dx = -g.dx; g.dy = -g.dy; g.dz = -g.dz;
+    rng.Child(1, g.ulo, g.uhi);
+    if (!Append(a.outP, a.outPCount, a.overflow, g)) acc += kEMC2f;
+  } else {
+    PState c = p;
+    c.e = e1; c.meta = 2u | (p.meta & ~3u);
+    rng.Child(1, c.ulo, c.uhi);
+    if (!Append(a.outE, a.outECount, a.overflow, c)) acc += e1 + 2.0f * kEMC2f;
+  }
+  atomicAdd(a.histE + p.slot, acc);
+}
+
+// a new photon (primary or queued) in slot k; false when it starts outside
+__device__ __forceinline__ bool PhotonRefillSlot(const PhaseArgs& a, const JobF* jobs,
+                                                 const unsigned long long* spre, PSlotArrays& S, int k,
+                                                 unsigned long long item, EscTally& esc) {
+  PState p;
+  PRng rng;
+  if (item < (unsigned long long)a.nPrimaries) {
+    MakePrimary(a, a.segs, (long long)item, p, rng);
+  } else {
+    LoadParticle(a.in, StripedIndex(a.in, spre, item - a.nPrimaries), p);
+    const JobF& J = jobs[p.meta >> 2];
+    rng.Init(J.k0, J.k1, p.hist, p.ulo, p.uhi);
+  }
+  const JobF& J = jobs[p.meta >> 2];
+  if (!InBox(J, p.ix, p.iy, p.iz) || MaterialAt(J, p.ix, p.iy, p.iz) < 0) {
+    esc.Add(jobs, int(p.meta >> 2), double(p.e));
+    atomicAdd(a.histE + p.slot, double(p.e));
+    return false;
+  }
+  S.meta[k] = p.meta; S.hist[k] = p.hist; S.slot[k] = p.slot; S.ulo[k] = p.ulo; S.uhi[k] = p.uhi;
+  S.pst[k] = 0;
+  S.acc[k] = 0.0;
+  StorePhoton(S, k, p, rng);
+  return true;
+}
+
+template <int AGG>
+__global__ void __launch_bounds__(256, kPBlockMinBlocks) PhotonPhaseB(PhaseArgs a) {
+  extern __shared__ __align__(16) unsigned char dyn[];
+  PSlotArrays& S = *reinterpret_cast<PSlotArrays*>(dyn);
+  PSlotLists& L = *reinterpret_cast<PSlotLists*>(dyn + sizeof(PSlotArrays));
+  __shared__ JobF sjobs[16];
+  __shared__ unsigned long long spre[kStripes + 1];
+  __shared__ PTables pt;
+  const bool fewJobs = a.njobs <= 16;
+  if (fewJobs)
+    for (int j = threadIdx.x; j < a.njobs; j += blockDim.x) sjobs[j] = a.jobs[j];
+  const unsigned long long nQ = StripePrefix(a.inCount, spre);
+  const JobF* jobs = fewJobs ? sjobs : a.jobs;
+  const unsigned long long total = (unsigned long long)a.nPrimaries + nQ;
+  if (total == 0) return;
+  StagePhotonTables(a.T, false, nullptr, &pt);
+  const DepthAcc dacc = DepthAccInit(a, dyn + ((PhotonBlockStaticBytes() + 15) & ~size_t(15)));
+  const int tid = threadIdx.x, lane = tid & 31;
+  for (int k = tid; k < kPSlots; k += blockDim.x) L.run[0][kPSlots - 1 - k] = uint16_t(k);
+  for (int c = tid; c < 3 * kQCounts; c += blockDim.x) (&L.cnt[0][0])[c] = (c == kQIdle) ? kPSlots : 0;
+  __syncthreads();
+  EscTally esc;
+  unsigned long long nph = 0;
+  int cr = 0, lr = 0;
+  for (;;) {
+    const int cw = cr == 2 ? 0 : cr + 1, cz = cw == 2 ? 0 : cw + 1, lw = lr ^ 1;
+    const int* nr = L.cnt[cr];
+    int* nw = L.cnt[cw];
+    const int e0 = nr[kQComp], e1 = e0 + nr[kQPair], e2 = e1 + nr[kQStep];
+    const bool exhausted = nr[kQExhausted] != 0;
+    if (e2 == 0 && exhausted) break;
+    if (tid == 0) {
+      for (int c = 0; c < kQCounts; ++c) L.cnt[cz][c] = 0;
+      if (exhausted) nw[kQExhausted] = 1;
+    }
+    for (;;) {
+      int b = 0;
+      if (lane == 0) b = atomicAdd(&L.cnt[cr][kQClaim], 32);
+      const int claimed = __shfl_sync(kFull, b, 0);
+      if (claimed >= kPSlots) break;
+      const int i = claimed + lane;
+      int k;
+      bool live = true;
+      if (i < e0) {
+        k = L.cp[lr][i];
+        live = PhotonComptonSlot<AGG>(a, jobs, S, k, dacc);
+      } else if (i < e1) {
+        k = L.cp[lr][kPSlots - 1 - (i - e0)];
+        PhotonPairSlot<AGG>(a, jobs, S, k, dacc);
+        live = false;
+      } else if (i < e2) {
+        k = L.run[lr][i - e1];
+      } else {
+        k = L.run[lr][kPSlots - 1 - (i - e2)];
+        live = false;
+        if (!exhausted) {
+          cg::coalesced_group g = cg::coalesced_threads();
+          unsigned long long base = 0;
+          if (g.thread_rank() == 0) base = atomicAdd(a.head, (unsigned long long)g.size());
+          base = g.shfl(base, 0);
+          const unsigned long long item = base + g.thread_rank();
+          if (base + g.size() >= total) nw[kQExhausted] = 1;
+          if (item < total) live = PhotonRefillSlot(a, jobs, spre, S, k, item, esc);
+        }
+      }
+      const int code = live ? PhotonStepSlot<AGG>(a, pt, jobs, S, k, esc, nph, dacc) : 3;
+      switch (code) {
+        case 0: PushP(L.run[lw], &nw[kQStep], k, false); break;
+        case 1: PushP(L.cp[lw], &nw[kQComp], k, false); break;
+        case 2: PushP(L.cp[lw], &nw[kQPair], k, true); break;
+        default: PushP(L.run[lw], &nw[kQIdle], k, true); break;
+      }
+    }
+    __syncthreads();
+    cr = cw;
+    lr = lw;
+  }
+  esc.Flush(jobs);
+  DepthAccFlush(a, jobs, dacc);
+  for (int o = 16; o > 0; o >>= 1) nph += __shfl_down_sync(kFull, nph, o);
+  if (lane == 0 && a.njobs > 0) atomicAdd(&a.jobs[0].cnt->photonSteps, nph);
+}
+
 __global__ void FoldKernel(double* t, double* dose, double* dose2, long long n) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const double v = t[i];
@@ -1661,9 +1994,27 @@ __global__ void TableKernel32(DevTables<float> T, int q, int imat, const double*
 
 int ElectronPhaseSmemBytes(const DevTables<float>& T) { return int(T.elecCount * sizeof(float)); }
 
+// dynamic shared memory of the block-batched photon phase
+__host__ __device__ inline size_t PhotonBlockSmemBytes(int depthBins) {
+  return ((PhotonBlockStaticBytes() + 15) & ~size_t(15)) + DepthAccBytes(depthBins);
+}
+
 cudaError_t PreparePhotonPhase(const DevTables<float>& T) {
-  return cudaFuncSetAttribute(PhotonPhase, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              int(PhotonTableBytes(T) + DepthAccBytes(kDepthBins)));
+  cudaError_t e = cudaFuncSetAttribute(PhotonPhase, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       int(PhotonTableBytes(T) + DepthAccBytes(kDepthBins)));
+  const int sb = int(PhotonBlockSmemBytes(kDepthBins));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(PhotonPhaseB<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(PhotonPhaseB<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
+  return e;
+}
+
+int PhotonBlockBlocksPerSM() { return kPBlockMinBlocks; }
+
+cudaError_t LaunchPhotonPhaseBlock(const PhaseArgs& a, int blocks, cudaStream_t st) {
+  const size_t smem = PhotonBlockSmemBytes(a.depthBins);
+  if (a.aggregate) PhotonPhaseB<1><<<blocks, 256, smem, st>>>(a);
+  else PhotonPhaseB<0><<<blocks, 256, smem, st>>>(a);
+  return cudaGetLastError();
 }
 
 cudaError_t LaunchPhotonPhase(const PhaseArgs& a, int blocks, int threads, cudaStream_t st) {

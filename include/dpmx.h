@@ -122,6 +122,9 @@ typedef struct {
   int electron_kernel;       /* FP32 electron phase: -1 default, 0 one electron per lane with
                                 refill, 1 block-batched (shared-memory slots, interactions
                                 processed over compacted per-type lists) */
+  int photon_kernel;         /* FP32 photon phase: -1 default, 0 one photon per lane, 1
+                                block-batched (Compton and pair over compacted lists); both
+                                draw the same random numbers per photon */
   void* stream;              /* cudaStream_t to run on, NULL = library stream */
 } dpmx_run_options;
 
@@ -151,7 +154,7 @@ int dpmx_result_stats(const dpmx_result* r, int job, dpmx_job_stats* s);
 double dpmx_result_elapsed_ms(const dpmx_result* r);
 long long dpmx_result_launches(const dpmx_result* r);
 /* chosen launch configuration: [block_size, blocks_per_sm, chunk_histories,
- * tally_aggregate + 2 * electron_kernel] */
+ * tally_aggregate + 2 * electron_kernel + 4 * photon_kernel] */
 int dpmx_result_config(const dpmx_result* r, long long* cfg4);
 /* phase profile of a run with profile_phases = 1 (zeros otherwise), 10 values:
  * electron-phase ms, photon-phase ms, electron-phase launches, photon-phase

@@ -102,3 +102,21 @@ def test_precision_workload_full_size(tables_wlb, dpm):
     assert np.abs(rel).mean() < 0.01, np.abs(rel).mean()
     assert (np.abs(p32[mask] - p64[mask]) <= 2 * np.sqrt(s32[mask] ** 2 + s64[mask] ** 2)).mean() >= 0.95
     assert abs(d32.sum() / n32 / (d64.sum() / n64) - 1.0) < 0.005
+
+
+@pytest.mark.parametrize("kind", ["photon", "electron"])
+def test_photon_kernels_give_the_same_histories(tables_wlb, dpm, kind):
+    """the lane and the block-batched photon phase draw the same random numbers
+    per photon: the same histories, up to FP32 rounding (the compiler contracts
+    the same formulas differently in the two kernels) and summation order"""
+    from importlib import import_module
+    wl = import_module("dpm-g4cpp_gb300.workloads")
+    m = wl.precision_phantom(nx=32, ny=32, nz=64, v=4.0)
+    ph = dpm.Phantom.voxels(tables_wlb, m, 4.0)
+    src = wl.precision_source(field=60.0) if kind == "photon" else dpm.Source(particle=-1, e0=12.0, e1=12.0, shape=1,
+                                                                              fx=40.0, fy=40.0)
+    a = dpm.run(tables_wlb, [dpm.Job(ph, src, 100000, 13)], batches=4, photon_kernel=0).tally(0)[0]
+    b = dpm.run(tables_wlb, [dpm.Job(ph, src, 100000, 13)], batches=4, photon_kernel=1).tally(0)[0]
+    assert abs(a.sum() / b.sum() - 1.0) < 1e-5
+    close = np.isclose(a, b, rtol=1e-4, atol=1e-9 * a.max())
+    assert close.mean() > 0.999, close.mean()
