@@ -326,12 +326,15 @@ int dpmx_phantom_voxels(const dpmx_tables* t, int nx, int ny, int nz, double vx,
     return Fail(DPMX_ERR_ARG, "phantom dimensions must be 1..2047 (x, y) and 1..1023 (z)");
   if (!(vx > 0 && vy > 0 && vz > 0)) return Fail(DPMX_ERR_ARG, "voxel sizes must be positive");
   const size_t n = size_t(nx) * ny * nz;
-  for (size_t i = 0; i < n; ++i)
-    if (mat[i] != kVacuum && mat[i] >= t->h.nmat) return Fail(DPMX_ERR_ARG, "material id beyond the data set");
-  float lut[256] = {0.0f};
-  for (int m = 0; m < t->h.nmat; ++m) lut[m] = float(t->h.density[m]);
-  auto rho = std::make_shared<std::vector<float>>(n);
-  for (size_t i = 0; i < n; ++i) (*rho)[i] = lut[mat[i]];
+  int worst = 0;   // the largest material id other than vacuum
+  for (size_t i = 0; i < n; ++i) {
+    const int m = mat[i] == kVacuum ? 0 : mat[i];
+    worst = m > worst ? m : worst;
+  }
+  if (worst >= t->h.nmat) return Fail(DPMX_ERR_ARG, "material id beyond the data set");
+  auto lut = std::make_shared<std::vector<float>>(256, 0.0f);
+  for (int m = 0; m < t->h.nmat; ++m) (*lut)[m] = float(t->h.density[m]);
+  auto hostMat = std::make_shared<std::vector<uint8_t>>(mat, mat + n);
   std::unique_ptr<dpmx_phantom> p(new dpmx_phantom());
   p->tables = t;
   p->kind = 1;
@@ -349,7 +352,8 @@ int dpmx_phantom_voxels(const dpmx_tables* t, int nx, int ny, int nz, double vx,
   g.rho = nullptr;
   g.wscale = 1.0;
   p->tallySize = (long long)n;
-  p->binDensity = rho;
+  p->binMaterial = hostMat;
+  p->materialDensity = lut;
   *out = p.release();
   return DPMX_OK;
 }

@@ -148,7 +148,10 @@ struct dpmx_phantom {
   uint8_t* d_mat = nullptr;
   float* d_rho = nullptr;   // per-voxel densities (dpmx_phantom_voxels_density) or null
   long long tallySize = 0;
-  // host copies for the dose outputs: density of every tally bin [g/cm3]
-  // (0 for vacuum), shared with the results that outlive the phantom
+  // host copies for the dose outputs, shared with the results that outlive
+  // the phantom: the density of every tally bin [g/cm3] (0 for vacuum), either
+  // given per bin or as material ids and a density per material
   std::shared_ptr<const std::vector<float>> binDensity;
+  std::shared_ptr<const std::vector<uint8_t>> binMaterial;
+  std::shared_ptr<const std::vector<float>> materialDensity;   // 256 entries
 };

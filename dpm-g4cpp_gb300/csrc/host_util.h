@@ -45,6 +45,11 @@ struct JobOut {
   GridGeom grid{};                                      // for the dose outputs
   double lbox = 1.0;
   std::shared_ptr<const std::vector<float>> binDensity;
+  std::shared_ptr<const std::vector<uint8_t>> binMaterial;
+  std::shared_ptr<const std::vector<float>> materialDensity;
+  float BinDensity(long long i) const {
+    return binDensity ? (*binDensity)[i] : (*materialDensity)[(*binMaterial)[i]];
+  }
 };
 
 }  // namespace dpmx

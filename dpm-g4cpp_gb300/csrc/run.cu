@@ -591,6 +591,8 @@ int PrepareOutputs(const dpmx_job* jobs, int njobs, bool tag, std::vector<JobOut
     o.grid = ph->grid;
     o.lbox = ph->lbox;
     o.binDensity = ph->binDensity;
+    o.binMaterial = ph->binMaterial;
+    o.materialDensity = ph->materialDensity;
     // dose and dose^2 come from the scratch pool; every run writes them whole
     void* p = nullptr;
     CK(ScratchPool::Instance().Get(o.tallySize * sizeof(double), &p));
@@ -634,11 +636,13 @@ int CheckJobs(const dpmx_tables* t, const dpmx_job* jobs, int njobs) {
   return DPMX_OK;
 }
 
-Cfg DefaultCfg(const dpmx_run_options* o, long long totalHist, bool photonSources) {
+Cfg DefaultCfg(const dpmx_run_options* o, long long totalHist) {
+  // The block-batched photon phase is the default for every run. It is faster
+  // with photon beams and somewhat slower when photons are few (electron
+  // beams), but the two photon kernels round some FP32 results differently, so
+  // a choice that depended on the job mix would make a batched run differ
+  // (slightly) from the same jobs run alone.
   Cfg c;
-  // the block-batched photon phase pays off when photons are many (photon
-  // beams); with electron beams the photons are few bremsstrahlung secondaries
-  c.pblock = photonSources ? 1 : 0;
   if (o && o->block_size > 0) c.threads = std::min(256, std::max(32, o->block_size / 32 * 32));
   if (o && o->blocks_per_sm > 0) c.blocksPerSM = o->blocks_per_sm;
   if (o && o->chunk_histories > 0) c.chunk = o->chunk_histories;
@@ -661,10 +665,13 @@ int Autotune(const dpmx_tables* t, const dpmx_job* jobs, int njobs, const Cfg ba
   const long long sample = std::min<long long>(total, 1 << 18);
   std::vector<dpmx_job> sj(jobs, jobs + njobs);
   for (auto& j : sj) j.histories = std::max<long long>(1, (long long)(double(j.histories) * sample / std::max(1LL, total)));
-  struct Cand { int threads, bps, agg, eblock; };
+  // threads and blocks per SM of the lane kernels, tally aggregation and the
+  // electron kernel; the photon kernel stays the run's (the two photon
+  // kernels round some FP32 results differently)
+  struct Cand { int threads, bps, agg, eblock, pblock; };
   // the phase kernels are compiled for at most 256 threads per block
-  const Cand cands[] = {{256, 3, 0, 0}, {256, 3, 1, 0}, {256, 2, 0, 0}, {128, 6, 0, 0},
-                        {256, 3, 0, 1}, {256, 3, 1, 1}, {256, 2, 0, 1}};
+  const Cand cands[] = {{256, 3, 0, 0, -1}, {256, 3, 1, 0, -1}, {256, 2, 0, 0, -1}, {128, 6, 0, 0, -1},
+                        {256, 3, 0, 1, -1}, {256, 3, 1, 1, -1}, {256, 2, 0, 1, -1}};
   double bestMs = 1e30;
   *best = base;
   for (const Cand& c : cands) {
@@ -673,6 +680,7 @@ int Autotune(const dpmx_tables* t, const dpmx_job* jobs, int njobs, const Cfg ba
     cfg.blocksPerSM = c.bps;
     cfg.aggregate = c.agg;
     cfg.eblock = c.eblock;
+    if (c.pblock >= 0) cfg.pblock = c.pblock;
     cfg.chunk = sample;
     std::vector<JobOut> outs;
     if (int rc = PrepareOutputs(sj.data(), njobs, false, outs)) return rc;
@@ -727,12 +735,8 @@ int dpmx_run(const dpmx_tables* t, const dpmx_job* jobs, int njobs, const dpmx_r
       r->cfg[0] = 128; r->cfg[1] = 16; r->cfg[2] = 0; r->cfg[3] = 0;
     } else {
       long long total = 0;
-      bool photons = false;
-      for (int j = 0; j < njobs; ++j) {
-        total += jobs[j].histories;
-        photons = photons || (jobs[j].source.particle == 0 && jobs[j].histories > 0);
-      }
-      Cfg cfg = DefaultCfg(&o, total, photons);
+      for (int j = 0; j < njobs; ++j) total += jobs[j].histories;
+      Cfg cfg = DefaultCfg(&o, total);
       if (o.autotune) rc = Autotune(t, jobs, njobs, cfg, st, &cfg);
       if (!rc)
         rc = RunFp32(t, jobs, njobs, o.batches, cfg, tag, o.use_graph != 0 && !o.profile_phases, st, r->jobs, &r->ms,
@@ -813,7 +817,6 @@ int dpmx_result_write(const dpmx_result* r, int job, const char* path, int forma
   }
   const double hist = double(o.cnt.histories);
   if (!(hist > 0)) return Fail(DPMX_ERR_ARG, "the job ran no histories");
-  const std::vector<float>& rho = *o.binDensity;
   FILE* f = std::fopen(path, format == DPMX_DOSE_RAW ? "wb" : "w");
   if (!f) return Fail(DPMX_ERR_FILE, std::string("file ") + path + " could not be created");
   bool ok = true;
@@ -831,7 +834,7 @@ int dpmx_result_write(const dpmx_result* r, int job, const char* path, int forma
     const int B = r->batches;
     std::vector<double> dose(n), rel(n);
     for (long long i = 0; i < n; ++i) {
-      const double massKg = double(rho[i]) * volCm3 * 1.0e-3;
+      const double massKg = double(o.BinDensity(i)) * volCm3 * 1.0e-3;
       dose[i] = massKg > 0.0 ? d[i] * mevToJ / massKg / hist : 0.0;
       // batch sums t_b: sum_b t_b = d, sum_b t_b^2 = d2; error of the mean of B batches
       const double var = B > 1 ? std::max(0.0, (d2[i] - d[i] * d[i] / B) / (B - 1)) * B : 0.0;
@@ -847,12 +850,12 @@ int dpmx_result_write(const dpmx_result* r, int job, const char* path, int forma
     const double dz = o.slab ? o.lbox : g.vz;
     std::vector<double> ez(nz, 0.0), rz(nz, 0.0), sz(nz, 0.0);
     if (o.slab) {
-      for (int i = 0; i < nz; ++i) { ez[i] = d[i]; rz[i] = rho[i]; sz[i] = st.empty() ? 0.0 : st[i]; }
+      for (int i = 0; i < nz; ++i) { ez[i] = d[i]; rz[i] = o.BinDensity(i); sz[i] = st.empty() ? 0.0 : st[i]; }
     } else {
       const long long plane = (long long)g.nx * g.ny;
       for (int iz = 0; iz < nz; ++iz) {
         double e = 0.0, r0 = 0.0;
-        for (long long k = 0; k < plane; ++k) { e += d[iz * plane + k]; r0 += rho[iz * plane + k]; }
+        for (long long k = 0; k < plane; ++k) { e += d[iz * plane + k]; r0 += o.BinDensity(iz * plane + k); }
         ez[iz] = e;
         rz[iz] = r0 / double(plane);
       }
