@@ -156,12 +156,14 @@ struct Chunk {
 
 // Cuts batches [b0, b1) (of B) of every job into chunks of at most `chunk`
 // histories. Batch b of job j runs as sub-job (b - b0) * njobs + j, which
-// scores into its own tally slice; a chunk may span several batches.
+// scores into its own tally slice; a chunk may span several batches. Jobs
+// come one after another (all their batches together), so that a chunk holds
+// few jobs and their tallies stay in L2.
 std::vector<Chunk> PlanGroup(const dpmx_job* jobs, int njobs, int b0, int b1, int B, long long chunk) {
   std::vector<Chunk> out;
   Chunk cur;
-  for (int b = b0; b < b1; ++b) {
-    for (int j = 0; j < njobs; ++j) {
+  for (int j = 0; j < njobs; ++j) {
+    for (int b = b0; b < b1; ++b) {
       const long long N = jobs[j].histories;
       long long first = N * b / B;
       long long left = N * (b + 1) / B - first;
