@@ -68,8 +68,9 @@ struct JobF {                  // per-job geometry, source and tally (device vie
   float vx, vy, vz, ivx, ivy, ivz;
   double x0, y0, z0;           // lower corner of voxel (0,0,0) [mm]
   const uint8_t* mat;
-  double* tally;               // batch tally of this job: bin i at tally[i * tstride]
-  long long tstride;           // batch slices interleaved per bin
+  double* tally;               // batch tally of this job: bin i of slice r at tally[r * sstride + i * tstride]
+  long long tstride;
+  long long sstride;
   double* steps;               // scoring-step counts (depth tally only) or null
   double* btally;              // beamlet-tagged tally [beamlet][nvox] or null
   int nbeamlets;
@@ -77,7 +78,7 @@ struct JobF {                  // per-job geometry, source and tally (device vie
   float e0, e1, cx, cy, fx, fy;
   uint32_t k0, k1;             // Philox key (job seed)
   RunCounters* cnt;
-  int dbase;                   // first bin of this job in a block's shared depth tally, or -1
+  int dbase;                   // first bin of this job (slice 0) in a block's shared depth tally, or -1
   const float* rho;            // per-voxel density [g/cm3] or null
   float wscale;                // Woodcock majorant scale (>= 1)
 };

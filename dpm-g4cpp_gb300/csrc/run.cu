@@ -155,7 +155,7 @@ struct Chunk {
 };
 
 // Cuts batches [b0, b1) (of B) of every job into chunks of at most `chunk`
-// histories. Batch b of job j runs as sub-job (b - b0) * njobs + j, which
+// histories. Batch b of job j runs as sub-job ((b - b0) << 8) | j, which
 // scores into its own tally slice; a chunk may span several batches. Jobs
 // come one after another (all their batches together), so that a chunk holds
 // few jobs and their tallies stay in L2.
@@ -170,7 +170,7 @@ std::vector<Chunk> PlanGroup(const dpmx_job* jobs, int njobs, int b0, int b1, in
       while (left > 0) {
         const long long take = std::min(left, chunk - cur.nslots);
         Segment s{};
-        s.job = (b - b0) * njobs + j;
+        s.job = ((b - b0) << 8) | j;   // sub-job: job (low 8 bits) and tally slice
         s.firstHist = jobs[j].first_history + first;
         s.count = take;
         s.slotBase = cur.nslots;
@@ -228,9 +228,10 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
   unsigned long long* dlast;
   if (int rc = buf.Get(&dsum, njobs)) return rc;
   if (int rc = buf.Get(&dlast, njobs)) return rc;
-  // sub-job r * njobs + j: job j scoring into tally slice r
+  // one JobF per job; a particle's sub-job (slice << 8 | job) selects the
+  // job's tally slice
   const int nsub = R * njobs;
-  std::vector<JobF> hj(nsub);
+  std::vector<JobF> hj(njobs);
   for (int j = 0; j < njobs; ++j) {
     const dpmx_phantom* ph = jobs[j].phantom;
     const GridGeom& g = ph->grid;
@@ -247,6 +248,7 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
     J.wscale = float(g.wscale);
     J.tally = tB + off[j] * binStride;
     J.tstride = binStride;
+    J.sstride = sliceStride;
     J.steps = outs[j].d_steps;
     J.btally = tag ? outs[j].d_btally : nullptr;
     J.nbeamlets = std::max(1, outs[j].nbeamlets);
@@ -258,10 +260,6 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
     J.k0 = uint32_t(jobs[j].seed);
     J.k1 = uint32_t(jobs[j].seed >> 32) ^ 0x5bd1e995u;
     J.cnt = cnt + j;
-    for (int r = 1; r < R; ++r) {
-      hj[r * njobs + j] = J;
-      hj[r * njobs + j].tally = tB + off[j] * binStride + r * sliceStride;
-    }
   }
   // slab jobs: the depth tallies are summed per block in shared memory first
   // when the bins of all sub-jobs fit
@@ -271,11 +269,12 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
     allSlab = allSlab && outs[j].slab;
     maxNz = std::max(maxNz, jobs[j].phantom->grid.nz);
   }
+  // bins: (slice * njobs + job) * maxNz + iz
   const int depthBins = (allSlab && (long long)nsub * maxNz <= kDepthBins) ? nsub * maxNz : 0;
-  for (int k = 0; k < nsub; ++k) hj[k].dbase = depthBins ? k * maxNz : -1;
+  for (int j = 0; j < njobs; ++j) hj[j].dbase = depthBins ? j * maxNz : -1;
   JobF* dj;
-  if (int rc = buf.Get(&dj, nsub)) return rc;
-  CK(cudaMemcpyAsync(dj, hj.data(), nsub * sizeof(JobF), cudaMemcpyHostToDevice, st));
+  if (int rc = buf.Get(&dj, njobs)) return rc;
+  CK(cudaMemcpyAsync(dj, hj.data(), njobs * sizeof(JobF), cudaMemcpyHostToDevice, st));
 
   // plan and segment tables
   std::vector<std::vector<Chunk>> plan(ngroups);
@@ -334,7 +333,7 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
           std::memset(&a, 0, sizeof(a));
           a.T = T->t32;
           a.jobs = dj;
-          a.njobs = nsub;
+          a.njobs = njobs;
           a.histE = histE;
           a.histE0 = histE0;
           a.overflow = ovf;
@@ -723,6 +722,7 @@ int dpmx_run(const dpmx_tables* t, const dpmx_job* jobs, int njobs, const dpmx_r
   dpmx_run_options o;
   if (opt) o = *opt; else dpmx_run_options_default(&o);
   if (o.batches < 1) o.batches = 1;
+  if (o.batches > 65536) return Fail(DPMX_ERR_ARG, "at most 65536 statistical batches");
   if (o.precision != DPMX_FP64_PLAIN && o.precision != DPMX_FP32_EVENT) return Fail(DPMX_ERR_ARG, "bad precision");
   cudaStream_t st = static_cast<cudaStream_t>(o.stream);
   bool ownStream = false;

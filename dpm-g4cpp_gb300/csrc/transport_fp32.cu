@@ -39,6 +39,10 @@ constexpr float kTolF = 1.0e-4f;
 constexpr float kHalfTolF = 0.5e-4f;
 constexpr unsigned kFull = 0xffffffffu;
 constexpr unsigned kMaxPhotonSteps = 1u << 22;     // per particle: a lane never loops without bound
+// A particle's sub-job (meta >> 2) is its job (low 8 bits) and the statistical
+// batch slice of the job's tally it scores into (the bits above).
+__device__ __forceinline__ int JobOfSub(uint32_t sub) { return int(sub & 0xffu); }
+__device__ __forceinline__ uint32_t SliceOfSub(uint32_t sub) { return sub >> 8; }
 constexpr unsigned kMaxElectronSteps = 1u << 24;
 
 // ---------------------------------------------------------------------------
@@ -220,18 +224,22 @@ __device__ __forceinline__ bool Append(const Queue& q, unsigned long long* count
 struct DepthAcc {
   double* e = nullptr;
   unsigned* n = nullptr;
+  int sliceStride = 0;   // bins between the batch slices of a job
 };
 
-__device__ __forceinline__ void Score(const JobF& J, int ix, int iy, int iz, uint32_t hist, float e, int agg,
-                                      const DepthAcc& d = DepthAcc()) {
+// deposit e of a particle (meta: its type and sub-job) in voxel (ix, iy, iz)
+__device__ __forceinline__ void Score(const JobF& J, uint32_t meta, int ix, int iy, int iz, uint32_t hist, float e,
+                                      int agg, const DepthAcc& d = DepthAcc()) {
   const double de = double(e);
+  const uint32_t slice = SliceOfSub(meta >> 2);
   if (d.e != nullptr && J.dbase >= 0) {   // depth tally of a slab job: block-local first
-    atomicAdd(d.e + J.dbase + iz, de);
-    atomicAdd(d.n + J.dbase + iz, 1u);
+    const int b = J.dbase + int(slice) * d.sliceStride + iz;
+    atomicAdd(d.e + b, de);
+    atomicAdd(d.n + b, 1u);
     return;
   }
   const long long idx = J.tallyDepth ? (long long)iz : ((long long)iz * J.ny + iy) * J.nx + ix;
-  double* ptr = J.tally + idx * J.tstride;
+  double* ptr = J.tally + (long long)slice * J.sstride + idx * J.tstride;
   if (agg) {
     cg::coalesced_group g = cg::coalesced_threads();
     cg::coalesced_group peers = cg::labeled_partition(g, (unsigned long long)ptr);
@@ -255,6 +263,7 @@ __host__ __device__ constexpr size_t DepthAccBytes(int bins) { return size_t(bin
 __device__ __forceinline__ DepthAcc DepthAccInit(const PhaseArgs& a, unsigned char* mem) {
   DepthAcc d;
   if (a.depthBins > 0) {
+    d.sliceStride = a.njobs * a.depthStride;
     d.e = reinterpret_cast<double*>(mem);
     d.n = reinterpret_cast<unsigned*>(mem + size_t(a.depthBins) * sizeof(double));
     for (int b = threadIdx.x; b < a.depthBins; b += blockDim.x) { d.e[b] = 0.0; d.n[b] = 0u; }
@@ -269,9 +278,10 @@ __device__ __forceinline__ void DepthAccFlush(const PhaseArgs& a, const JobF* jo
   for (int b = threadIdx.x; b < a.depthBins; b += blockDim.x) {
     const unsigned n = d.n[b];
     if (n == 0u) continue;
-    const JobF& J = jobs[b / a.depthStride];
-    const int iz = b % a.depthStride;
-    atomicAdd(J.tally + (long long)iz * J.tstride, d.e[b]);
+    // bin b = (slice * njobs + job) * depthStride + iz
+    const int q = b / a.depthStride, iz = b % a.depthStride;
+    const JobF& J = jobs[q % a.njobs];
+    atomicAdd(J.tally + (long long)(q / a.njobs) * J.sstride + (long long)iz * J.tstride, d.e[b]);
     if (J.steps) atomicAdd(J.steps + iz, double(n));
   }
 }
@@ -371,7 +381,7 @@ __device__ __forceinline__ int FindSegment(const Segment* segs, int n, long long
 
 __device__ void MakePrimary(const PhaseArgs& a, const Segment* segs, long long i, PState& p, PRng& rng) {
   const Segment& sg = segs[FindSegment(segs, a.nsegs, i)];
-  const JobF& J = a.jobs[sg.job];
+  const JobF& J = a.jobs[JobOfSub(uint32_t(sg.job))];
   const long long h = sg.firstHist + (i - sg.prefix);
   p.hist = uint32_t(h);
   p.slot = uint32_t(sg.slotBase + (i - sg.prefix));
@@ -501,16 +511,16 @@ __global__ void __launch_bounds__(256) PhotonPhase(PhaseArgs a) {
         MakePrimary(a, a.segs, (long long)my, p, rng);
       } else {
         LoadParticle(a.in, StripedIndex(a.in, spre, my - a.nPrimaries), p);
-        const JobF& J = jobs[p.meta >> 2];
+        const JobF& J = jobs[JobOfSub(p.meta >> 2)];
         rng.Init(J.k0, J.k1, p.hist, p.ulo, p.uhi);
       }
       acc = 0.0;
       pst = 0;
       active = true;
-      const JobF& J = jobs[p.meta >> 2];
+      const JobF& J = jobs[JobOfSub(p.meta >> 2)];
       if (!InBox(J, p.ix, p.iy, p.iz) || MaterialAt(J, p.ix, p.iy, p.iz) < 0) {
         acc += p.e;
-        esc.Add(jobs, int(p.meta >> 2), double(p.e));
+        esc.Add(jobs, JobOfSub(p.meta >> 2), double(p.e));
         atomicAdd(a.histE + p.slot, acc);
         active = false;
       }
@@ -522,7 +532,7 @@ __global__ void __launch_bounds__(256) PhotonPhase(PhaseArgs a) {
     if (!active) continue;
 
     // one Woodcock step
-    const int job = int(p.meta >> 2);
+    const int job = JobOfSub(p.meta >> 2);
     const JobF& J = jobs[job];
     bool done = false;
     if (++pst > kMaxPhotonSteps) {   // cannot happen for finite cross sections; bounded anyway
@@ -563,7 +573,7 @@ __global__ void __launch_bounds__(256) PhotonPhase(PhaseArgs a) {
           float sn, cs;
           __sincosf(phPhi, &sn, &cs);
           if (elE < T.ecut) {
-            Score(J, p.ix, p.iy, p.iz, p.hist, elE, a.aggregate, dacc);
+            Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, elE, a.aggregate, dacc);
             acc += elE;
           } else {
             const float e0 = kappa;
@@ -579,7 +589,7 @@ __global__ void __launch_bounds__(256) PhotonPhase(PhaseArgs a) {
           }
           p.e = phE;
           if (p.e < T.gcut) {
-            Score(J, p.ix, p.iy, p.iz, p.hist, p.e, a.aggregate, dacc);
+            Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, p.e, a.aggregate, dacc);
             acc += p.e;
             done = true;
           } else {
@@ -596,7 +606,7 @@ __global__ void __launch_bounds__(256) PhotonPhase(PhaseArgs a) {
             const float e1 = rng.U() * sum;
             const float e2 = sum - e1;
             if (e2 < T.ecut) {
-              Score(J, p.ix, p.iy, p.iz, p.hist, e2, a.aggregate, dacc);
+              Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, e2, a.aggregate, dacc);
               acc += e2;
             } else {
               PState c = p;
@@ -605,7 +615,7 @@ __global__ void __launch_bounds__(256) PhotonPhase(PhaseArgs a) {
               if (!Append(a.outE, a.outECount, a.overflow, c)) acc += e2;
             }
             if (e1 < T.ecut) {
-              Score(J, p.ix, p.iy, p.iz, p.hist, e1, a.aggregate, dacc);
+              Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, e1, a.aggregate, dacc);
               acc += e1;
               // annihilation at rest (SimDPMLike.cc:753-791)
               const float cost = 1.0f - 2.0f * rng.U();
@@ -630,12 +640,12 @@ __global__ void __launch_bounds__(256) PhotonPhase(PhaseArgs a) {
             done = true;
           } else if (r1 < prob) {
             // below threshold (pair IMFP floor): treated as photoelectric
-            Score(J, p.ix, p.iy, p.iz, p.hist, p.e, a.aggregate, dacc);
+            Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, p.e, a.aggregate, dacc);
             acc += p.e;
             done = true;
           } else {
             // photoelectric absorption
-            Score(J, p.ix, p.iy, p.iz, p.hist, p.e, a.aggregate, dacc);
+            Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, p.e, a.aggregate, dacc);
             acc += p.e;
             done = true;
           }
@@ -711,16 +721,16 @@ __global__ void __launch_bounds__(256) ElectronPhase(PhaseArgs a) {
         MakePrimary(a, a.segs, (long long)my, p, rng);
       } else {
         LoadParticle(a.in, StripedIndex(a.in, spre, my - a.nPrimaries), p);
-        const JobF& J = jobs[p.meta >> 2];
+        const JobF& J = jobs[JobOfSub(p.meta >> 2)];
         rng.Init(J.k0, J.k1, p.hist, p.ulo, p.uhi);
       }
       acc = 0.0;
       pst = 0;
       active = true;
-      const JobF& J = jobs[p.meta >> 2];
+      const JobF& J = jobs[JobOfSub(p.meta >> 2)];
       if (!InBox(J, p.ix, p.iy, p.iz) || MaterialAt(J, p.ix, p.iy, p.iz) < 0) {
         acc += p.e + ((p.meta & 3u) == 2u ? 2.0f * kEMC2f : 0.f);
-        esc.Add(jobs, int(p.meta >> 2), acc);
+        esc.Add(jobs, JobOfSub(p.meta >> 2), acc);
         atomicAdd(a.histE + p.slot, acc);
         active = false;
       } else {
@@ -734,7 +744,7 @@ __global__ void __launch_bounds__(256) ElectronPhase(PhaseArgs a) {
     if (!active) continue;
 
     // ---- one condensed-history sub-step (SimDPMLike.cc:273-458) ----
-    const int job = int(p.meta >> 2);
+    const int job = JobOfSub(p.meta >> 2);
     const JobF& J = jobs[job];
     const bool positron = (p.meta & 3u) == 2u;
     bool done = false;
@@ -791,7 +801,7 @@ __global__ void __launch_bounds__(256) ElectronPhase(PhaseArgs a) {
         const float edep = p.e;
         p.e = 0.f;
         if (!positron) {
-          Score(J, p.ix, p.iy, p.iz, p.hist, edep, a.aggregate);
+          Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, edep, a.aggregate);
           acc += edep;
         } else {
           // e+: move to the end of the step, annihilate there
@@ -816,7 +826,7 @@ __global__ void __launch_bounds__(256) ElectronPhase(PhaseArgs a) {
             g.dx = -g.dx; g.dy = -g.dy; g.dz = -g.dz;
             rng.Child(1, g.ulo, g.uhi);
             if (!Append(a.outP, a.outPCount, a.overflow, g)) acc += kEMC2f;
-            Score(J, p.ix, p.iy, p.iz, p.hist, edep, a.aggregate);
+            Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, edep, a.aggregate);
             acc += edep;
           }
         }
@@ -824,7 +834,7 @@ __global__ void __launch_bounds__(256) ElectronPhase(PhaseArgs a) {
       } else {
         p.e = ef;
         // score in the voxel of the step, then move
-        Score(J, p.ix, p.iy, p.iz, p.hist, de, a.aggregate);
+        Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, de, a.aggregate);
         acc += de;
         if (what == 0) {
           if (!MoveToFace(J, p, step, s.axis)) {
@@ -860,7 +870,7 @@ __global__ void __launch_bounds__(256) ElectronPhase(PhaseArgs a) {
               p.e -= eg;
             }
             if (p.e < ecut) {
-              Score(J, p.ix, p.iy, p.iz, p.hist, p.e, a.aggregate);
+              Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, p.e, a.aggregate);
               acc += p.e;
               if (positron) {
                 const float cost = 1.0f - 2.0f * rng.U();
@@ -1124,7 +1134,7 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
   EState s;
   uint32_t fl;
   LoadStepState(S, k, p, s, fl);
-  const int job = int(fl >> 8);
+  const int job = JobOfSub(fl >> 8);
   const JobF& J = jobs[job];
   const bool positron = (fl & kFPositron) != 0;
   double acc = S.acc[k];
@@ -1184,7 +1194,7 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
       const float edep = p.e;
       p.e = 0.f;
       if (!positron) {
-        Score(J, p.ix, p.iy, p.iz, p.hist, edep, AGG, dacc);
+        Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, edep, AGG, dacc);
         acc += edep;
       } else {
         bool inside;
@@ -1198,14 +1208,14 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
           PRng rng;
           SlotRng(S, k, J, p, rng);
           AnnihilateF(a, p, rng, acc);
-          Score(J, p.ix, p.iy, p.iz, p.hist, edep, AGG, dacc);
+          Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, edep, AGG, dacc);
           acc += edep;
         }
       }
       code = 5;
     } else {
       p.e = ef;
-      Score(J, p.ix, p.iy, p.iz, p.hist, de, AGG, dacc);
+      Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, de, AGG, dacc);
       acc += de;
       if (what == 0) {
         if (!MoveToFace(J, p, step, s.axis) || !Settle(J, p, s.sGeom, s.axis)) {
@@ -1238,7 +1248,7 @@ __device__ __forceinline__ void EventHinge(const PhaseArgs& a, const JobF* jobs,
   uint32_t fl;
   LoadSlot(S, k, p, s, fl);
   PRng rng;
-  SlotRng(S, k, jobs[fl >> 8], p, rng);
+  SlotRng(S, k, jobs[JobOfSub(fl >> 8)], p, rng);
   const float r2 = rng.U(), r1 = rng.U();
   const float d = SampleGS(a.T.gs, s.ekin0, r1, r2);
   const float cost = fmaxf(-1.0f, fminf(1.0f, d));
@@ -1259,7 +1269,7 @@ __device__ __forceinline__ void EventHinge(const PhaseArgs& a, const JobF* jobs,
 __device__ __forceinline__ void EventMscEnd(const PhaseArgs& a, const ETables& et, const JobF* jobs, SlotArrays& S,
                                             int k) {
   const uint32_t fl = S.flags[k];
-  const JobF& J = jobs[fl >> 8];
+  const JobF& J = jobs[JobOfSub(fl >> 8)];
   PRng rng;
   rng.Init(J.k0, J.k1, S.hist[k], S.ulo[k], S.uhi[k]);
   rng.ctr = S.ctr[k];
@@ -1282,7 +1292,7 @@ __device__ __forceinline__ bool EventBrem(const PhaseArgs& a, const JobF* jobs, 
   EState s;
   uint32_t fl;
   LoadSlot(S, k, p, s, fl);
-  const JobF& J = jobs[fl >> 8];
+  const JobF& J = jobs[JobOfSub(fl >> 8)];
   const DevTables<float>& T = a.T;
   PRng rng;
   SlotRng(S, k, J, p, rng);
@@ -1306,7 +1316,7 @@ __device__ __forceinline__ bool EventBrem(const PhaseArgs& a, const JobF* jobs, 
     p.e -= eg;
   }
   if (p.e < T.ecut) {
-    Score(J, p.ix, p.iy, p.iz, p.hist, p.e, AGG, dacc);
+    Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, p.e, AGG, dacc);
     acc += p.e;
     if ((fl & kFPositron) != 0) AnnihilateF(a, p, rng, acc);
     atomicAdd(a.histE + p.slot, acc);
@@ -1327,7 +1337,7 @@ __device__ __forceinline__ void EventMoller(const PhaseArgs& a, const ETables& e
   EState s;
   uint32_t fl;
   LoadSlot(S, k, p, s, fl);
-  const JobF& J = jobs[fl >> 8];
+  const JobF& J = jobs[JobOfSub(fl >> 8)];
   PRng rng;
   SlotRng(S, k, J, p, rng);
   double acc = S.acc[k];
@@ -1366,10 +1376,10 @@ __device__ __forceinline__ bool RefillSlot(const PhaseArgs& a, const ETables& et
     MakePrimary(a, a.segs, (long long)item, p, rng);
   } else {
     LoadParticle(a.in, StripedIndex(a.in, spre, item - a.nPrimaries), p);
-    const JobF& J = jobs[p.meta >> 2];
+    const JobF& J = jobs[JobOfSub(p.meta >> 2)];
     rng.Init(J.k0, J.k1, p.hist, p.ulo, p.uhi);
   }
-  const int job = int(p.meta >> 2);
+  const int job = JobOfSub(p.meta >> 2);
   const JobF& J = jobs[job];
   if (!InBox(J, p.ix, p.iy, p.iz) || MaterialAt(J, p.ix, p.iy, p.iz) < 0) {
     const double out = p.e + ((p.meta & 3u) == 2u ? 2.0 * kEMC2f : 0.0);
@@ -1565,7 +1575,7 @@ __device__ __forceinline__ void LoadPhoton(const PSlotArrays& S, int k, const Jo
   p.dx = S.dx[k]; p.dy = S.dy[k]; p.dz = S.dz[k];
   p.e = S.e[k];
   p.meta = S.meta[k]; p.hist = S.hist[k]; p.slot = S.slot[k]; p.ulo = S.ulo[k]; p.uhi = S.uhi[k];
-  const JobF& J = jobs[p.meta >> 2];
+  const JobF& J = jobs[JobOfSub(p.meta >> 2)];
   rng.Init(J.k0, J.k1, p.hist, p.ulo, p.uhi);
   rng.ctr = S.ctr[k];
   rng.have = int(S.have[k]);
@@ -1590,7 +1600,7 @@ __device__ __forceinline__ int PhotonStepSlot(const PhaseArgs& a, const PTables&
   PState p;
   PRng rng;
   LoadPhoton(S, k, jobs, p, rng);
-  const int job = int(p.meta >> 2);
+  const int job = JobOfSub(p.meta >> 2);
   const JobF& J = jobs[job];
   double acc = S.acc[k];
   int code = 0;
@@ -1624,7 +1634,7 @@ __device__ __forceinline__ int PhotonStepSlot(const PhaseArgs& a, const PTables&
             code = 2;
           } else {
             // photoelectric absorption (also below the pair threshold)
-            Score(J, p.ix, p.iy, p.iz, p.hist, p.e, AGG, dacc);
+            Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, p.e, AGG, dacc);
             acc += p.e;
             code = 3;
           }
@@ -1650,7 +1660,7 @@ __device__ __forceinline__ bool PhotonComptonSlot(const PhaseArgs& a, const JobF
   PState p;
   PRng rng;
   LoadPhoton(S, k, jobs, p, rng);
-  const JobF& J = jobs[p.meta >> 2];
+  const JobF& J = jobs[JobOfSub(p.meta >> 2)];
   double acc = S.acc[k];
   const float a3 = rng.U(), a2 = rng.U(), a1 = rng.U();
   const float eps = SampleKN(T.kn, p.e, a1, a2, a3);
@@ -1662,7 +1672,7 @@ __device__ __forceinline__ bool PhotonComptonSlot(const PhaseArgs& a, const JobF
   float sn, cs;
   __sincosf(phPhi, &sn, &cs);
   if (elE < T.ecut) {
-    Score(J, p.ix, p.iy, p.iz, p.hist, elE, AGG, dacc);
+    Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, elE, AGG, dacc);
     acc += elE;
   } else {
     const float e0 = kappa;
@@ -1678,7 +1688,7 @@ __device__ __forceinline__ bool PhotonComptonSlot(const PhaseArgs& a, const JobF
   }
   p.e = phE;
   if (p.e < T.gcut) {
-    Score(J, p.ix, p.iy, p.iz, p.hist, p.e, AGG, dacc);
+    Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, p.e, AGG, dacc);
     acc += p.e;
     atomicAdd(a.histE + p.slot, acc);
     return false;
@@ -1700,13 +1710,13 @@ __device__ __forceinline__ void PhotonPairSlot(const PhaseArgs& a, const JobF* j
   PState p;
   PRng rng;
   LoadPhoton(S, k, jobs, p, rng);
-  const JobF& J = jobs[p.meta >> 2];
+  const JobF& J = jobs[JobOfSub(p.meta >> 2)];
   double acc = S.acc[k];
   const float sum = p.e - 2.0f * kEMC2f;
   const float e1 = rng.U() * sum;
   const float e2 = sum - e1;
   if (e2 < T.ecut) {
-    Score(J, p.ix, p.iy, p.iz, p.hist, e2, AGG, dacc);
+    Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, e2, AGG, dacc);
     acc += e2;
   } else {
     PState c = p;
@@ -1715,7 +1725,7 @@ __device__ __forceinline__ void PhotonPairSlot(const PhaseArgs& a, const JobF* j
     if (!Append(a.outE, a.outECount, a.overflow, c)) acc += e2;
   }
   if (e1 < T.ecut) {
-    Score(J, p.ix, p.iy, p.iz, p.hist, e1, AGG, dacc);
+    Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, e1, AGG, dacc);
     acc += e1;
     // annihilation at rest (SimDPMLike.cc:753-791)
     const float cost = 1.0f - 2.0f * rng.U();
@@ -1750,12 +1760,12 @@ __device__ __forceinline__ bool PhotonRefillSlot(const PhaseArgs& a, const JobF*
     MakePrimary(a, a.segs, (long long)item, p, rng);
   } else {
     LoadParticle(a.in, StripedIndex(a.in, spre, item - a.nPrimaries), p);
-    const JobF& J = jobs[p.meta >> 2];
+    const JobF& J = jobs[JobOfSub(p.meta >> 2)];
     rng.Init(J.k0, J.k1, p.hist, p.ulo, p.uhi);
   }
-  const JobF& J = jobs[p.meta >> 2];
+  const JobF& J = jobs[JobOfSub(p.meta >> 2)];
   if (!InBox(J, p.ix, p.iy, p.iz) || MaterialAt(J, p.ix, p.iy, p.iz) < 0) {
-    esc.Add(jobs, int(p.meta >> 2), double(p.e));
+    esc.Add(jobs, JobOfSub(p.meta >> 2), double(p.e));
     atomicAdd(a.histE + p.slot, double(p.e));
     return false;
   }
@@ -1931,7 +1941,7 @@ __global__ void EnergyCheckKernel(const double* histE, const double* histE0, lon
       const int mid = (lo + hi + 1) >> 1;
       if (segs[mid].slotBase <= i) lo = mid; else hi = mid - 1;
     }
-    RunCounters* c = jobs[segs[lo].job].cnt;
+    RunCounters* c = jobs[JobOfSub(uint32_t(segs[lo].job))].cnt;
     if (c != cur) {
       if (cur) flush(cur);
       cur = c;
