@@ -1475,8 +1475,10 @@ __global__ void __launch_bounds__(256, kBlockMinBlocks) ElectronPhaseB(PhaseArgs
         int b = 0;
         if (lane == 0) b = atomicAdd(&L.cnt[cr][kLClaim], 32);
         const int claimed = __shfl_sync(kFull, b, 0);
-        if (claimed >= kSetSlots) break;
+        // no more work: the idle slots stay idle without being visited
+        if (claimed >= (exhausted ? e4 : kSetSlots)) break;
         const int i = claimed + lane;
+        if (exhausted && i >= e4) continue;
         int k;
         bool live = true;
         if (i < e4) {
@@ -1815,8 +1817,10 @@ __global__ void __launch_bounds__(256, kPBlockMinBlocks) PhotonPhaseB(PhaseArgs 
       int b = 0;
       if (lane == 0) b = atomicAdd(&L.cnt[cr][kQClaim], 32);
       const int claimed = __shfl_sync(kFull, b, 0);
-      if (claimed >= kPSlots) break;
+      // no more work: the idle slots stay idle without being visited
+      if (claimed >= (exhausted ? e2 : kPSlots)) break;
       const int i = claimed + lane;
+      if (exhausted && i >= e2) continue;
       int k;
       bool live = true;
       if (i < e0) {
