@@ -264,6 +264,7 @@ def main():
     r = one(10**6, profile=True)
     pr = r.profile
     eblock = r.config["electron_kernel"] == 1
+    pblock = r.config["photon_kernel"] == 1
     r.close()
     peak, peak_kind = measured_peaks()
     e_bytes = pr["electron_steps"] * BYTES_E_STEP + pr["electrons"] * BYTES_PARTICLE
@@ -274,7 +275,8 @@ def main():
         kflops = pr["electron_steps"] * FLOPS_E_STEP
         kunits = pr["electron_steps"]
     else:
-        kname, kms, kbytes, nl = "PhotonPhase", pr["photon_ms"], p_bytes, pr["photon_launches"]
+        kname = "PhotonPhaseB" if pblock else "PhotonPhase"
+        kms, kbytes, nl = pr["photon_ms"], p_bytes, pr["photon_launches"]
         kflops = pr["photon_steps"] * FLOPS_P_STEP
         kunits = pr["photon_steps"]
     achieved = kbytes / (kms * 1e-3) / 1e9
