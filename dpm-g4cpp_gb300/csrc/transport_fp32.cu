@@ -961,6 +961,7 @@ __global__ void __launch_bounds__(256) ElectronPhase(PhaseArgs a) {
 constexpr int kSlots = 512;
 constexpr int kBlockMinBlocks = 3;      // resident blocks per SM the kernel is compiled for
 constexpr bool kTablesInSmem = false;  // electron tables staged per block, else read through L1
+constexpr bool kCacheMaterial = true;  // a slot keeps its voxel's material: read once per voxel entered
 constexpr uint32_t kFAxis = 3u, kFHinge = 4u, kFNeedGeom = 8u, kFPositron = 16u, kFAlive = 32u;
 
 struct SlotArrays {     // shared-memory state of the resident electrons
@@ -970,6 +971,7 @@ struct SlotArrays {     // shared-memory state of the resident electrons
   uint32_t flags[kSlots];   // axis (2 bits), hinge, needGeom, positron, alive; job << 8
   uint32_t hist[kSlots], slot[kSlots], ulo[kSlots], uhi[kSlots], ctr[kSlots], pst[kSlots];
   double acc[kSlots];
+  int8_t mat[kSlots];       // material of the slot's current voxel (-1: vacuum)
 };
 // The block's slots form kSets sets with their own lists. With two sets the
 // warps alternate between them: when a warp has no more items of one set's
@@ -1141,10 +1143,18 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
   int code = 0;
   int im = -1;
   if (s.needGeom) {
-    if (Settle(J, p, s.sGeom, s.axis)) im = MaterialAt(J, p.ix, p.iy, p.iz);
+    const int ox = p.ix, oy = p.iy, oz = p.iz;
+    if (Settle(J, p, s.sGeom, s.axis)) {
+      if (!kCacheMaterial || p.ix != ox || p.iy != oy || p.iz != oz) {
+        im = MaterialAt(J, p.ix, p.iy, p.iz);
+        if (kCacheMaterial) S.mat[k] = int8_t(im);
+      } else {
+        im = S.mat[k];
+      }
+    }
     s.needGeom = false;
   } else {
-    im = MaterialAt(J, p.ix, p.iy, p.iz);
+    im = kCacheMaterial ? int(S.mat[k]) : MaterialAt(J, p.ix, p.iy, p.iz);
   }
   const uint32_t pst = S.pst[k] + 1;
   S.pst[k] = pst;
@@ -1223,6 +1233,8 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
           acc += out;
           esc.Add(jobs, job, double(out));
           code = 5;
+        } else if (kCacheMaterial) {
+          S.mat[k] = int8_t(MaterialAt(J, p.ix, p.iy, p.iz));   // the voxel just entered
         }
       } else {
         p.lx += step * p.dx; p.ly += step * p.dy; p.lz += step * p.dz;
@@ -1297,7 +1309,7 @@ __device__ __forceinline__ bool EventBrem(const PhaseArgs& a, const JobF* jobs, 
   PRng rng;
   SlotRng(S, k, J, p, rng);
   double acc = S.acc[k];
-  const int im = MaterialAt(J, p.ix, p.iy, p.iz);
+  const int im = kCacheMaterial ? int(S.mat[k]) : MaterialAt(J, p.ix, p.iy, p.iz);
   if (p.e > T.gcut && im >= 0) {
     const float r3 = rng.U(), r2 = rng.U(), r1 = rng.U();
     const float eg = SampleSB(T.sb[im], p.e, r1, r2, r3);
@@ -1381,7 +1393,8 @@ __device__ __forceinline__ bool RefillSlot(const PhaseArgs& a, const ETables& et
   }
   const int job = JobOfSub(p.meta >> 2);
   const JobF& J = jobs[job];
-  if (!InBox(J, p.ix, p.iy, p.iz) || MaterialAt(J, p.ix, p.iy, p.iz) < 0) {
+  const int im0 = InBox(J, p.ix, p.iy, p.iz) ? MaterialAt(J, p.ix, p.iy, p.iz) : -1;
+  if (im0 < 0) {
     const double out = p.e + ((p.meta & 3u) == 2u ? 2.0 * kEMC2f : 0.0);
     esc.Add(jobs, job, out);
     atomicAdd(a.histE + p.slot, out);
@@ -1401,6 +1414,7 @@ __device__ __forceinline__ bool RefillSlot(const PhaseArgs& a, const ETables& et
   S.acc[k] = 0.0;
   S.ctr[k] = rng.ctr;
   S.pst[k] = 0;
+  S.mat[k] = int8_t(im0);
   return true;
 }
 
