@@ -13,8 +13,9 @@
 //    captured into one CUDA graph and launched once. Empty phases return at
 //    once (their input count is read on the device).
 //  * Tuning: a short sample of the jobs is timed for a few launch shapes
-//    (threads per block, blocks per SM, warp-aggregated tally) and chunk
-//    sizes, and the fastest is used for the run.
+//    (lane or block electron kernel, threads per block and blocks per SM of
+//    the lane kernels, warp-aggregated tally), and the fastest is used for
+//    the run.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>

@@ -2,21 +2,26 @@
 //
 // Particles of one generation live in SoA queues in HBM. A generation is
 // transported in two phases: all photons (Woodcock tracking), then all
-// electrons/positrons (condensed-history stepping). Each phase is a persistent
-// kernel: every lane holds one particle, advances it one step per loop
-// iteration and, when the particle is finished, refills from the phase's work
-// counter (one atomic per warp per refill). Secondaries are appended to the
-// next generation's queues with warp-aggregated atomics, so photons and
-// electrons never share a warp and lanes stay busy until the queue drains.
+// electrons/positrons (condensed-history stepping). Each phase is one
+// persistent launch, in one of two forms:
+//  * block-batched (the default): a block keeps 512 particles in shared
+//    memory; every iteration each particle runs its pending interaction, over
+//    a list compacted by interaction type so that a warp runs one kind at a
+//    time, or is refilled from the phase's work counter, and then takes one
+//    step (ElectronPhaseB, PhotonPhaseB);
+//  * one particle per lane, refilled from the work counter when it ends
+//    (ElectronPhase, PhotonPhase).
+// Secondaries are appended to the next generation's queues with
+// warp-aggregated atomics on striped counters.
 //
 // Geometry is tracked as an integer voxel index plus an FP32 offset inside the
 // voxel, which keeps the 1e-4 mm boundary tolerance of the reference
-// (Geom.hh:107) meaningful at any phantom size. Electron spline tables are
-// staged in shared memory; photon and sampling tables are read through the
-// read-only cache with vector loads. Energy deposits are tallied in FP64
-// (optionally warp-aggregated on equal voxels), and every particle's deposited
-// plus escaped energy is added to its history's FP64 slot once, at the end of
-// the particle, for the per-history energy-conservation check.
+// (Geom.hh:107) meaningful at any phantom size. Electron spline tables are read
+// through L1 (or staged in shared memory); photon and sampling tables are read
+// in place. Energy deposits are tallied in FP64 (optionally warp-aggregated on
+// equal voxels; slab depth tallies per block in shared memory first), and every
+// particle's deposited plus escaped energy is added to its history's FP64 slot
+// once, at the end of the particle, for the per-history energy check.
 //
 // The physics of each step and interaction is the reference's
 // (SimDPMLike.cc:254-791) evaluated in FP32; the order in which particles of a
