@@ -1554,6 +1554,245 @@ __global__ void __launch_bounds__(256, kBlockMinBlocks) ElectronPhaseB(PhaseArgs
 }
 
 // ---------------------------------------------------------------------------
+// electron phase, ring-scheduled: the slots of ElectronPhaseB without the
+// block's iterations. Every slot waits in one of six rings (shared memory) by
+// what it does next; a warp takes up to 32 entries of one ring whenever it is
+// free, runs that interaction (or the refill) and one sub-step on them, and
+// puts each slot on the ring of its next action. No warp waits for another
+// between sub-steps, and the 32 slots a warp takes run the same interaction.
+// A particle's histories do not depend on this order: every particle draws
+// from its own random stream.
+//
+// A ring has kSlots cells and two counters (head: entries taken, tail:
+// entries reserved). The cell of position pos holds (lap << 10 | full << 9 |
+// slot) with lap = pos / kSlots mod 64, the bounded-queue scheme of D. Vyukov:
+// a producer waits until its cell is empty for its lap, a consumer until it is
+// full for its lap, so neither can take the other lap's entry. At most one
+// operation of each warp is pending on a cell, so a cell never lags its
+// newest reservation by more than 8 laps and 6 bits tell the laps apart.
+// ---------------------------------------------------------------------------
+constexpr bool kRingScheduler = true;   // ElectronPhaseR, else ElectronPhaseB
+enum : int { kRBrem, kRMoller, kRHinge, kRMscEnd, kRIdle, kRStep, kRings };   // in the order rings are preferred
+constexpr int kRingBits = 9;
+static_assert((1 << kRingBits) == kSlots, "one ring cell per slot");
+static_assert(kSets == 1, "one slot set");
+constexpr uint32_t kCellSlot = (1u << kRingBits) - 1u, kCellFull = 1u << kRingBits;
+// ring of a sub-step's result code (0 step, 1 brem, 2 Moller, 3 hinge, 4 MSC
+// step end, 5 finished), four bits per code
+constexpr uint32_t kRingOfCode = 0x432105u;
+
+struct SlotRings {
+  uint16_t cell[kRings][kSlots];
+  unsigned int head[kRings], tail[kRings];
+  int live;        // slots not retired: queued or held by a warp
+  int exhausted;   // every work item of the generation has been claimed
+};
+
+__device__ __forceinline__ uint32_t CellEmpty(uint32_t pos) { return ((pos >> kRingBits) & 63u) << (kRingBits + 1); }
+__device__ __forceinline__ uint32_t CellFull(uint32_t pos) { return CellEmpty(pos) | kCellFull; }
+
+__device__ __forceinline__ uint32_t CellLoad(const uint16_t* c) {
+  uint16_t v;
+  asm volatile("ld.acquire.cta.shared::cta.u16 %0, [%1];"
+               : "=h"(v)
+               : "r"(uint32_t(__cvta_generic_to_shared(c)))
+               : "memory");
+  return v;
+}
+// publishes a cell: the slot's state written before it is visible to the
+// warp that loads the cell
+__device__ __forceinline__ void CellStore(uint16_t* c, uint32_t v) {
+  asm volatile("st.release.cta.shared::cta.u16 [%0], %1;" ::"r"(uint32_t(__cvta_generic_to_shared(c))),
+               "h"(uint16_t(v))
+               : "memory");
+}
+// waits until (cell & m) == want; false after kWaitCycles
+__device__ __forceinline__ bool CellWait(const uint16_t* c, uint32_t want, uint32_t m, uint32_t& v) {
+  v = CellLoad(c);
+  if ((v & m) == want) return true;
+  const long long t0 = clock64();
+  for (;;) {
+    __nanosleep(32);
+    v = CellLoad(c);
+    if ((v & m) == want) return true;
+    if (clock64() - t0 > kWaitCycles) return false;
+  }
+}
+
+__host__ __device__ constexpr size_t RingPhaseStaticBytes() { return sizeof(SlotArrays) + sizeof(SlotRings); }
+static_assert(sizeof(SlotRings) <= kSets * sizeof(SlotLists), "the rings fit where the lists are");
+
+template <int AGG>
+__global__ void __launch_bounds__(256, kBlockMinBlocks) ElectronPhaseR(PhaseArgs a) {
+  extern __shared__ __align__(16) unsigned char dyn[];
+  SlotArrays& S = *reinterpret_cast<SlotArrays*>(dyn);
+  SlotRings& R = *reinterpret_cast<SlotRings*>(dyn + sizeof(SlotArrays));
+  float* sdata = reinterpret_cast<float*>(dyn + RingPhaseStaticBytes());
+  __shared__ ETables et;
+  __shared__ JobF sjobs[16];
+  __shared__ unsigned long long spre[kStripes + 1];
+  const bool fewJobs = a.njobs <= 16;
+  if (fewJobs)
+    for (int j = threadIdx.x; j < a.njobs; j += blockDim.x) sjobs[j] = a.jobs[j];
+  const DepthAcc dacc = DepthAccInit(a, dyn + BlockPhaseSmemBytesFor(a.T, 0));
+  const unsigned long long nQ = StripePrefix(a.inCount, spre);
+  const JobF* jobs = fewJobs ? sjobs : a.jobs;
+  const unsigned long long total = (unsigned long long)a.nPrimaries + nQ;
+  if (total == 0) return;   // an empty generation skips the table staging
+  if (kTablesInSmem) StageElectronTables(a.T, sdata, &et);
+  else if (threadIdx.x == 0) BindElectronTables(a.T, &et);   // visible after the barrier below
+  const int tid = threadIdx.x, lane = tid & 31;
+  // every slot starts on the idle ring (lap 0, full); the other rings are empty
+  for (int i = tid; i < kRings * kSlots; i += blockDim.x) {
+    const int r = i / kSlots, k = i % kSlots;
+    R.cell[r][k] = uint16_t(r == kRIdle ? (kCellFull | uint32_t(k)) : 0u);
+  }
+  for (int k = tid; k < kSlots; k += blockDim.x) S.flags[k] = 0u;
+  if (tid < kRings) {
+    R.head[tid] = 0u;
+    R.tail[tid] = tid == kRIdle ? unsigned(kSlots) : 0u;
+  }
+  if (tid == 0) {
+    R.live = kSlots;
+    R.exhausted = 0;
+  }
+  __syncthreads();
+  volatile unsigned int* vhead = R.head;
+  volatile unsigned int* vtail = R.tail;
+  volatile int* vlive = &R.live;
+  volatile int* vexh = &R.exhausted;
+  EscTally esc;
+  unsigned long long nsteps = 0;
+  bool gaveUp = false;
+  for (;;) {
+    // take up to 32 entries: the first ring (in preference order) holding a
+    // full warp's worth, else the fullest; none queued and none live: done
+    int ring = -1, n = 0;
+    uint32_t h = 0;
+    long long t0 = 0;
+    bool waited = false;
+    for (;;) {
+      uint32_t hh = 0;
+      int av = 0;
+      if (lane < kRings) {
+        hh = vhead[lane];
+        av = int(vtail[lane] - hh);
+      }
+      const unsigned full = __ballot_sync(kFull, av >= 32);
+      const int pick = full ? __ffs(full) - 1
+                            : 7 - int(__reduce_max_sync(kFull, lane < kRings ? (uint32_t(av) << 3) | uint32_t(7 - lane)
+                                                                             : 0u) &
+                                      7u);
+      const int pav = __shfl_sync(kFull, av, pick);
+      if (pav > 0) {
+        const int take = min(pav, 32);
+        int ok = 0;
+        if (lane == pick) ok = atomicCAS(&R.head[pick], hh, hh + uint32_t(take)) == hh;
+        if (__shfl_sync(kFull, ok, pick)) {
+          ring = pick;
+          h = __shfl_sync(kFull, hh, pick);
+          n = take;
+          break;
+        }
+        continue;   // another warp took them first
+      }
+      if (__shfl_sync(kFull, *vlive, 0) == 0) break;
+      // the rings are empty while other warps hold slots: wait for their pushes
+      if (!waited) {
+        t0 = clock64();
+        waited = true;
+      } else if (clock64() - t0 > kWaitCycles) {
+        gaveUp = true;
+        break;
+      }
+      __nanosleep(128);
+    }
+    if (ring < 0) break;
+    int k = 0;
+    bool have = lane < n;
+    if (have) {
+      const uint32_t pos = h + uint32_t(lane);
+      uint16_t* c = &R.cell[ring][pos & kCellSlot];
+      uint32_t v;
+      if (CellWait(c, CellFull(pos), ~kCellSlot, v)) {
+        k = int(v & kCellSlot);
+        CellStore(c, CellEmpty(pos + kSlots));
+      } else {
+        have = false;
+        gaveUp = true;
+      }
+    }
+    if (__any_sync(kFull, gaveUp)) {
+      gaveUp = true;
+      break;
+    }
+    bool live = have;
+    switch (ring) {   // the same on every lane
+      case kRHinge:
+        if (have) EventHinge(a, jobs, S, k);
+        break;
+      case kRMscEnd:
+        if (have) EventMscEnd(a, et, jobs, S, k);
+        break;
+      case kRBrem:
+        if (have) live = EventBrem<AGG>(a, jobs, S, k, dacc);
+        break;
+      case kRMoller:
+        if (have) EventMoller(a, et, jobs, S, k);
+        break;
+      case kRIdle:
+        live = false;
+        if (have && *vexh == 0) {
+          // one claim on the work counter per warp
+          cg::coalesced_group g = cg::coalesced_threads();
+          unsigned long long base = 0;
+          if (g.thread_rank() == 0) base = atomicAdd(a.head, (unsigned long long)g.size());
+          base = g.shfl(base, 0);
+          const unsigned long long item = base + g.thread_rank();
+          if (base + g.size() >= total) *vexh = 1;
+          if (item < total) live = RefillSlot(a, et, jobs, spre, S, k, item, esc);
+        }
+        break;
+      default:
+        break;
+    }
+    const int code = live ? StepSlot<AGG>(a, et, jobs, S, k, esc, nsteps, dacc) : 5;
+    // the ring of the slot's next action; a finished slot goes back to the
+    // idle ring while there is work left, else it retires (q == kRings)
+    int q = -1;
+    if (have) {
+      q = int((kRingOfCode >> (4 * code)) & 15u);
+      if (q == kRIdle && *vexh != 0) q = kRings;
+    }
+    const unsigned grp = __match_any_sync(kFull, q);
+    const int leader = __ffs(grp) - 1;
+    uint32_t base = 0;
+    if (lane == leader && q >= 0) {
+      if (q < kRings) base = atomicAdd(&R.tail[q], uint32_t(__popc(grp)));
+      else atomicSub(&R.live, __popc(grp));
+    }
+    base = __shfl_sync(kFull, base, leader);
+    if (q >= 0 && q < kRings) {
+      const uint32_t pos = base + uint32_t(__popc(grp & ((1u << lane) - 1u)));
+      uint16_t* c = &R.cell[q][pos & kCellSlot];
+      uint32_t v;
+      if (CellWait(c, CellEmpty(pos), 0xffffu, v)) CellStore(c, CellFull(pos) | uint32_t(k));
+      else gaveUp = true;
+    }
+    if (__any_sync(kFull, gaveUp)) {
+      gaveUp = true;
+      break;
+    }
+  }
+  // a warp that gave up a wait leaves electrons unfinished: reported
+  if (gaveUp && lane == 0) atomicAdd(a.fault, 1ull);
+  esc.Flush(jobs);
+  DepthAccFlush(a, jobs, dacc);
+  for (int o = 16; o > 0; o >>= 1) nsteps += __shfl_down_sync(kFull, nsteps, o);
+  if (lane == 0 && a.njobs > 0) atomicAdd(&a.jobs[0].cnt->steps, nsteps);
+}
+
+// ---------------------------------------------------------------------------
 // photon phase, block-batched: kPSlots photons per block live in shared
 // memory with their random-number state; every iteration each slot runs its
 // pending interaction (Compton or pair, over a compacted list) or its refill,
@@ -2061,6 +2300,11 @@ int BlockPhaseBlocksPerSM() { return kBlockMinBlocks; }
 
 cudaError_t PrepareBlockPhase(const DevTables<float>& T) {
   const int smem = BlockPhaseSmemBytes(T);
+  if (kRingScheduler) {
+    cudaError_t e = cudaFuncSetAttribute(ElectronPhaseR<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(ElectronPhaseR<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  }
   cudaError_t e = cudaFuncSetAttribute(ElectronPhaseB<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(ElectronPhaseB<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
@@ -2068,8 +2312,14 @@ cudaError_t PrepareBlockPhase(const DevTables<float>& T) {
 
 cudaError_t LaunchElectronPhaseBlock(const PhaseArgs& a, int blocks, cudaStream_t st) {
   const size_t smem = BlockPhaseSmemBytesFor(a.T, a.depthBins);
-  if (a.aggregate) ElectronPhaseB<1><<<blocks, 256, smem, st>>>(a);
-  else ElectronPhaseB<0><<<blocks, 256, smem, st>>>(a);
+  if (kRingScheduler) {
+    if (a.aggregate) ElectronPhaseR<1><<<blocks, 256, smem, st>>>(a);
+    else ElectronPhaseR<0><<<blocks, 256, smem, st>>>(a);
+  } else if (a.aggregate) {
+    ElectronPhaseB<1><<<blocks, 256, smem, st>>>(a);
+  } else {
+    ElectronPhaseB<0><<<blocks, 256, smem, st>>>(a);
+  }
   return cudaGetLastError();
 }
 
