@@ -4,11 +4,13 @@
 // transported in two phases: all photons (Woodcock tracking), then all
 // electrons/positrons (condensed-history stepping). Each phase is one
 // persistent launch, in one of two forms:
-//  * block-batched (the default): a block keeps 512 particles in shared
-//    memory; every iteration each particle runs its pending interaction, over
-//    a list compacted by interaction type so that a warp runs one kind at a
-//    time, or is refilled from the phase's work counter, and then takes one
-//    step (ElectronPhaseB, PhotonPhaseB);
+//  * block-batched (the default): a block keeps a few hundred particles in shared
+//    memory; each particle runs its pending interaction, grouped by
+//    interaction type so that a warp runs one kind at a time, or is refilled
+//    from the phase's work counter, and then takes one step. Electrons wait
+//    in per-type rings that warps take from whenever they are free
+//    (ElectronPhaseB); photons move in block-wide iterations over compacted
+//    lists (PhotonPhaseB);
 //  * one particle per lane, refilled from the work counter when it ends
 //    (ElectronPhase, PhotonPhase).
 // Secondaries are appended to the next generation's queues with
@@ -958,12 +960,26 @@ __global__ void __launch_bounds__(256) ElectronPhase(PhaseArgs a) {
 
 // ---------------------------------------------------------------------------
 // electron phase, block-batched: kSlots electrons per block live in shared
-// memory; every iteration of the block refills idle slots, advances every
-// active electron by one condensed-history sub-step (all threads), and then
-// runs each kind of interaction over a compacted list of the electrons that
-// reached it, so that the code of one interaction runs with full warps.
+// memory, each waiting in one of six rings (shared memory) by what it does
+// next: MSC hinge, MSC step end, brem, Moller, plain sub-step or refill. A
+// warp takes up to 32 entries of one ring whenever it is free, runs that
+// interaction (or the refill) and one condensed-history sub-step on them, and
+// puts each slot on the ring of its next action. The code of one interaction
+// thus runs with full warps, and no warp waits for another between sub-steps.
+// A particle's history does not depend on this order: every particle draws
+// from its own random stream.
+//
+// A ring has kRingSize (512) cells, at least one per slot, and two counters
+// (head: entries taken, tail: entries reserved); every slot is on at most one
+// ring, so no ring holds more than kSlots entries. The cell of position pos
+// holds (lap << 10 | full << 9 | slot) with lap = pos / 512 mod 64, the
+// bounded-queue scheme of D. Vyukov: a producer waits until its cell is empty
+// for its lap, a consumer until it is full for its lap, so neither can take
+// the other lap's entry. At most one operation of each warp is pending on a
+// cell, so a cell never lags its newest reservation by more than 8 laps and 6
+// bits tell the laps apart.
 // ---------------------------------------------------------------------------
-constexpr int kSlots = 512;
+constexpr int kSlots = 416;   // 3 blocks leave the SM 164 KB of shared memory and the rest to L1
 constexpr int kBlockMinBlocks = 3;      // resident blocks per SM the kernel is compiled for
 constexpr bool kTablesInSmem = false;  // electron tables staged per block, else read through L1
 constexpr bool kCacheMaterial = true;  // a slot keeps its voxel's material: read once per voxel entered
@@ -978,81 +994,173 @@ struct SlotArrays {     // shared-memory state of the resident electrons
   double acc[kSlots];
   int8_t mat[kSlots];       // material of the slot's current voxel (-1: vacuum)
 };
-// The block's slots form kSets sets with their own lists. With two sets the
-// warps alternate between them: when a warp has no more items of one set's
-// iteration it signals that set's split-phase barrier and goes on to the other
-// set, and waits for the first set's iteration to complete only when it comes
-// back to it, so the wait for the slowest warp of an iteration overlaps with
-// work. With one set the iteration ends at a block barrier.
-constexpr int kSets = 1;   // two sets measured slower: shorter lists, less uniform warps
-constexpr int kSetSlots = kSlots / kSets;
 constexpr long long kWaitCycles = 4LL << 30;   // bound of one wait (~2 s): then the block gives up
-// Every slot of a set sits in exactly one of six lists, by what it does
-// next: MSC hinge, MSC step end, brem, Moller, plain sub-step, idle. The lists
-// share three arrays (one kind filled from the front, one from the back) and
-// are double-buffered: an iteration reads one buffer and fills the other.
-// Their counts rotate over three sets, so that the set an iteration reads, the
-// set it fills and the set it clears for the next iteration are never the same
-// and one barrier per iteration suffices.
-// (kLClaim: the iteration's item counter, from which warps claim items)
-enum : int { kLHinge, kLMscEnd, kLBrem, kLMoller, kLStep, kLIdle, kLExhausted, kLClaim, kLCounts = 8 };
-struct SlotLists {
-  uint16_t ev[2][kSetSlots];    // hinge from the front, MSC step end from the back
-  uint16_t ia[2][kSetSlots];    // brem from the front, Moller from the back
-  uint16_t run[2][kSetSlots];   // plain sub-step from the front, idle from the back
-  int cnt[3][kLCounts];
+constexpr int kRingBits = 9;
+constexpr int kRingSize = 1 << kRingBits;   // cells per ring: at least the slots of a block
+constexpr uint32_t kCellSlot = uint32_t(kRingSize) - 1u, kCellFull = uint32_t(kRingSize);
+
+template <int NR>
+struct Rings {
+  uint16_t cell[NR][kRingSize];
+  unsigned int head[NR], tail[NR];
+  int live;        // slots not retired: queued or held by a warp
+  int exhausted;   // every work item of the generation has been claimed
 };
 
-__host__ __device__ constexpr size_t BlockPhaseStaticBytes() {
-  return sizeof(SlotArrays) + kSets * sizeof(SlotLists);
+__device__ __forceinline__ uint32_t CellEmpty(uint32_t pos) { return ((pos >> kRingBits) & 63u) << (kRingBits + 1); }
+__device__ __forceinline__ uint32_t CellFull(uint32_t pos) { return CellEmpty(pos) | kCellFull; }
+
+__device__ __forceinline__ uint32_t CellLoad(const uint16_t* c) {
+  uint16_t v;
+  asm volatile("ld.acquire.cta.shared::cta.u16 %0, [%1];"
+               : "=h"(v)
+               : "r"(uint32_t(__cvta_generic_to_shared(c)))
+               : "memory");
+  return v;
+}
+// publishes a cell: the slot's state written before it is visible to the
+// warp that loads the cell
+__device__ __forceinline__ void CellStore(uint16_t* c, uint32_t v) {
+  asm volatile("st.release.cta.shared::cta.u16 [%0], %1;" ::"r"(uint32_t(__cvta_generic_to_shared(c))),
+               "h"(uint16_t(v))
+               : "memory");
+}
+// waits until (cell & m) == want; false after kWaitCycles
+__device__ __forceinline__ bool CellWait(const uint16_t* c, uint32_t want, uint32_t m, uint32_t& v) {
+  v = CellLoad(c);
+  if ((v & m) == want) return true;
+  const long long t0 = clock64();
+  for (;;) {
+    __nanosleep(32);
+    v = CellLoad(c);
+    if ((v & m) == want) return true;
+    if (clock64() - t0 > kWaitCycles) return false;
+  }
 }
 
-// dynamic shared memory of the block kernel: slots, lists, the electron tables
+// slots 0 .. nslots - 1 on ring `idle` (lap 0, full), every other cell empty
+// for lap 0; before a barrier
+template <int NR>
+__device__ __forceinline__ void RingsInit(Rings<NR>& R, int idle, int nslots) {
+  for (int i = threadIdx.x; i < NR * kRingSize; i += blockDim.x) {
+    const int r = i / kRingSize, k = i % kRingSize;
+    R.cell[r][k] = uint16_t(r == idle && k < nslots ? (kCellFull | uint32_t(k)) : 0u);
+  }
+  if (threadIdx.x < NR) {
+    R.head[threadIdx.x] = 0u;
+    R.tail[threadIdx.x] = int(threadIdx.x) == idle ? unsigned(nslots) : 0u;
+  }
+  if (threadIdx.x == 0) {
+    R.live = nslots;
+    R.exhausted = 0;
+  }
+}
+
+// the calling warp (all lanes) takes up to 32 entries of the fullest ring
+// (the longest wait, and the fullest warps). Returns the ring, with
+// the slot of each lane < n in k, or -1 when no slot is queued or live (done)
+// or a wait gave up (gaveUp set).
+template <int NR>
+__device__ __forceinline__ int RingTake(Rings<NR>& R, int lane, int& n, int& k, bool& gaveUp) {
+  static_assert(NR <= 6, "ring index packed in 3 bits");
+  volatile unsigned int* vhead = R.head;
+  volatile unsigned int* vtail = R.tail;
+  int ring = -1;
+  uint32_t h = 0;
+  long long t0 = 0;
+  bool waited = false;
+  n = 0;
+  for (;;) {
+    uint32_t hh = 0;
+    int av = 0;
+    if (lane < NR) {
+      hh = vhead[lane];
+      av = int(vtail[lane] - hh);
+    }
+    // the fullest ring; of equally full ones, the first
+    const int pick =
+        7 - int(__reduce_max_sync(kFull, lane < NR ? (uint32_t(av) << 3) | uint32_t(7 - lane) : 0u) & 7u);
+    const int pav = __shfl_sync(kFull, av, pick);
+    if (pav > 0) {
+      const int take = min(pav, 32);
+      int ok = 0;
+      if (lane == pick) ok = atomicCAS(&R.head[pick], hh, hh + uint32_t(take)) == hh;
+      if (__shfl_sync(kFull, ok, pick)) {
+        ring = pick;
+        h = __shfl_sync(kFull, hh, pick);
+        n = take;
+        break;
+      }
+      continue;   // another warp took them first
+    }
+    if (__shfl_sync(kFull, *(volatile int*)&R.live, 0) == 0) return -1;
+    // the rings are empty while other warps hold slots: wait for their puts
+    if (!waited) {
+      t0 = clock64();
+      waited = true;
+    } else if (clock64() - t0 > kWaitCycles) {
+      gaveUp = true;
+      return -1;
+    }
+    __nanosleep(128);
+  }
+  bool bad = false;
+  if (lane < n) {
+    const uint32_t pos = h + uint32_t(lane);
+    uint16_t* c = &R.cell[ring][pos & kCellSlot];
+    uint32_t v;
+    if (CellWait(c, CellFull(pos), ~kCellSlot, v)) {
+      k = int(v & kCellSlot);
+      CellStore(c, CellEmpty(pos + kRingSize));
+    } else {
+      bad = true;
+    }
+  }
+  if (__any_sync(kFull, bad)) {
+    gaveUp = true;
+    return -1;
+  }
+  return ring;
+}
+
+// the calling warp (all lanes) puts slot k on ring q (q == NR: the slot
+// retires; q < 0: nothing to put); one reservation per ring and warp
+template <int NR>
+__device__ __forceinline__ void RingPut(Rings<NR>& R, int lane, int q, int k, bool& gaveUp) {
+  const unsigned grp = __match_any_sync(kFull, q);
+  const int leader = __ffs(grp) - 1;
+  uint32_t base = 0;
+  if (lane == leader && q >= 0) {
+    if (q < NR) base = atomicAdd(&R.tail[q], uint32_t(__popc(grp)));
+    else atomicSub(&R.live, __popc(grp));
+  }
+  base = __shfl_sync(kFull, base, leader);
+  bool bad = false;
+  if (q >= 0 && q < NR) {
+    const uint32_t pos = base + uint32_t(__popc(grp & ((1u << lane) - 1u)));
+    uint16_t* c = &R.cell[q][pos & kCellSlot];
+    uint32_t v;
+    if (CellWait(c, CellEmpty(pos), 0xffffu, v)) CellStore(c, CellFull(pos) | uint32_t(k));
+    else bad = true;
+  }
+  if (__any_sync(kFull, bad)) gaveUp = true;
+}
+
+// electron rings (of equally full rings the first is taken)
+enum : int { kRBrem, kRMoller, kRHinge, kRMscEnd, kRIdle, kRStep, kRings };
+static_assert(kSlots <= kRingSize, "a ring holds every slot");
+// ring of a sub-step's result code (0 step, 1 brem, 2 Moller, 3 hinge, 4 MSC
+// step end, 5 finished), four bits per code
+constexpr uint32_t kRingOfCode = 0x432105u;
+using SlotRings = Rings<kRings>;
+
+__host__ __device__ constexpr size_t BlockPhaseStaticBytes() { return sizeof(SlotArrays) + sizeof(SlotRings); }
+
+// dynamic shared memory of the block kernel: slots, rings, the electron tables
 // when staged, then the depth tally of `depthBins` bins
 __host__ __device__ inline size_t BlockPhaseSmemBytesFor(const DevTables<float>& T, int depthBins) {
   const size_t b = BlockPhaseStaticBytes() + (kTablesInSmem ? size_t(T.elecCount) * sizeof(float) : 0);
   return ((b + 15) & ~size_t(15)) + DepthAccBytes(depthBins);
-}
-
-// warp-aggregated push of v onto a set's list, from its front or its back
-__device__ __forceinline__ void Push(uint16_t* list, int* n, int v, bool back) {
-  cg::coalesced_group g = cg::coalesced_threads();
-  int base = 0;
-  if (g.thread_rank() == 0) base = atomicAdd(n, int(g.size()));
-  const int pos = g.shfl(base, 0) + int(g.thread_rank());
-  list[back ? kSetSlots - 1 - pos : pos] = uint16_t(v);
-}
-
-// split-phase barrier of a slot set: an mbarrier in shared memory that
-// completes a phase when every warp of the block has arrived once
-__device__ __forceinline__ void SetBarrierInit(uint64_t* bar, int warps) {
-  asm volatile("mbarrier.init.shared.b64 [%0], %1;" ::"r"(uint32_t(__cvta_generic_to_shared(bar))), "r"(warps)
-               : "memory");
-}
-// one arrival per warp (lane 0, after the warp's writes to the set)
-__device__ __forceinline__ void SetBarrierArrive(uint64_t* bar) {
-  __syncwarp();
-  if ((threadIdx.x & 31) == 0)
-    asm volatile("{ .reg .b64 st; mbarrier.arrive.shared.b64 st, [%0]; }" ::"r"(
-                     uint32_t(__cvta_generic_to_shared(bar)))
-                 : "memory");
-  __syncwarp();
-}
-// waits until phase `phase` of the barrier has completed; false after
-// kWaitCycles (the caller then abandons the phase and reports it)
-__device__ __forceinline__ bool SetBarrierWait(uint64_t* bar, int phase) {
-  const uint32_t addr = uint32_t(__cvta_generic_to_shared(bar));
-  const long long t0 = clock64();
-  for (;;) {
-    uint32_t ok = 0;
-    asm volatile(
-        "{ .reg .pred p; mbarrier.try_wait.parity.shared.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
-        : "=r"(ok)
-        : "r"(addr), "r"(uint32_t(phase & 1))
-        : "memory");
-    if (ok) return true;
-    if (clock64() - t0 > kWaitCycles) return false;
-  }
 }
 
 __device__ __forceinline__ void LoadSlot(const SlotArrays& S, int k, PState& p, EState& s, uint32_t& fl) {
@@ -1427,7 +1535,7 @@ template <int AGG>
 __global__ void __launch_bounds__(256, kBlockMinBlocks) ElectronPhaseB(PhaseArgs a) {
   extern __shared__ __align__(16) unsigned char dyn[];
   SlotArrays& S = *reinterpret_cast<SlotArrays*>(dyn);
-  SlotLists* Lg = reinterpret_cast<SlotLists*>(dyn + sizeof(SlotArrays));
+  SlotRings& R = *reinterpret_cast<SlotRings*>(dyn + sizeof(SlotArrays));
   float* sdata = reinterpret_cast<float*>(dyn + BlockPhaseStaticBytes());
   __shared__ ETables et;
   __shared__ JobF sjobs[16];
@@ -1443,289 +1551,18 @@ __global__ void __launch_bounds__(256, kBlockMinBlocks) ElectronPhaseB(PhaseArgs
   if (kTablesInSmem) StageElectronTables(a.T, sdata, &et);
   else if (threadIdx.x == 0) BindElectronTables(a.T, &et);   // visible after the barrier below
   const int tid = threadIdx.x, lane = tid & 31;
-  __shared__ __align__(8) uint64_t setBar[kSets];
-  // all slots start idle
-  for (int k = tid; k < kSlots; k += blockDim.x) {
-    S.flags[k] = 0u;
-    Lg[k / kSetSlots].run[0][kSetSlots - 1 - k % kSetSlots] = uint16_t(k);
-  }
-  for (int c = tid; c < kSets * 3 * kLCounts; c += blockDim.x) {
-    const int j = c % (3 * kLCounts);
-    (&Lg[c / (3 * kLCounts)].cnt[0][0])[j] = (j == kLIdle) ? kSetSlots : 0;
-  }
-  if (kSets > 1 && tid == 0)
-    for (int st = 0; st < kSets; ++st) SetBarrierInit(&setBar[st], int(blockDim.x >> 5));
-  __syncthreads();
-  EscTally esc;
-  unsigned long long nsteps = 0;
-  // per set: iteration (its list buffer is it & 1), count set read, still running
-  int it0 = 0, it1 = 0, cr0 = 0, cr1 = 0;
-  bool run0 = true, run1 = kSets > 1, gaveUp = false;
-  while ((run0 || run1) && !gaveUp) {
-#pragma unroll 1
-    for (int st = 0; st < kSets; ++st) {
-      if (!(st ? run1 : run0)) continue;
-      const int itS = st ? it1 : it0;
-      // the set's previous iteration must be complete on every warp
-      if (kSets > 1 && itS > 0 && !SetBarrierWait(&setBar[st], itS - 1)) {
-        gaveUp = true;
-        break;
-      }
-      SlotLists& L = Lg[st];
-      const int lr = itS & 1, lw = lr ^ 1;
-      const int cr = st ? cr1 : cr0, cw = cr == 2 ? 0 : cr + 1, cz = cw == 2 ? 0 : cw + 1;
-      const int* nr = L.cnt[cr];
-      int* nw = L.cnt[cw];
-      const int e0 = nr[kLHinge], e1 = e0 + nr[kLMscEnd], e2 = e1 + nr[kLBrem], e3 = e2 + nr[kLMoller],
-                e4 = e3 + nr[kLStep];
-      const bool exhausted = nr[kLExhausted] != 0;
-      if (e4 == 0 && exhausted) {   // the same decision on every warp (same counts)
-        if (st) run1 = false; else run0 = false;
-        continue;
-      }
-      if (tid == 0) {
-        for (int c = 0; c < kLCounts; ++c) L.cnt[cz][c] = 0;
-        if (exhausted) nw[kLExhausted] = 1;
-      }
-      // each slot once: its pending interaction or its refill, then one
-      // sub-step; a warp claims 32 items at a time, so warps that finish
-      // early take more
-      for (;;) {
-        int b = 0;
-        if (lane == 0) b = atomicAdd(&L.cnt[cr][kLClaim], 32);
-        const int claimed = __shfl_sync(kFull, b, 0);
-        // no more work: the idle slots stay idle without being visited
-        if (claimed >= (exhausted ? e4 : kSetSlots)) break;
-        const int i = claimed + lane;
-        if (exhausted && i >= e4) continue;
-        int k;
-        bool live = true;
-        if (i < e4) {
-          if (i < e0) {
-            k = L.ev[lr][i];
-            EventHinge(a, jobs, S, k);
-          } else if (i < e1) {
-            k = L.ev[lr][kSetSlots - 1 - (i - e0)];
-            EventMscEnd(a, et, jobs, S, k);
-          } else if (i < e2) {
-            k = L.ia[lr][i - e1];
-            live = EventBrem<AGG>(a, jobs, S, k, dacc);
-          } else if (i < e3) {
-            k = L.ia[lr][kSetSlots - 1 - (i - e2)];
-            EventMoller(a, et, jobs, S, k);
-          } else {
-            k = L.run[lr][i - e3];
-          }
-        } else {
-          k = L.run[lr][kSetSlots - 1 - (i - e4)];
-          live = false;
-          if (!exhausted) {
-            // one claim on the work counter per warp
-            cg::coalesced_group g = cg::coalesced_threads();
-            unsigned long long base = 0;
-            if (g.thread_rank() == 0) base = atomicAdd(a.head, (unsigned long long)g.size());
-            base = g.shfl(base, 0);
-            const unsigned long long item = base + g.thread_rank();
-            if (base + g.size() >= total) nw[kLExhausted] = 1;
-            if (item < total) live = RefillSlot(a, et, jobs, spre, S, k, item, esc);
-          }
-        }
-        const int code = live ? StepSlot<AGG>(a, et, jobs, S, k, esc, nsteps, dacc) : 5;
-        switch (code) {
-          case 0: Push(L.run[lw], &nw[kLStep], k, false); break;
-          case 1: Push(L.ia[lw], &nw[kLBrem], k, false); break;
-          case 2: Push(L.ia[lw], &nw[kLMoller], k, true); break;
-          case 3: Push(L.ev[lw], &nw[kLHinge], k, false); break;
-          case 4: Push(L.ev[lw], &nw[kLMscEnd], k, true); break;
-          default: Push(L.run[lw], &nw[kLIdle], k, true); break;
-        }
-      }
-      if (kSets > 1) SetBarrierArrive(&setBar[st]);
-      else __syncthreads();
-      if (st) { cr1 = cw; ++it1; } else { cr0 = cw; ++it0; }
-    }
-  }
-  // a block that gave up a wait leaves its electrons unfinished: reported
-  if (gaveUp && lane == 0) atomicAdd(a.fault, 1ull);
-  esc.Flush(jobs);
-  DepthAccFlush(a, jobs, dacc);
-  for (int o = 16; o > 0; o >>= 1) nsteps += __shfl_down_sync(kFull, nsteps, o);
-  if ((tid & 31) == 0 && a.njobs > 0) atomicAdd(&a.jobs[0].cnt->steps, nsteps);
-}
-
-// ---------------------------------------------------------------------------
-// electron phase, ring-scheduled: the slots of ElectronPhaseB without the
-// block's iterations. Every slot waits in one of six rings (shared memory) by
-// what it does next; a warp takes up to 32 entries of one ring whenever it is
-// free, runs that interaction (or the refill) and one sub-step on them, and
-// puts each slot on the ring of its next action. No warp waits for another
-// between sub-steps, and the 32 slots a warp takes run the same interaction.
-// A particle's histories do not depend on this order: every particle draws
-// from its own random stream.
-//
-// A ring has kSlots cells and two counters (head: entries taken, tail:
-// entries reserved). The cell of position pos holds (lap << 10 | full << 9 |
-// slot) with lap = pos / kSlots mod 64, the bounded-queue scheme of D. Vyukov:
-// a producer waits until its cell is empty for its lap, a consumer until it is
-// full for its lap, so neither can take the other lap's entry. At most one
-// operation of each warp is pending on a cell, so a cell never lags its
-// newest reservation by more than 8 laps and 6 bits tell the laps apart.
-// ---------------------------------------------------------------------------
-constexpr bool kRingScheduler = true;   // ElectronPhaseR, else ElectronPhaseB
-enum : int { kRBrem, kRMoller, kRHinge, kRMscEnd, kRIdle, kRStep, kRings };   // in the order rings are preferred
-constexpr int kRingBits = 9;
-static_assert((1 << kRingBits) == kSlots, "one ring cell per slot");
-static_assert(kSets == 1, "one slot set");
-constexpr uint32_t kCellSlot = (1u << kRingBits) - 1u, kCellFull = 1u << kRingBits;
-// ring of a sub-step's result code (0 step, 1 brem, 2 Moller, 3 hinge, 4 MSC
-// step end, 5 finished), four bits per code
-constexpr uint32_t kRingOfCode = 0x432105u;
-
-struct SlotRings {
-  uint16_t cell[kRings][kSlots];
-  unsigned int head[kRings], tail[kRings];
-  int live;        // slots not retired: queued or held by a warp
-  int exhausted;   // every work item of the generation has been claimed
-};
-
-__device__ __forceinline__ uint32_t CellEmpty(uint32_t pos) { return ((pos >> kRingBits) & 63u) << (kRingBits + 1); }
-__device__ __forceinline__ uint32_t CellFull(uint32_t pos) { return CellEmpty(pos) | kCellFull; }
-
-__device__ __forceinline__ uint32_t CellLoad(const uint16_t* c) {
-  uint16_t v;
-  asm volatile("ld.acquire.cta.shared::cta.u16 %0, [%1];"
-               : "=h"(v)
-               : "r"(uint32_t(__cvta_generic_to_shared(c)))
-               : "memory");
-  return v;
-}
-// publishes a cell: the slot's state written before it is visible to the
-// warp that loads the cell
-__device__ __forceinline__ void CellStore(uint16_t* c, uint32_t v) {
-  asm volatile("st.release.cta.shared::cta.u16 [%0], %1;" ::"r"(uint32_t(__cvta_generic_to_shared(c))),
-               "h"(uint16_t(v))
-               : "memory");
-}
-// waits until (cell & m) == want; false after kWaitCycles
-__device__ __forceinline__ bool CellWait(const uint16_t* c, uint32_t want, uint32_t m, uint32_t& v) {
-  v = CellLoad(c);
-  if ((v & m) == want) return true;
-  const long long t0 = clock64();
-  for (;;) {
-    __nanosleep(32);
-    v = CellLoad(c);
-    if ((v & m) == want) return true;
-    if (clock64() - t0 > kWaitCycles) return false;
-  }
-}
-
-__host__ __device__ constexpr size_t RingPhaseStaticBytes() { return sizeof(SlotArrays) + sizeof(SlotRings); }
-static_assert(sizeof(SlotRings) <= kSets * sizeof(SlotLists), "the rings fit where the lists are");
-
-template <int AGG>
-__global__ void __launch_bounds__(256, kBlockMinBlocks) ElectronPhaseR(PhaseArgs a) {
-  extern __shared__ __align__(16) unsigned char dyn[];
-  SlotArrays& S = *reinterpret_cast<SlotArrays*>(dyn);
-  SlotRings& R = *reinterpret_cast<SlotRings*>(dyn + sizeof(SlotArrays));
-  float* sdata = reinterpret_cast<float*>(dyn + RingPhaseStaticBytes());
-  __shared__ ETables et;
-  __shared__ JobF sjobs[16];
-  __shared__ unsigned long long spre[kStripes + 1];
-  const bool fewJobs = a.njobs <= 16;
-  if (fewJobs)
-    for (int j = threadIdx.x; j < a.njobs; j += blockDim.x) sjobs[j] = a.jobs[j];
-  const DepthAcc dacc = DepthAccInit(a, dyn + BlockPhaseSmemBytesFor(a.T, 0));
-  const unsigned long long nQ = StripePrefix(a.inCount, spre);
-  const JobF* jobs = fewJobs ? sjobs : a.jobs;
-  const unsigned long long total = (unsigned long long)a.nPrimaries + nQ;
-  if (total == 0) return;   // an empty generation skips the table staging
-  if (kTablesInSmem) StageElectronTables(a.T, sdata, &et);
-  else if (threadIdx.x == 0) BindElectronTables(a.T, &et);   // visible after the barrier below
-  const int tid = threadIdx.x, lane = tid & 31;
-  // every slot starts on the idle ring (lap 0, full); the other rings are empty
-  for (int i = tid; i < kRings * kSlots; i += blockDim.x) {
-    const int r = i / kSlots, k = i % kSlots;
-    R.cell[r][k] = uint16_t(r == kRIdle ? (kCellFull | uint32_t(k)) : 0u);
-  }
+  RingsInit(R, kRIdle, kSlots);
   for (int k = tid; k < kSlots; k += blockDim.x) S.flags[k] = 0u;
-  if (tid < kRings) {
-    R.head[tid] = 0u;
-    R.tail[tid] = tid == kRIdle ? unsigned(kSlots) : 0u;
-  }
-  if (tid == 0) {
-    R.live = kSlots;
-    R.exhausted = 0;
-  }
   __syncthreads();
-  volatile unsigned int* vhead = R.head;
-  volatile unsigned int* vtail = R.tail;
-  volatile int* vlive = &R.live;
   volatile int* vexh = &R.exhausted;
   EscTally esc;
   unsigned long long nsteps = 0;
   bool gaveUp = false;
   for (;;) {
-    // take up to 32 entries: the first ring (in preference order) holding a
-    // full warp's worth, else the fullest; none queued and none live: done
-    int ring = -1, n = 0;
-    uint32_t h = 0;
-    long long t0 = 0;
-    bool waited = false;
-    for (;;) {
-      uint32_t hh = 0;
-      int av = 0;
-      if (lane < kRings) {
-        hh = vhead[lane];
-        av = int(vtail[lane] - hh);
-      }
-      const unsigned full = __ballot_sync(kFull, av >= 32);
-      const int pick = full ? __ffs(full) - 1
-                            : 7 - int(__reduce_max_sync(kFull, lane < kRings ? (uint32_t(av) << 3) | uint32_t(7 - lane)
-                                                                             : 0u) &
-                                      7u);
-      const int pav = __shfl_sync(kFull, av, pick);
-      if (pav > 0) {
-        const int take = min(pav, 32);
-        int ok = 0;
-        if (lane == pick) ok = atomicCAS(&R.head[pick], hh, hh + uint32_t(take)) == hh;
-        if (__shfl_sync(kFull, ok, pick)) {
-          ring = pick;
-          h = __shfl_sync(kFull, hh, pick);
-          n = take;
-          break;
-        }
-        continue;   // another warp took them first
-      }
-      if (__shfl_sync(kFull, *vlive, 0) == 0) break;
-      // the rings are empty while other warps hold slots: wait for their pushes
-      if (!waited) {
-        t0 = clock64();
-        waited = true;
-      } else if (clock64() - t0 > kWaitCycles) {
-        gaveUp = true;
-        break;
-      }
-      __nanosleep(128);
-    }
+    int n = 0, k = 0;
+    const int ring = RingTake(R, lane, n, k, gaveUp);
     if (ring < 0) break;
-    int k = 0;
-    bool have = lane < n;
-    if (have) {
-      const uint32_t pos = h + uint32_t(lane);
-      uint16_t* c = &R.cell[ring][pos & kCellSlot];
-      uint32_t v;
-      if (CellWait(c, CellFull(pos), ~kCellSlot, v)) {
-        k = int(v & kCellSlot);
-        CellStore(c, CellEmpty(pos + kSlots));
-      } else {
-        have = false;
-        gaveUp = true;
-      }
-    }
-    if (__any_sync(kFull, gaveUp)) {
-      gaveUp = true;
-      break;
-    }
+    const bool have = lane < n;
     bool live = have;
     switch (ring) {   // the same on every lane
       case kRHinge:
@@ -1764,25 +1601,8 @@ __global__ void __launch_bounds__(256, kBlockMinBlocks) ElectronPhaseR(PhaseArgs
       q = int((kRingOfCode >> (4 * code)) & 15u);
       if (q == kRIdle && *vexh != 0) q = kRings;
     }
-    const unsigned grp = __match_any_sync(kFull, q);
-    const int leader = __ffs(grp) - 1;
-    uint32_t base = 0;
-    if (lane == leader && q >= 0) {
-      if (q < kRings) base = atomicAdd(&R.tail[q], uint32_t(__popc(grp)));
-      else atomicSub(&R.live, __popc(grp));
-    }
-    base = __shfl_sync(kFull, base, leader);
-    if (q >= 0 && q < kRings) {
-      const uint32_t pos = base + uint32_t(__popc(grp & ((1u << lane) - 1u)));
-      uint16_t* c = &R.cell[q][pos & kCellSlot];
-      uint32_t v;
-      if (CellWait(c, CellEmpty(pos), 0xffffu, v)) CellStore(c, CellFull(pos) | uint32_t(k));
-      else gaveUp = true;
-    }
-    if (__any_sync(kFull, gaveUp)) {
-      gaveUp = true;
-      break;
-    }
+    RingPut(R, lane, q, k, gaveUp);
+    if (gaveUp) break;
   }
   // a warp that gave up a wait leaves electrons unfinished: reported
   if (gaveUp && lane == 0) atomicAdd(a.fault, 1ull);
@@ -1794,12 +1614,13 @@ __global__ void __launch_bounds__(256, kBlockMinBlocks) ElectronPhaseR(PhaseArgs
 
 // ---------------------------------------------------------------------------
 // photon phase, block-batched: kPSlots photons per block live in shared
-// memory with their random-number state; every iteration each slot runs its
-// pending interaction (Compton or pair, over a compacted list) or its refill,
-// then one Woodcock step. The uniforms are drawn in the order of PhotonPhase,
-// so both kernels give the same histories.
+// memory with their random-number state, each waiting on one of four rings
+// (Compton, pair, refill, plain step); a warp takes up to 32 slots of one ring,
+// runs that interaction or the refill, then one Woodcock step on them, as in
+// the electron phase. The uniforms are drawn in the order of PhotonPhase, so
+// both kernels give the same histories.
 // ---------------------------------------------------------------------------
-constexpr int kPSlots = 512;
+constexpr int kPSlots = 352;   // 4 blocks leave the SM 164 KB of shared memory and the rest to L1
 constexpr int kPBlockMinBlocks = 4;
 
 struct PSlotArrays {
@@ -1809,24 +1630,14 @@ struct PSlotArrays {
   uint32_t ctr[kPSlots], have[kPSlots], w0[kPSlots], w1[kPSlots], w2[kPSlots], w3[kPSlots];
   double acc[kPSlots];
 };
-// lists: Compton from the front and pair from the back of cp; plain steps from
-// the front and idle slots from the back of run; counts rotate as for electrons
-enum : int { kQComp, kQPair, kQStep, kQIdle, kQExhausted, kQClaim, kQCounts = 8 };
-struct PSlotLists {
-  uint16_t cp[2][kPSlots];
-  uint16_t run[2][kPSlots];
-  int cnt[3][kQCounts];
-};
+// photon rings (of equally full rings the first is taken)
+enum : int { kPRComp, kPRPair, kPRIdle, kPRStep, kPRings };
+static_assert(kPSlots <= kRingSize, "a ring holds every slot");
+// ring of a Woodcock step's result code (0 step, 1 Compton, 2 pair, 3 finished)
+constexpr uint32_t kPRingOfCode = 0x2103u;
+using PSlotRings = Rings<kPRings>;
 
-__host__ __device__ constexpr size_t PhotonBlockStaticBytes() { return sizeof(PSlotArrays) + sizeof(PSlotLists); }
-
-__device__ __forceinline__ void PushP(uint16_t* list, int* n, int v, bool back) {
-  cg::coalesced_group g = cg::coalesced_threads();
-  int base = 0;
-  if (g.thread_rank() == 0) base = atomicAdd(n, int(g.size()));
-  const int pos = g.shfl(base, 0) + int(g.thread_rank());
-  list[back ? kPSlots - 1 - pos : pos] = uint16_t(v);
-}
+__host__ __device__ constexpr size_t PhotonBlockStaticBytes() { return sizeof(PSlotArrays) + sizeof(PSlotRings); }
 
 __device__ __forceinline__ void LoadPhoton(const PSlotArrays& S, int k, const JobF* jobs, PState& p, PRng& rng) {
   const uint32_t v = S.vox[k];
@@ -2040,7 +1851,7 @@ template <int AGG>
 __global__ void __launch_bounds__(256, kPBlockMinBlocks) PhotonPhaseB(PhaseArgs a) {
   extern __shared__ __align__(16) unsigned char dyn[];
   PSlotArrays& S = *reinterpret_cast<PSlotArrays*>(dyn);
-  PSlotLists& L = *reinterpret_cast<PSlotLists*>(dyn + sizeof(PSlotArrays));
+  PSlotRings& R = *reinterpret_cast<PSlotRings*>(dyn + sizeof(PSlotArrays));
   __shared__ JobF sjobs[16];
   __shared__ unsigned long long spre[kStripes + 1];
   __shared__ PTables pt;
@@ -2054,67 +1865,46 @@ __global__ void __launch_bounds__(256, kPBlockMinBlocks) PhotonPhaseB(PhaseArgs 
   StagePhotonTables(a.T, false, nullptr, &pt);
   const DepthAcc dacc = DepthAccInit(a, dyn + ((PhotonBlockStaticBytes() + 15) & ~size_t(15)));
   const int tid = threadIdx.x, lane = tid & 31;
-  for (int k = tid; k < kPSlots; k += blockDim.x) L.run[0][kPSlots - 1 - k] = uint16_t(k);
-  for (int c = tid; c < 3 * kQCounts; c += blockDim.x) (&L.cnt[0][0])[c] = (c == kQIdle) ? kPSlots : 0;
+  RingsInit(R, kPRIdle, kPSlots);
   __syncthreads();
+  volatile int* vexh = &R.exhausted;
   EscTally esc;
   unsigned long long nph = 0;
-  int cr = 0, lr = 0;
+  bool gaveUp = false;
   for (;;) {
-    const int cw = cr == 2 ? 0 : cr + 1, cz = cw == 2 ? 0 : cw + 1, lw = lr ^ 1;
-    const int* nr = L.cnt[cr];
-    int* nw = L.cnt[cw];
-    const int e0 = nr[kQComp], e1 = e0 + nr[kQPair], e2 = e1 + nr[kQStep];
-    const bool exhausted = nr[kQExhausted] != 0;
-    if (e2 == 0 && exhausted) break;
-    if (tid == 0) {
-      for (int c = 0; c < kQCounts; ++c) L.cnt[cz][c] = 0;
-      if (exhausted) nw[kQExhausted] = 1;
-    }
-    for (;;) {
-      int b = 0;
-      if (lane == 0) b = atomicAdd(&L.cnt[cr][kQClaim], 32);
-      const int claimed = __shfl_sync(kFull, b, 0);
-      // no more work: the idle slots stay idle without being visited
-      if (claimed >= (exhausted ? e2 : kPSlots)) break;
-      const int i = claimed + lane;
-      if (exhausted && i >= e2) continue;
-      int k;
-      bool live = true;
-      if (i < e0) {
-        k = L.cp[lr][i];
-        live = PhotonComptonSlot<AGG>(a, jobs, S, k, dacc);
-      } else if (i < e1) {
-        k = L.cp[lr][kPSlots - 1 - (i - e0)];
-        PhotonPairSlot<AGG>(a, jobs, S, k, dacc);
-        live = false;
-      } else if (i < e2) {
-        k = L.run[lr][i - e1];
-      } else {
-        k = L.run[lr][kPSlots - 1 - (i - e2)];
-        live = false;
-        if (!exhausted) {
-          cg::coalesced_group g = cg::coalesced_threads();
-          unsigned long long base = 0;
-          if (g.thread_rank() == 0) base = atomicAdd(a.head, (unsigned long long)g.size());
-          base = g.shfl(base, 0);
-          const unsigned long long item = base + g.thread_rank();
-          if (base + g.size() >= total) nw[kQExhausted] = 1;
-          if (item < total) live = PhotonRefillSlot(a, jobs, spre, S, k, item, esc);
-        }
-      }
-      const int code = live ? PhotonStepSlot<AGG>(a, pt, jobs, S, k, esc, nph, dacc) : 3;
-      switch (code) {
-        case 0: PushP(L.run[lw], &nw[kQStep], k, false); break;
-        case 1: PushP(L.cp[lw], &nw[kQComp], k, false); break;
-        case 2: PushP(L.cp[lw], &nw[kQPair], k, true); break;
-        default: PushP(L.run[lw], &nw[kQIdle], k, true); break;
+    int n = 0, k = 0;
+    const int ring = RingTake(R, lane, n, k, gaveUp);
+    if (ring < 0) break;
+    const bool have = lane < n;
+    bool live = have;
+    if (ring == kPRComp) {
+      if (have) live = PhotonComptonSlot<AGG>(a, jobs, S, k, dacc);
+    } else if (ring == kPRPair) {
+      if (have) PhotonPairSlot<AGG>(a, jobs, S, k, dacc);
+      live = false;
+    } else if (ring == kPRIdle) {
+      live = false;
+      if (have && *vexh == 0) {
+        cg::coalesced_group g = cg::coalesced_threads();
+        unsigned long long base = 0;
+        if (g.thread_rank() == 0) base = atomicAdd(a.head, (unsigned long long)g.size());
+        base = g.shfl(base, 0);
+        const unsigned long long item = base + g.thread_rank();
+        if (base + g.size() >= total) *vexh = 1;
+        if (item < total) live = PhotonRefillSlot(a, jobs, spre, S, k, item, esc);
       }
     }
-    __syncthreads();
-    cr = cw;
-    lr = lw;
+    const int code = live ? PhotonStepSlot<AGG>(a, pt, jobs, S, k, esc, nph, dacc) : 3;
+    int q = -1;
+    if (have) {
+      q = int((kPRingOfCode >> (4 * code)) & 15u);
+      if (q == kPRIdle && *vexh != 0) q = kPRings;
+    }
+    RingPut(R, lane, q, k, gaveUp);
+    if (gaveUp) break;
   }
+  // a warp that gave up a wait leaves photons unfinished: reported
+  if (gaveUp && lane == 0) atomicAdd(a.fault, 1ull);
   esc.Flush(jobs);
   DepthAccFlush(a, jobs, dacc);
   for (int o = 16; o > 0; o >>= 1) nph += __shfl_down_sync(kFull, nph, o);
@@ -2300,11 +2090,6 @@ int BlockPhaseBlocksPerSM() { return kBlockMinBlocks; }
 
 cudaError_t PrepareBlockPhase(const DevTables<float>& T) {
   const int smem = BlockPhaseSmemBytes(T);
-  if (kRingScheduler) {
-    cudaError_t e = cudaFuncSetAttribute(ElectronPhaseR<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(ElectronPhaseR<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  }
   cudaError_t e = cudaFuncSetAttribute(ElectronPhaseB<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(ElectronPhaseB<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
@@ -2312,14 +2097,8 @@ cudaError_t PrepareBlockPhase(const DevTables<float>& T) {
 
 cudaError_t LaunchElectronPhaseBlock(const PhaseArgs& a, int blocks, cudaStream_t st) {
   const size_t smem = BlockPhaseSmemBytesFor(a.T, a.depthBins);
-  if (kRingScheduler) {
-    if (a.aggregate) ElectronPhaseR<1><<<blocks, 256, smem, st>>>(a);
-    else ElectronPhaseR<0><<<blocks, 256, smem, st>>>(a);
-  } else if (a.aggregate) {
-    ElectronPhaseB<1><<<blocks, 256, smem, st>>>(a);
-  } else {
-    ElectronPhaseB<0><<<blocks, 256, smem, st>>>(a);
-  }
+  if (a.aggregate) ElectronPhaseB<1><<<blocks, 256, smem, st>>>(a);
+  else ElectronPhaseB<0><<<blocks, 256, smem, st>>>(a);
   return cudaGetLastError();
 }
 
