@@ -490,7 +490,7 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
     if (outs[j].slab) outs[j].maxIz = hlast[j] > 0 ? int(hlast[j] - 1) : 0;
   }
   if (faults > 0)
-    return Fail(DPMX_ERR_CUDA, std::to_string(faults) + " blocks of the electron phase gave up a wait; run incomplete");
+    return Fail(DPMX_ERR_CUDA, std::to_string(faults) + " warps of a transport phase gave up a bounded wait; run incomplete");
   lost = leftover + overflowed;
   // losses of the queues are reported on job 0
   if (njobs > 0) outs[0].cnt.lost += lost;
