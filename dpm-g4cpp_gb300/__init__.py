@@ -127,6 +127,8 @@ def library():
         "dpmx_csr_spmv_t": (C.c_int, [P, C.c_void_p, C.c_void_p, C.c_void_p]),
         "dpmx_csr_download": (C.c_int, [P, C.c_void_p, C.c_void_p, C.c_void_p]),
         "dpmx_csr_free": (None, [P]),
+        "dpmx_ring_selftest": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_uint64, C.c_longlong,
+                                         C.POINTER(C.c_longlong)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -151,7 +153,7 @@ def exported_symbols():
             "dpmx_result_free", "dpmx_scratch_release", "dpmx_result_write", "dpmx_model_histogram",
             "dpmx_simulate", "dpmx_simulate_noalloc", "dpmx_write_hist", "dpmx_sampler_eval", "dpmx_table_eval", "dpmx_simulate_histories",
             "dpmx_influence_build", "dpmx_csr_shape", "dpmx_csr_device", "dpmx_csr_spmv", "dpmx_csr_spmv_t",
-            "dpmx_csr_download", "dpmx_csr_free"]
+            "dpmx_csr_download", "dpmx_csr_free", "dpmx_ring_selftest"]
 
 
 class Tables:
@@ -418,6 +420,15 @@ def read_dose_raw(path):
     head = dict(nx=int(nx), ny=int(ny), nz=int(nz), voxel_mm=(vx, vy, vz), origin_mm=(x0, y0, z0),
                 histories=int(hist), batches=int(batches))
     return dose, rel, head
+
+
+def ring_selftest(blocks=152, nslots=416, rounds=1000, seed=1, probe_cycles=1 << 20):
+    """Runs the slot-ring self-test on the GPU (dpmx_ring_selftest): returns
+    (slots taken, slots taken a wrong number of times, warps that gave up a
+    wait, blocks whose probe wait on a never-filled cell ran out)."""
+    out = (C.c_longlong * 4)()
+    _check(library().dpmx_ring_selftest(int(blocks), int(nslots), int(rounds), int(seed), int(probe_cycles), out))
+    return tuple(int(v) for v in out)
 
 
 def scratch_release():

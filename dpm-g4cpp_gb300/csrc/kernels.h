@@ -152,6 +152,11 @@ cudaError_t LaunchSamplerEval32(const DevTables<float>& T, int s, int imat, cons
                                 double* out, int n, cudaStream_t st);
 cudaError_t LaunchTableEval32(const DevTables<float>& T, int q, int imat, const double* e, double* out, int n,
                               cudaStream_t st);
+// self-test of the block kernels' slot rings; out[4] (device, zeroed):
+// visits, slots with a wrong visit count, warps that gave up, probe waits that
+// ran out (one per block expected)
+cudaError_t LaunchRingSelfTest(int blocks, int nslots, int rounds, uint32_t seed, long long probeCycles,
+                               unsigned long long* out, cudaStream_t st);
 int ElectronPhaseSmemBytes(const DevTables<float>& T);
 // block-batched electron phase (256 threads per block, shared-memory slots)
 int BlockPhaseSmemBytes(const DevTables<float>& T);

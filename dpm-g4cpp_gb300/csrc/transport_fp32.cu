@@ -1025,8 +1025,9 @@ __device__ __forceinline__ void CellStore(uint16_t* c, uint32_t v) {
                "h"(uint16_t(v))
                : "memory");
 }
-// waits until (cell & m) == want; false after kWaitCycles
-__device__ __forceinline__ bool CellWait(const uint16_t* c, uint32_t want, uint32_t m, uint32_t& v) {
+// waits until (cell & m) == want; false after `limit` cycles
+__device__ __forceinline__ bool CellWait(const uint16_t* c, uint32_t want, uint32_t m, uint32_t& v,
+                                         long long limit = kWaitCycles) {
   v = CellLoad(c);
   if ((v & m) == want) return true;
   const long long t0 = clock64();
@@ -1034,7 +1035,7 @@ __device__ __forceinline__ bool CellWait(const uint16_t* c, uint32_t want, uint3
     __nanosleep(32);
     v = CellLoad(c);
     if ((v & m) == want) return true;
-    if (clock64() - t0 > kWaitCycles) return false;
+    if (clock64() - t0 > limit) return false;
   }
 }
 
@@ -2052,6 +2053,60 @@ __global__ void TableKernel32(DevTables<float> T, int q, int imat, const double*
   out[i] = double(v);
 }
 
+// Self-test of the slot rings (one independent run per block): slots
+// 0 .. nslots - 1 start on ring 0; a warp that takes a slot counts a visit
+// and puts it on the ring picked by a hash of (seed, slot, visit), until the
+// slot has `rounds` visits and retires. out[0] += visits, out[1] += slots
+// whose visit count is not `rounds`, out[2] += warps that gave up a wait,
+// out[3] += blocks whose probe wait on a cell nothing fills gave up after
+// `probeCycles` (as it must).
+__global__ void __launch_bounds__(256) RingSelfTestKernel(int nslots, int rounds, uint32_t seed, long long probeCycles,
+                                                          unsigned long long* out) {
+  __shared__ Rings<4> R;
+  __shared__ unsigned int visits[kRingSize];
+  __shared__ uint16_t probe;
+  const int lane = threadIdx.x & 31;
+  RingsInit(R, 0, nslots);
+  for (int k = threadIdx.x; k < kRingSize; k += blockDim.x) visits[k] = 0u;
+  if (threadIdx.x == 0) probe = uint16_t(CellEmpty(0));
+  __syncthreads();
+  bool gaveUp = false;
+  unsigned long long taken = 0;
+  for (;;) {
+    int n = 0, k = 0;
+    const int ring = RingTake(R, lane, n, k, gaveUp);
+    if (ring < 0) break;
+    int q = -1;
+    if (lane < n) {
+      const unsigned v = atomicAdd(&visits[k], 1u) + 1u;
+      ++taken;
+      uint32_t h = seed ^ (uint32_t(k) * 0x9E3779B1u) ^ (v * 0x85EBCA77u);
+      h ^= h >> 15;
+      h *= 0x2C1B3C6Du;
+      h ^= h >> 12;
+      q = v >= unsigned(rounds) ? 4 : int(h & 3u);
+    }
+    RingPut(R, lane, q, k, gaveUp);
+    if (gaveUp) break;
+  }
+  __syncthreads();
+  unsigned long long bad = 0;
+  for (int k = threadIdx.x; k < nslots; k += blockDim.x) bad += visits[k] != unsigned(rounds);
+  for (int o = 16; o > 0; o >>= 1) {
+    taken += __shfl_down_sync(kFull, taken, o);
+    bad += __shfl_down_sync(kFull, bad, o);
+  }
+  if (lane == 0) {
+    atomicAdd(out, taken);
+    atomicAdd(out + 1, bad);
+    if (gaveUp) atomicAdd(out + 2, 1ull);
+  }
+  if (threadIdx.x == 0) {
+    uint32_t v;
+    if (!CellWait(&probe, CellFull(0), ~kCellSlot, v, probeCycles)) atomicAdd(out + 3, 1ull);
+  }
+}
+
 }  // namespace
 
 int ElectronPhaseSmemBytes(const DevTables<float>& T) { return int(T.elecCount * sizeof(float)); }
@@ -2146,6 +2201,12 @@ cudaError_t LaunchSamplerEval32(const DevTables<float>& T, int s, int imat, cons
 cudaError_t LaunchTableEval32(const DevTables<float>& T, int q, int imat, const double* e, double* out, int n,
                               cudaStream_t st) {
   TableKernel32<<<(n + 127) / 128, 128, 0, st>>>(T, q, imat, e, out, n);
+  return cudaGetLastError();
+}
+
+cudaError_t LaunchRingSelfTest(int blocks, int nslots, int rounds, uint32_t seed, long long probeCycles,
+                               unsigned long long* out, cudaStream_t st) {
+  RingSelfTestKernel<<<blocks, 256, 0, st>>>(nslots, rounds, seed, probeCycles, out);
   return cudaGetLastError();
 }
 

@@ -12,6 +12,7 @@
 
 #include "device_common.cuh"
 #include "host_util.h"
+#include "kernels.h"
 
 namespace dpmx {
 namespace {
@@ -100,5 +101,22 @@ extern "C" int dpmx_model_histogram(const dpmx_tables* t, int precision, int mod
     hist_x[b] = double(h[b]);
     hist_cos[b] = double(h[hbins + b]);
   }
+  return DPMX_OK;
+}
+
+extern "C" int dpmx_ring_selftest(int blocks, int nslots, int rounds, uint64_t seed, long long probe_cycles,
+                                  long long* out) {
+  if (!out || blocks < 1 || blocks > 152 * 64 || nslots < 1 || nslots > 512 || rounds < 1 || rounds > (1 << 20) ||
+      probe_cycles < 0 || probe_cycles > (1LL << 32))
+    return Fail(DPMX_ERR_ARG, "bad ring self-test arguments");
+  unsigned long long* d = nullptr;
+  CK(cudaMalloc(&d, 4 * sizeof(unsigned long long)));
+  cudaError_t e = cudaMemset(d, 0, 4 * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = LaunchRingSelfTest(blocks, nslots, rounds, uint32_t(seed), probe_cycles, d, 0);
+  unsigned long long h[4] = {0, 0, 0, 0};
+  if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  CK(e);
+  for (int i = 0; i < 4; ++i) out[i] = (long long)h[i];
   return DPMX_OK;
 }

@@ -231,6 +231,16 @@ int dpmx_simulate_histories(const dpmx_tables* t, int nprimary, double eprimary,
 int dpmx_model_histogram(const dpmx_tables* t, int precision, int model, int imat, double e0, long long n,
                          uint64_t seed, int hbins, double* hist_x, double* hist_cos);
 
+/* ---- self-test of the block kernels' slot rings ---- */
+/* `blocks` independent blocks of 256 threads each pass `nslots` slots (1..512)
+ * through four slot rings (the shared-memory queues the block-batched phases
+ * schedule with) until every slot has been taken `rounds` times; then each
+ * block waits `probe_cycles` clock cycles on a ring cell that nothing fills.
+ * out[0] = slots taken, out[1] = slots taken a number of times other than
+ * `rounds`, out[2] = warps that gave up a wait, out[3] = blocks whose probe
+ * wait ran out. A correct ring gives blocks * nslots * rounds, 0, 0, blocks. */
+int dpmx_ring_selftest(int blocks, int nslots, int rounds, uint64_t seed, long long probe_cycles, long long* out);
+
 /* ---- influence matrix (beamlet-tagged run with tag_beamlets = 1) ---- */
 /* builds A (rows: voxels, cols: beamlets, FP32 values from the FP64 tally,
  * entries <= threshold * max dropped) on the device */

@@ -42,3 +42,12 @@ def test_truncated_file(dpm, tmp_path, victim):
     open(d / victim, "w").write(text[: len(text) // 2])
     rc, msg = load(dpm, d)
     assert rc == dpm.ERR_PARSE and victim in msg
+
+
+def test_ring_selftest_rejects_bad_arguments(dpm):
+    """argument checks come before any CUDA call"""
+    import importlib
+    importlib.import_module("dpm-g4cpp_gb300.builder").build_library()
+    for kw in ({"nslots": 0}, {"nslots": 513}, {"rounds": 0}, {"blocks": 0}, {"probe_cycles": -1}):
+        with pytest.raises(dpm.DpmxError):
+            dpm.ring_selftest(**kw)
