@@ -982,14 +982,14 @@ __global__ void __launch_bounds__(256) ElectronPhase(PhaseArgs a) {
 constexpr int kSlots = 416;   // 3 blocks leave the SM 164 KB of shared memory and the rest to L1
 constexpr int kBlockMinBlocks = 3;      // resident blocks per SM the kernel is compiled for
 constexpr bool kTablesInSmem = false;  // electron tables staged per block, else read through L1
-constexpr bool kCacheMaterial = true;  // a slot keeps its voxel's material: read once per voxel entered
-constexpr uint32_t kFAxis = 3u, kFHinge = 4u, kFNeedGeom = 8u, kFPositron = 16u, kFAlive = 32u;
+constexpr uint32_t kFHinge = 4u, kFPositron = 16u;
+constexpr int8_t kMatUnknown = -2;   // the slot's voxel changed since its material was read
 
 struct SlotArrays {     // shared-memory state of the resident electrons
   uint32_t vox[kSlots];
   float lx[kSlots], ly[kSlots], lz[kSlots], dx[kSlots], dy[kSlots], dz[kSlots], e[kSlots];
-  float nTr1[kSlots], nTr10[kSlots], nMol[kSlots], invMol[kSlots], nBrem[kSlots], ekin0[kSlots], sGeom[kSlots];
-  uint32_t flags[kSlots];   // axis (2 bits), hinge, needGeom, positron, alive; job << 8
+  float nTr1[kSlots], nTr10[kSlots], nMol[kSlots], invMol[kSlots], nBrem[kSlots], ekin0[kSlots];
+  uint32_t flags[kSlots];   // hinge, positron; sub-job << 8
   uint32_t hist[kSlots], slot[kSlots], ulo[kSlots], uhi[kSlots], ctr[kSlots], pst[kSlots];
   double acc[kSlots];
   int8_t mat[kSlots];       // material of the slot's current voxel (-1: vacuum)
@@ -1174,21 +1174,18 @@ __device__ __forceinline__ void LoadSlot(const SlotArrays& S, int k, PState& p, 
   p.hist = S.hist[k]; p.slot = S.slot[k]; p.ulo = S.ulo[k]; p.uhi = S.uhi[k];
   p.meta = ((fl >> 8) << 2) | ((fl & kFPositron) ? 2u : 1u);
   s.nTr1 = S.nTr1[k]; s.nTr10 = S.nTr10[k]; s.nMol = S.nMol[k]; s.invMol = S.invMol[k];
-  s.nBrem = S.nBrem[k]; s.ekin0 = S.ekin0[k]; s.sGeom = S.sGeom[k];
-  s.axis = int(fl & kFAxis);
+  s.nBrem = S.nBrem[k]; s.ekin0 = S.ekin0[k];
   s.hinge = (fl & kFHinge) != 0;
-  s.needGeom = (fl & kFNeedGeom) != 0;
 }
 
-__device__ __forceinline__ void StoreSlot(SlotArrays& S, int k, const PState& p, const EState& s, bool alive) {
+__device__ __forceinline__ void StoreSlot(SlotArrays& S, int k, const PState& p, const EState& s) {
   S.vox[k] = PackVox(p.ix, p.iy, p.iz);
   S.lx[k] = p.lx; S.ly[k] = p.ly; S.lz[k] = p.lz;
   S.dx[k] = p.dx; S.dy[k] = p.dy; S.dz[k] = p.dz;
   S.e[k] = p.e;
   S.nTr1[k] = s.nTr1; S.nTr10[k] = s.nTr10; S.nMol[k] = s.nMol; S.invMol[k] = s.invMol;
-  S.nBrem[k] = s.nBrem; S.ekin0[k] = s.ekin0; S.sGeom[k] = s.sGeom;
-  S.flags[k] = (uint32_t(s.axis) & kFAxis) | (s.hinge ? kFHinge : 0u) | (s.needGeom ? kFNeedGeom : 0u) |
-               ((p.meta & 3u) == 2u ? kFPositron : 0u) | (alive ? kFAlive : 0u) | ((p.meta >> 2) << 8);
+  S.nBrem[k] = s.nBrem; S.ekin0[k] = s.ekin0;
+  S.flags[k] = (s.hinge ? kFHinge : 0u) | ((p.meta & 3u) == 2u ? kFPositron : 0u) | ((p.meta >> 2) << 8);
 }
 
 // the part of slot k a plain sub-step reads (direction, the MSC hinge state
@@ -1202,19 +1199,15 @@ __device__ __forceinline__ void LoadStepState(const SlotArrays& S, int k, PState
   fl = S.flags[k];
   p.hist = S.hist[k]; p.slot = S.slot[k]; p.ulo = S.ulo[k]; p.uhi = S.uhi[k];
   p.meta = ((fl >> 8) << 2) | ((fl & kFPositron) ? 2u : 1u);
-  s.nTr1 = S.nTr1[k]; s.nMol = S.nMol[k]; s.invMol = S.invMol[k]; s.nBrem = S.nBrem[k]; s.sGeom = S.sGeom[k];
-  s.axis = int(fl & kFAxis);
+  s.nTr1 = S.nTr1[k]; s.nMol = S.nMol[k]; s.invMol = S.invMol[k]; s.nBrem = S.nBrem[k];
   s.hinge = (fl & kFHinge) != 0;
-  s.needGeom = (fl & kFNeedGeom) != 0;
 }
 
-__device__ __forceinline__ void StoreStepState(SlotArrays& S, int k, const PState& p, const EState& s,
-                                               uint32_t fl) {
+__device__ __forceinline__ void StoreStepState(SlotArrays& S, int k, const PState& p, const EState& s) {
   S.vox[k] = PackVox(p.ix, p.iy, p.iz);
   S.lx[k] = p.lx; S.ly[k] = p.ly; S.lz[k] = p.lz;
   S.e[k] = p.e;
-  S.nTr1[k] = s.nTr1; S.nMol[k] = s.nMol; S.nBrem[k] = s.nBrem; S.sGeom[k] = s.sGeom;
-  S.flags[k] = (fl & ~(kFAxis | kFNeedGeom)) | (uint32_t(s.axis) & kFAxis) | (s.needGeom ? kFNeedGeom : 0u);
+  S.nTr1[k] = s.nTr1; S.nMol[k] = s.nMol; S.nBrem[k] = s.nBrem;
 }
 
 // random stream of slot k (a fresh Philox block per use; the counter advances)
@@ -1233,15 +1226,20 @@ __device__ __forceinline__ void AnnihilateF(const PhaseArgs& a, const PState& p,
   PState g = p;
   g.e = kEMC2f; g.meta = 0u | (p.meta & ~3u);
   g.dx = sint * cs; g.dy = sint * sn; g.dz = cost;
-  rng.Child(0, g.ulo, g.uhi);
-  if (!Append(a.outP, a.outPCount, a.overflow, g)) acc += kEMC2f;
-  g.dx = -g.dx; g.dy = -g.dy; g.dz = -g.dz;
-  rng.Child(1, g.ulo, g.uhi);
-  if (!Append(a.outP, a.outPCount, a.overflow, g)) acc += kEMC2f;
+#pragma unroll 1
+  for (int c = 0; c < 2; ++c) {   // child c; the second photon opposite the first
+    rng.Child(c, g.ulo, g.uhi);
+    if (!Append(a.outP, a.outPCount, a.overflow, g)) acc += kEMC2f;
+    g.dx = -g.dx; g.dy = -g.dy; g.dz = -g.dz;
+  }
 }
 
 // one condensed-history sub-step of slot k. Returns 0 to keep stepping,
 // 1 brem, 2 Moller, 3 MSC hinge, 4 MSC step end, 5 finished.
+// Every sub-step starts by settling the electron in its voxel (distance to the
+// walls, a face within the tolerance crossed first); a sub-step that ends on
+// a voxel face only moves onto it, and the next one settles. One deposit at
+// most is scored per sub-step, at one place in the code.
 template <int AGG>
 __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, const JobF* jobs, SlotArrays& S,
                                         int k, EscTally& esc, unsigned long long& nsteps, const DepthAcc& dacc) {
@@ -1256,22 +1254,21 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
   double acc = S.acc[k];
   int code = 0;
   int im = -1;
-  if (s.needGeom) {
+  {
     const int ox = p.ix, oy = p.iy, oz = p.iz;
     if (Settle(J, p, s.sGeom, s.axis)) {
-      if (!kCacheMaterial || p.ix != ox || p.iy != oy || p.iz != oz) {
+      im = S.mat[k];
+      if (im == kMatUnknown || p.ix != ox || p.iy != oy || p.iz != oz) {
         im = MaterialAt(J, p.ix, p.iy, p.iz);
-        if (kCacheMaterial) S.mat[k] = int8_t(im);
-      } else {
-        im = S.mat[k];
+        S.mat[k] = int8_t(im);
       }
     }
-    s.needGeom = false;
-  } else {
-    im = kCacheMaterial ? int(S.mat[k]) : MaterialAt(J, p.ix, p.iy, p.iz);
   }
   const uint32_t pst = S.pst[k] + 1;
   S.pst[k] = pst;
+  float step = 0.f, scored = 0.f;
+  int what = 0;
+  bool score = false, moves = false;
   if (im < 0) {
     const float out = p.e + (positron ? 2.0f * kEMC2f : 0.f);
     acc += out;
@@ -1285,8 +1282,7 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
     ++nsteps;
     const float ecut = T.ecut;
     const float rho = VoxelRho(J, T, p.ix, p.iy, p.iz, im);
-    float step = s.sGeom;
-    int what = 0;
+    step = s.sGeom;
     const float le = __logf(p.e);
     float dedx = SplineLe(et.dedx[im], p.e, le) * rho;
     float emid = fmaxf(p.e - 0.5f * step * dedx, ecut);
@@ -1315,46 +1311,51 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
     const float de = step * dedx;
     const float ef = p.e - de;
     if (ef < ecut) {
-      const float edep = p.e;
+      // the electron stops: its energy is deposited here; a positron moves
+      // to the end of the step first and annihilates there
+      scored = p.e;
       p.e = 0.f;
-      if (!positron) {
-        Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, edep, AGG, dacc);
-        acc += edep;
-      } else {
+      score = true;
+      if (positron) {
         bool inside;
         if (what == 0) inside = MoveToFace(J, p, step, s.axis);
         else { p.lx += step * p.dx; p.ly += step * p.dy; p.lz += step * p.dz; inside = true; }
         const int im2 = inside ? MaterialAt(J, p.ix, p.iy, p.iz) : -1;
         if (im2 < 0) {
-          acc += edep + 2.0f * kEMC2f;
-          esc.Add(jobs, job, double(edep + 2.0f * kEMC2f));
+          acc += scored + 2.0f * kEMC2f;
+          esc.Add(jobs, job, double(scored + 2.0f * kEMC2f));
+          score = false;
         } else {
           PRng rng;
           SlotRng(S, k, J, p, rng);
           AnnihilateF(a, p, rng, acc);
-          Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, edep, AGG, dacc);
-          acc += edep;
         }
       }
       code = 5;
     } else {
       p.e = ef;
-      Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, de, AGG, dacc);
-      acc += de;
-      if (what == 0) {
-        if (!MoveToFace(J, p, step, s.axis) || !Settle(J, p, s.sGeom, s.axis)) {
-          const float out = p.e + (positron ? 2.0f * kEMC2f : 0.f);
-          acc += out;
-          esc.Add(jobs, job, double(out));
-          code = 5;
-        } else if (kCacheMaterial) {
-          S.mat[k] = int8_t(MaterialAt(J, p.ix, p.iy, p.iz));   // the voxel just entered
-        }
+      scored = de;
+      score = true;
+      moves = true;
+    }
+  }
+  if (score) {
+    Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, scored, AGG, dacc);
+    acc += scored;
+  }
+  if (moves) {
+    if (what == 0) {
+      if (MoveToFace(J, p, step, s.axis)) {
+        S.mat[k] = kMatUnknown;   // the voxel just entered; read when the next sub-step settles
       } else {
-        p.lx += step * p.dx; p.ly += step * p.dy; p.lz += step * p.dz;
-        s.needGeom = true;
-        code = (what == 3) ? (s.hinge ? 3 : 4) : what;
+        const float out = p.e + (positron ? 2.0f * kEMC2f : 0.f);
+        acc += out;
+        esc.Add(jobs, job, double(out));
+        code = 5;
       }
+    } else {
+      p.lx += step * p.dx; p.ly += step * p.dy; p.lz += step * p.dz;
+      code = (what == 3) ? (s.hinge ? 3 : 4) : what;
     }
   }
   if (code == 5) {
@@ -1362,7 +1363,7 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
     S.flags[k] = 0u;
   } else {
     S.acc[k] = acc;
-    StoreStepState(S, k, p, s, fl);
+    StoreStepState(S, k, p, s);
   }
   return code;
 }
@@ -1423,7 +1424,7 @@ __device__ __forceinline__ bool EventBrem(const PhaseArgs& a, const JobF* jobs, 
   PRng rng;
   SlotRng(S, k, J, p, rng);
   double acc = S.acc[k];
-  const int im = kCacheMaterial ? int(S.mat[k]) : MaterialAt(J, p.ix, p.iy, p.iz);
+  const int im = S.mat[k];
   if (p.e > T.gcut && im >= 0) {
     const float r3 = rng.U(), r2 = rng.U(), r1 = rng.U();
     const float eg = SampleSB(T.sb[im], p.e, r1, r2, r3);
@@ -1516,9 +1517,7 @@ __device__ __forceinline__ bool RefillSlot(const PhaseArgs& a, const ETables& et
   }
   EState s;
   InitElectron(et, p, rng, s);
-  s.sGeom = 0.f;
-  s.axis = 0;
-  StoreSlot(S, k, p, s, true);
+  StoreSlot(S, k, p, s);
   // the particle's identity (history, energy-check slot, stream) is set once
   // here; StoreSlot only writes the state that changes while stepping
   S.hist[k] = p.hist;
