@@ -1239,7 +1239,8 @@ __device__ __forceinline__ void AnnihilateF(const PhaseArgs& a, const PState& p,
 // Every sub-step starts by settling the electron in its voxel (distance to the
 // walls, a face within the tolerance crossed first); a sub-step that ends on
 // a voxel face only moves onto it, and the next one settles. One deposit at
-// most is scored per sub-step, at one place in the code.
+// most is scored, and one escape counted, per sub-step, at one place in the
+// code each (fewer inlined copies: the kernel is instruction-fetch bound).
 template <int AGG>
 __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, const JobF* jobs, SlotArrays& S,
                                         int k, EscTally& esc, unsigned long long& nsteps, const DepthAcc& dacc) {
@@ -1266,13 +1267,12 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
   }
   const uint32_t pst = S.pst[k] + 1;
   S.pst[k] = pst;
-  float step = 0.f, scored = 0.f;
+  float step = 0.f, scored = 0.f, out = 0.f;
   int what = 0;
-  bool score = false, moves = false;
+  bool score = false, moves = false, escapes = false;
   if (im < 0) {
-    const float out = p.e + (positron ? 2.0f * kEMC2f : 0.f);
-    acc += out;
-    esc.Add(jobs, job, double(out));
+    out = p.e + (positron ? 2.0f * kEMC2f : 0.f);
+    escapes = true;
     code = 5;
   } else if (pst > kMaxElectronSteps) {
     acc += p.e + (positron ? 2.0f * kEMC2f : 0.f);
@@ -1322,8 +1322,8 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
         else { p.lx += step * p.dx; p.ly += step * p.dy; p.lz += step * p.dz; inside = true; }
         const int im2 = inside ? MaterialAt(J, p.ix, p.iy, p.iz) : -1;
         if (im2 < 0) {
-          acc += scored + 2.0f * kEMC2f;
-          esc.Add(jobs, job, double(scored + 2.0f * kEMC2f));
+          out = scored + 2.0f * kEMC2f;
+          escapes = true;
           score = false;
         } else {
           PRng rng;
@@ -1348,15 +1348,18 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
       if (MoveToFace(J, p, step, s.axis)) {
         S.mat[k] = kMatUnknown;   // the voxel just entered; read when the next sub-step settles
       } else {
-        const float out = p.e + (positron ? 2.0f * kEMC2f : 0.f);
-        acc += out;
-        esc.Add(jobs, job, double(out));
+        out = p.e + (positron ? 2.0f * kEMC2f : 0.f);
+        escapes = true;
         code = 5;
       }
     } else {
       p.lx += step * p.dx; p.ly += step * p.dy; p.lz += step * p.dz;
       code = (what == 3) ? (s.hinge ? 3 : 4) : what;
     }
+  }
+  if (escapes) {
+    acc += out;
+    esc.Add(jobs, job, double(out));
   }
   if (code == 5) {
     atomicAdd(a.histE + p.slot, acc);
