@@ -1801,20 +1801,7 @@ __device__ __forceinline__ void PhotonPairSlot(const PhaseArgs& a, const JobF* j
   if (e1 < T.ecut) {
     Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, e1, AGG, dacc);
     acc += e1;
-    // annihilation at rest (SimDPMLike.cc:753-791)
-    const float cost = 1.0f - 2.0f * rng.U();
-    const float sint = sqrtf(fmaxf(0.f, (1.0f - cost) * (1.0f + cost)));
-    const float phi = 2.0f * kPIf * rng.U();
-    float s2, c2;
-    __sincosf(phi, &s2, &c2);
-    PState g = p;
-    g.e = kEMC2f; g.meta = 0u | (p.meta & ~3u);
-    g.dx = sint * c2; g.dy = sint * s2; g.dz = cost;
-    rng.Child(0, g.ulo, g.uhi);
-    if (!Append(a.outP, a.outPCount, a.overflow, g)) acc += kEMC2f;
-    g.dx = -g.dx; g.dy = -g.dy; g.dz = -g.dz;
-    rng.Child(1, g.ulo, g.uhi);
-    if (!Append(a.outP, a.outPCount, a.overflow, g)) acc += kEMC2f;
+    AnnihilateF(a, p, rng, acc);   // at rest (SimDPMLike.cc:753-791)
   } else {
     PState c = p;
     c.e = e1; c.meta = 2u | (p.meta & ~3u);
