@@ -985,14 +985,17 @@ constexpr bool kTablesInSmem = false;  // electron tables staged per block, else
 constexpr uint32_t kFHinge = 4u, kFPositron = 16u;
 constexpr int8_t kMatUnknown = -2;   // the slot's voxel changed since its material was read
 
-struct SlotArrays {     // shared-memory state of the resident electrons
-  uint32_t vox[kSlots];
-  float lx[kSlots], ly[kSlots], lz[kSlots], dx[kSlots], dy[kSlots], dz[kSlots], e[kSlots];
-  float nTr1[kSlots], nTr10[kSlots], nMol[kSlots], invMol[kSlots], nBrem[kSlots], ekin0[kSlots];
-  uint32_t flags[kSlots];   // hinge, positron; sub-job << 8
-  uint32_t hist[kSlots], slot[kSlots], ulo[kSlots], uhi[kSlots], ctr[kSlots], pst[kSlots];
+// shared-memory state of the resident electrons, in 16-byte records that a
+// lane reads or writes with one 128-bit access
+struct SlotArrays {
+  float4 pos[kSlots];   // offset in the voxel lx, ly, lz; kinetic energy
+  float4 dir[kSlots];   // direction dx, dy, dz; voxel (PackVox, as float bits)
+  float4 mfp[kSlots];   // nTr1, nMol, invMol, nBrem
+  uint4 id[kSlots];     // flags (hinge, positron; sub-job << 8), history, energy-check slot, sub-steps
+  uint4 rs[kSlots];     // random stream uid lo, uid hi, counter; ekin0 (float bits)
+  float nTr10[kSlots];
   double acc[kSlots];
-  int8_t mat[kSlots];       // material of the slot's current voxel (-1: vacuum)
+  int8_t mat[kSlots];   // material of the slot's current voxel (-1: vacuum)
 };
 constexpr long long kWaitCycles = 4LL << 30;   // bound of one wait (~2 s): then the block gives up
 constexpr int kRingBits = 9;
@@ -1164,56 +1167,63 @@ __host__ __device__ inline size_t BlockPhaseSmemBytesFor(const DevTables<float>&
   return ((b + 15) & ~size_t(15)) + DepthAccBytes(depthBins);
 }
 
-__device__ __forceinline__ void LoadSlot(const SlotArrays& S, int k, PState& p, EState& s, uint32_t& fl) {
-  const uint32_t v = S.vox[k];
+__device__ __forceinline__ void UnpackVox(uint32_t v, PState& p) {
   p.ix = int(v & 0x7ffu); p.iy = int((v >> 11) & 0x7ffu); p.iz = int(v >> 22);
-  p.lx = S.lx[k]; p.ly = S.ly[k]; p.lz = S.lz[k];
-  p.dx = S.dx[k]; p.dy = S.dy[k]; p.dz = S.dz[k];
-  p.e = S.e[k];
-  fl = S.flags[k];
-  p.hist = S.hist[k]; p.slot = S.slot[k]; p.ulo = S.ulo[k]; p.uhi = S.uhi[k];
+}
+
+__device__ __forceinline__ void LoadSlot(const SlotArrays& S, int k, PState& p, EState& s, uint32_t& fl) {
+  const float4 a = S.pos[k], b = S.dir[k], c = S.mfp[k];
+  const uint4 d = S.id[k], r = S.rs[k];
+  p.lx = a.x; p.ly = a.y; p.lz = a.z; p.e = a.w;
+  p.dx = b.x; p.dy = b.y; p.dz = b.z;
+  UnpackVox(__float_as_uint(b.w), p);
+  s.nTr1 = c.x; s.nMol = c.y; s.invMol = c.z; s.nBrem = c.w;
+  fl = d.x; p.hist = d.y; p.slot = d.z;
+  p.ulo = r.x; p.uhi = r.y;
+  s.ekin0 = __uint_as_float(r.w);
+  s.nTr10 = S.nTr10[k];
   p.meta = ((fl >> 8) << 2) | ((fl & kFPositron) ? 2u : 1u);
-  s.nTr1 = S.nTr1[k]; s.nTr10 = S.nTr10[k]; s.nMol = S.nMol[k]; s.invMol = S.invMol[k];
-  s.nBrem = S.nBrem[k]; s.ekin0 = S.ekin0[k];
   s.hinge = (fl & kFHinge) != 0;
 }
 
-__device__ __forceinline__ void StoreSlot(SlotArrays& S, int k, const PState& p, const EState& s) {
-  S.vox[k] = PackVox(p.ix, p.iy, p.iz);
-  S.lx[k] = p.lx; S.ly[k] = p.ly; S.lz[k] = p.lz;
-  S.dx[k] = p.dx; S.dy[k] = p.dy; S.dz[k] = p.dz;
-  S.e[k] = p.e;
-  S.nTr1[k] = s.nTr1; S.nTr10[k] = s.nTr10; S.nMol[k] = s.nMol; S.invMol[k] = s.invMol;
-  S.nBrem[k] = s.nBrem; S.ekin0[k] = s.ekin0;
-  S.flags[k] = (s.hinge ? kFHinge : 0u) | ((p.meta & 3u) == 2u ? kFPositron : 0u) | ((p.meta >> 2) << 8);
+// a new particle in slot k, its random stream at counter ctr
+__device__ __forceinline__ void StoreSlot(SlotArrays& S, int k, const PState& p, const EState& s, uint32_t ctr) {
+  S.pos[k] = make_float4(p.lx, p.ly, p.lz, p.e);
+  S.dir[k] = make_float4(p.dx, p.dy, p.dz, __uint_as_float(PackVox(p.ix, p.iy, p.iz)));
+  S.mfp[k] = make_float4(s.nTr1, s.nMol, s.invMol, s.nBrem);
+  S.id[k] = make_uint4((s.hinge ? kFHinge : 0u) | ((p.meta & 3u) == 2u ? kFPositron : 0u) | ((p.meta >> 2) << 8),
+                       p.hist, p.slot, 0u);
+  S.rs[k] = make_uint4(p.ulo, p.uhi, ctr, __float_as_uint(s.ekin0));
+  S.nTr10[k] = s.nTr10;
 }
 
-// the part of slot k a plain sub-step reads (direction, the MSC hinge state
-// and the Moller IMFP stay as they are), and the part it writes back
-__device__ __forceinline__ void LoadStepState(const SlotArrays& S, int k, PState& p, EState& s, uint32_t& fl) {
-  const uint32_t v = S.vox[k];
-  p.ix = int(v & 0x7ffu); p.iy = int((v >> 11) & 0x7ffu); p.iz = int(v >> 22);
-  p.lx = S.lx[k]; p.ly = S.ly[k]; p.lz = S.lz[k];
-  p.dx = S.dx[k]; p.dy = S.dy[k]; p.dz = S.dz[k];
-  p.e = S.e[k];
-  fl = S.flags[k];
-  p.hist = S.hist[k]; p.slot = S.slot[k]; p.ulo = S.ulo[k]; p.uhi = S.uhi[k];
+// the part of slot k a plain sub-step reads (the random stream, the MSC hinge
+// state and nTr10 stay as they are; pst: sub-steps taken), and the part it
+// writes back
+__device__ __forceinline__ void LoadStepState(const SlotArrays& S, int k, PState& p, EState& s, uint32_t& fl,
+                                              uint32_t& pst) {
+  const float4 a = S.pos[k], b = S.dir[k], c = S.mfp[k];
+  const uint4 d = S.id[k];
+  p.lx = a.x; p.ly = a.y; p.lz = a.z; p.e = a.w;
+  p.dx = b.x; p.dy = b.y; p.dz = b.z;
+  UnpackVox(__float_as_uint(b.w), p);
+  s.nTr1 = c.x; s.nMol = c.y; s.invMol = c.z; s.nBrem = c.w;
+  fl = d.x; p.hist = d.y; p.slot = d.z; pst = d.w;
   p.meta = ((fl >> 8) << 2) | ((fl & kFPositron) ? 2u : 1u);
-  s.nTr1 = S.nTr1[k]; s.nMol = S.nMol[k]; s.invMol = S.invMol[k]; s.nBrem = S.nBrem[k];
   s.hinge = (fl & kFHinge) != 0;
 }
 
 __device__ __forceinline__ void StoreStepState(SlotArrays& S, int k, const PState& p, const EState& s) {
-  S.vox[k] = PackVox(p.ix, p.iy, p.iz);
-  S.lx[k] = p.lx; S.ly[k] = p.ly; S.lz[k] = p.lz;
-  S.e[k] = p.e;
-  S.nTr1[k] = s.nTr1; S.nMol[k] = s.nMol; S.nBrem[k] = s.nBrem;
+  S.pos[k] = make_float4(p.lx, p.ly, p.lz, p.e);
+  S.dir[k].w = __uint_as_float(PackVox(p.ix, p.iy, p.iz));
+  S.mfp[k] = make_float4(s.nTr1, s.nMol, s.invMol, s.nBrem);
 }
 
 // random stream of slot k (a fresh Philox block per use; the counter advances)
-__device__ __forceinline__ void SlotRng(const SlotArrays& S, int k, const JobF& J, const PState& p, PRng& r) {
-  r.Init(J.k0, J.k1, p.hist, p.ulo, p.uhi);
-  r.ctr = S.ctr[k];
+__device__ __forceinline__ void SlotRng(const SlotArrays& S, int k, const JobF& J, uint32_t hist, PRng& r) {
+  const uint4 q = S.rs[k];
+  r.Init(J.k0, J.k1, hist, q.x, q.y);
+  r.ctr = q.z;
 }
 
 // e+ annihilation at rest: two back-to-back 0.511 MeV photons (SimDPMLike.cc:753-791)
@@ -1247,8 +1257,8 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
   const DevTables<float>& T = a.T;
   PState p;
   EState s;
-  uint32_t fl;
-  LoadStepState(S, k, p, s, fl);
+  uint32_t fl, pst;
+  LoadStepState(S, k, p, s, fl, pst);
   const int job = JobOfSub(fl >> 8);
   const JobF& J = jobs[job];
   const bool positron = (fl & kFPositron) != 0;
@@ -1265,8 +1275,8 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
       }
     }
   }
-  const uint32_t pst = S.pst[k] + 1;
-  S.pst[k] = pst;
+  ++pst;
+  S.id[k].w = pst;
   float step = 0.f, scored = 0.f, out = 0.f;
   int what = 0;
   bool score = false, moves = false, escapes = false;
@@ -1327,7 +1337,7 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
           score = false;
         } else {
           PRng rng;
-          SlotRng(S, k, J, p, rng);
+          SlotRng(S, k, J, p.hist, rng);
           AnnihilateF(a, p, rng, acc);
         }
       }
@@ -1363,7 +1373,7 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
   }
   if (code == 5) {
     atomicAdd(a.histE + p.slot, acc);
-    S.flags[k] = 0u;
+    S.id[k].x = 0u;
   } else {
     S.acc[k] = acc;
     StoreStepState(S, k, p, s);
@@ -1378,7 +1388,7 @@ __device__ __forceinline__ void EventHinge(const PhaseArgs& a, const JobF* jobs,
   uint32_t fl;
   LoadSlot(S, k, p, s, fl);
   PRng rng;
-  SlotRng(S, k, jobs[JobOfSub(fl >> 8)], p, rng);
+  SlotRng(S, k, jobs[JobOfSub(fl >> 8)], p.hist, rng);
   const float r2 = rng.U(), r1 = rng.U();
   const float d = SampleGS(a.T.gs, s.ekin0, r1, r2);
   const float cost = fmaxf(-1.0f, fminf(1.0f, d));
@@ -1389,28 +1399,28 @@ __device__ __forceinline__ void EventHinge(const PhaseArgs& a, const JobF* jobs,
   float u1 = sint * cs, u2 = sint * sn, u3 = cost;
   RotateToLab(u1, u2, u3, p.dx, p.dy, p.dz);
   const float inv = rsqrtf(u1 * u1 + u2 * u2 + u3 * u3);
-  S.dx[k] = u1 * inv; S.dy[k] = u2 * inv; S.dz[k] = u3 * inv;
-  S.nTr1[k] = s.nTr10;
-  S.flags[k] = fl & ~kFHinge;
-  S.ctr[k] = rng.ctr;
+  S.dir[k] = make_float4(u1 * inv, u2 * inv, u3 * inv, __uint_as_float(PackVox(p.ix, p.iy, p.iz)));
+  S.mfp[k].x = s.nTr10;
+  S.id[k].x = fl & ~kFHinge;
+  S.rs[k].z = rng.ctr;
 }
 
 // end of an MSC step: new scattering strength and hinge (SimDPMLike.cc:227-237)
 __device__ __forceinline__ void EventMscEnd(const PhaseArgs& a, const ETables& et, const JobF* jobs, SlotArrays& S,
                                             int k) {
-  const uint32_t fl = S.flags[k];
+  const uint4 d = S.id[k], q = S.rs[k];
+  const uint32_t fl = d.x;
   const JobF& J = jobs[JobOfSub(fl >> 8)];
   PRng rng;
-  rng.Init(J.k0, J.k1, S.hist[k], S.ulo[k], S.uhi[k]);
-  rng.ctr = S.ctr[k];
-  const float e = S.e[k];
+  rng.Init(J.k0, J.k1, d.y, q.x, q.y);
+  rng.ctr = q.z;
+  const float e = S.pos[k].w;
   const float k1 = SplineLe(et.k1, e, __logf(e));
   const float n0 = rng.U() * k1;
-  S.ekin0[k] = e;
+  S.rs[k] = make_uint4(q.x, q.y, rng.ctr, __float_as_uint(e));   // ekin0 = e
   S.nTr10[k] = n0;
-  S.nTr1[k] = k1 - n0;
-  S.flags[k] = fl | kFHinge;
-  S.ctr[k] = rng.ctr;
+  S.mfp[k].x = k1 - n0;
+  S.id[k].x = fl | kFHinge;
 }
 
 // bremsstrahlung (SimDPMLike.cc:172-194, :661-695); false when the electron
@@ -1425,7 +1435,7 @@ __device__ __forceinline__ bool EventBrem(const PhaseArgs& a, const JobF* jobs, 
   const JobF& J = jobs[JobOfSub(fl >> 8)];
   const DevTables<float>& T = a.T;
   PRng rng;
-  SlotRng(S, k, J, p, rng);
+  SlotRng(S, k, J, p.hist, rng);
   double acc = S.acc[k];
   const int im = S.mat[k];
   if (p.e > T.gcut && im >= 0) {
@@ -1450,13 +1460,13 @@ __device__ __forceinline__ bool EventBrem(const PhaseArgs& a, const JobF* jobs, 
     acc += p.e;
     if ((fl & kFPositron) != 0) AnnihilateF(a, p, rng, acc);
     atomicAdd(a.histE + p.slot, acc);
-    S.flags[k] = 0u;
+    S.id[k].x = 0u;
     return false;
   }
-  S.e[k] = p.e;
-  S.nBrem[k] = -__logf(rng.U());
+  S.pos[k].w = p.e;
+  S.mfp[k].w = -__logf(rng.U());
   S.acc[k] = acc;
-  S.ctr[k] = rng.ctr;
+  S.rs[k].z = rng.ctr;
   return true;
 }
 
@@ -1469,7 +1479,7 @@ __device__ __forceinline__ void EventMoller(const PhaseArgs& a, const ETables& e
   LoadSlot(S, k, p, s, fl);
   const JobF& J = jobs[JobOfSub(fl >> 8)];
   PRng rng;
-  SlotRng(S, k, J, p, rng);
+  SlotRng(S, k, J, p.hist, rng);
   double acc = S.acc[k];
   if (p.e > 2.0f * a.T.ecut) {
     const float r3 = rng.U(), r2 = rng.U(), r1 = rng.U();
@@ -1488,11 +1498,11 @@ __device__ __forceinline__ void EventMoller(const PhaseArgs& a, const ETables& e
     if (!Append(a.outE, a.outECount, a.overflow, c)) acc += se;
     p.e -= se;
   }
-  S.e[k] = p.e;
-  S.nMol[k] = -__logf(rng.U());
-  S.invMol[k] = SplineLe(et.moller, p.e, __logf(p.e));
+  S.pos[k].w = p.e;
+  const float nMol = -__logf(rng.U());
+  S.mfp[k] = make_float4(s.nTr1, nMol, SplineLe(et.moller, p.e, __logf(p.e)), s.nBrem);
   S.acc[k] = acc;
-  S.ctr[k] = rng.ctr;
+  S.rs[k].z = rng.ctr;
 }
 
 // first sub-step state of a claimed work item (a primary or a queued
@@ -1520,16 +1530,8 @@ __device__ __forceinline__ bool RefillSlot(const PhaseArgs& a, const ETables& et
   }
   EState s;
   InitElectron(et, p, rng, s);
-  StoreSlot(S, k, p, s);
-  // the particle's identity (history, energy-check slot, stream) is set once
-  // here; StoreSlot only writes the state that changes while stepping
-  S.hist[k] = p.hist;
-  S.slot[k] = p.slot;
-  S.ulo[k] = p.ulo;
-  S.uhi[k] = p.uhi;
+  StoreSlot(S, k, p, s, rng.ctr);
   S.acc[k] = 0.0;
-  S.ctr[k] = rng.ctr;
-  S.pst[k] = 0;
   S.mat[k] = int8_t(im0);
   return true;
 }
@@ -1555,7 +1557,7 @@ __global__ void __launch_bounds__(256, kBlockMinBlocks) ElectronPhaseB(PhaseArgs
   else if (threadIdx.x == 0) BindElectronTables(a.T, &et);   // visible after the barrier below
   const int tid = threadIdx.x, lane = tid & 31;
   RingsInit(R, kRIdle, kSlots);
-  for (int k = tid; k < kSlots; k += blockDim.x) S.flags[k] = 0u;
+  for (int k = tid; k < kSlots; k += blockDim.x) S.id[k] = make_uint4(0u, 0u, 0u, 0u);
   __syncthreads();
   volatile int* vexh = &R.exhausted;
   EscTally esc;
