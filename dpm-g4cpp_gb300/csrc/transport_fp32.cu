@@ -1628,11 +1628,13 @@ __global__ void __launch_bounds__(256, kBlockMinBlocks) ElectronPhaseB(PhaseArgs
 constexpr int kPSlots = 352;   // 4 blocks leave the SM 164 KB of shared memory and the rest to L1
 constexpr int kPBlockMinBlocks = 4;
 
+// shared-memory state of the resident photons, in 16-byte records
 struct PSlotArrays {
-  uint32_t vox[kPSlots];
-  float lx[kPSlots], ly[kPSlots], lz[kPSlots], dx[kPSlots], dy[kPSlots], dz[kPSlots], e[kPSlots];
-  uint32_t meta[kPSlots], hist[kPSlots], slot[kPSlots], ulo[kPSlots], uhi[kPSlots], pst[kPSlots];
-  uint32_t ctr[kPSlots], have[kPSlots], w0[kPSlots], w1[kPSlots], w2[kPSlots], w3[kPSlots];
+  float4 pos[kPSlots];   // offset in the voxel lx, ly, lz; energy
+  float4 dir[kPSlots];   // direction dx, dy, dz; voxel (PackVox, as float bits)
+  uint4 id[kPSlots];     // meta (type, sub-job), history, energy-check slot, steps taken
+  uint4 rs[kPSlots];     // random stream uid lo, uid hi, counter, buffered words left
+  uint4 w[kPSlots];      // the buffered Philox words
   double acc[kPSlots];
 };
 // photon rings (of equally full rings the first is taken)
@@ -1645,26 +1647,24 @@ using PSlotRings = Rings<kPRings>;
 __host__ __device__ constexpr size_t PhotonBlockStaticBytes() { return sizeof(PSlotArrays) + sizeof(PSlotRings); }
 
 __device__ __forceinline__ void LoadPhoton(const PSlotArrays& S, int k, const JobF* jobs, PState& p, PRng& rng) {
-  const uint32_t v = S.vox[k];
-  p.ix = int(v & 0x7ffu); p.iy = int((v >> 11) & 0x7ffu); p.iz = int(v >> 22);
-  p.lx = S.lx[k]; p.ly = S.ly[k]; p.lz = S.lz[k];
-  p.dx = S.dx[k]; p.dy = S.dy[k]; p.dz = S.dz[k];
-  p.e = S.e[k];
-  p.meta = S.meta[k]; p.hist = S.hist[k]; p.slot = S.slot[k]; p.ulo = S.ulo[k]; p.uhi = S.uhi[k];
+  const float4 a = S.pos[k], b = S.dir[k];
+  const uint4 d = S.id[k], q = S.rs[k];
+  p.lx = a.x; p.ly = a.y; p.lz = a.z; p.e = a.w;
+  p.dx = b.x; p.dy = b.y; p.dz = b.z;
+  UnpackVox(__float_as_uint(b.w), p);
+  p.meta = d.x; p.hist = d.y; p.slot = d.z; p.ulo = q.x; p.uhi = q.y;
   const JobF& J = jobs[JobOfSub(p.meta >> 2)];
   rng.Init(J.k0, J.k1, p.hist, p.ulo, p.uhi);
-  rng.ctr = S.ctr[k];
-  rng.have = int(S.have[k]);
-  rng.w = make_uint4(S.w0[k], S.w1[k], S.w2[k], S.w3[k]);
+  rng.ctr = q.z;
+  rng.have = int(q.w);
+  rng.w = S.w[k];
 }
 
 __device__ __forceinline__ void StorePhoton(PSlotArrays& S, int k, const PState& p, const PRng& rng) {
-  S.vox[k] = PackVox(p.ix, p.iy, p.iz);
-  S.lx[k] = p.lx; S.ly[k] = p.ly; S.lz[k] = p.lz;
-  S.dx[k] = p.dx; S.dy[k] = p.dy; S.dz[k] = p.dz;
-  S.e[k] = p.e;
-  S.ctr[k] = rng.ctr; S.have[k] = uint32_t(rng.have);
-  S.w0[k] = rng.w.x; S.w1[k] = rng.w.y; S.w2[k] = rng.w.z; S.w3[k] = rng.w.w;
+  S.pos[k] = make_float4(p.lx, p.ly, p.lz, p.e);
+  S.dir[k] = make_float4(p.dx, p.dy, p.dz, __uint_as_float(PackVox(p.ix, p.iy, p.iz)));
+  S.rs[k] = make_uint4(p.ulo, p.uhi, rng.ctr, uint32_t(rng.have));
+  S.w[k] = rng.w;
 }
 
 // one Woodcock step of slot k (SimDPMLike.cc:471-508): 0 delta step, 1 Compton,
@@ -1680,8 +1680,8 @@ __device__ __forceinline__ int PhotonStepSlot(const PhaseArgs& a, const PTables&
   const JobF& J = jobs[job];
   double acc = S.acc[k];
   int code = 0;
-  const uint32_t pst = S.pst[k] + 1;
-  S.pst[k] = pst;
+  const uint32_t pst = S.id[k].w + 1;
+  S.id[k].w = pst;
   if (pst > kMaxPhotonSteps) {   // cannot happen for finite cross sections; bounded anyway
     acc += p.e;
     atomicAdd(&J.cnt->lost, 1ull);
@@ -1832,8 +1832,7 @@ __device__ __forceinline__ bool PhotonRefillSlot(const PhaseArgs& a, const JobF*
     atomicAdd(a.histE + p.slot, double(p.e));
     return false;
   }
-  S.meta[k] = p.meta; S.hist[k] = p.hist; S.slot[k] = p.slot; S.ulo[k] = p.ulo; S.uhi[k] = p.uhi;
-  S.pst[k] = 0;
+  S.id[k] = make_uint4(p.meta, p.hist, p.slot, 0u);
   S.acc[k] = 0.0;
   StorePhoton(S, k, p, rng);
   return true;
