@@ -1626,6 +1626,7 @@ __global__ void __launch_bounds__(256, kBlockMinBlocks) ElectronPhaseB(PhaseArgs
 // both kernels give the same histories.
 // ---------------------------------------------------------------------------
 constexpr int kPSlots = 352;   // 4 blocks leave the SM 164 KB of shared memory and the rest to L1
+constexpr int kPhotonStepsPerTake = 3;   // Woodcock steps a photon takes per turn while they are delta steps
 constexpr int kPBlockMinBlocks = 4;
 
 // shared-memory state of the resident photons, in 16-byte records
@@ -1667,8 +1668,9 @@ __device__ __forceinline__ void StorePhoton(PSlotArrays& S, int k, const PState&
   S.w[k] = rng.w;
 }
 
-// one Woodcock step of slot k (SimDPMLike.cc:471-508): 0 delta step, 1 Compton,
-// 2 pair, 3 finished (escaped, absorbed, or over the step cap)
+// Woodcock steps of slot k (SimDPMLike.cc:471-508), up to kPhotonStepsPerTake
+// while they are delta steps: 0 delta step, 1 Compton, 2 pair, 3 finished
+// (escaped, absorbed, or over the step cap)
 template <int AGG>
 __device__ __forceinline__ int PhotonStepSlot(const PhaseArgs& a, const PTables& pt, const JobF* jobs, PSlotArrays& S,
                                               int k, EscTally& esc, unsigned long long& nph, const DepthAcc& dacc) {
@@ -1680,44 +1682,48 @@ __device__ __forceinline__ int PhotonStepSlot(const PhaseArgs& a, const PTables&
   const JobF& J = jobs[job];
   double acc = S.acc[k];
   int code = 0;
-  const uint32_t pst = S.id[k].w + 1;
-  S.id[k].w = pst;
-  if (pst > kMaxPhotonSteps) {   // cannot happen for finite cross sections; bounded anyway
-    acc += p.e;
-    atomicAdd(&J.cnt->lost, 1ull);
-    code = 3;
-  } else {
-    ++nph;
-    const float lmax = 1.0f / (LinearGet(pt.imfpMax, p.e) * J.wscale);
-    const float step = -lmax * __logf(rng.U());
-    int im = -1;
-    if (Fly(J, p, step)) im = MaterialAt(J, p.ix, p.iy, p.iz);
-    if (im < 0) {
+  uint32_t pst = S.id[k].w;
+  // the majorant IMFP at the photon's energy, which delta steps keep
+  const float lmax = 1.0f / (LinearGet(pt.imfpMax, p.e) * J.wscale);
+#pragma unroll 1
+  for (int it = 0; it < kPhotonStepsPerTake && code == 0; ++it) {
+    if (++pst > kMaxPhotonSteps) {   // cannot happen for finite cross sections; bounded anyway
       acc += p.e;
-      esc.Add(jobs, job, double(p.e));
+      atomicAdd(&J.cnt->lost, 1ull);
       code = 3;
     } else {
-      const float rho = VoxelRho(J, T, p.ix, p.iy, p.iz, im);
-      const float r1 = rng.U();
-      float prob = 1.0f - LinearGet(pt.tot[im], p.e) * rho * lmax;
-      if (r1 >= prob) {
-        prob += LinearGet(pt.comp[im], p.e) * rho * lmax;
-        if (r1 < prob) {
-          code = 1;
-        } else {
-          prob += LinearGet(pt.pair[im], p.e) * rho * lmax;
-          if (r1 < prob && p.e > 2.0f * kEMC2f) {
-            code = 2;
+      ++nph;
+      const float step = -lmax * __logf(rng.U());
+      int im = -1;
+      if (Fly(J, p, step)) im = MaterialAt(J, p.ix, p.iy, p.iz);
+      if (im < 0) {
+        acc += p.e;
+        esc.Add(jobs, job, double(p.e));
+        code = 3;
+      } else {
+        const float rho = VoxelRho(J, T, p.ix, p.iy, p.iz, im);
+        const float r1 = rng.U();
+        float prob = 1.0f - LinearGet(pt.tot[im], p.e) * rho * lmax;
+        if (r1 >= prob) {
+          prob += LinearGet(pt.comp[im], p.e) * rho * lmax;
+          if (r1 < prob) {
+            code = 1;
           } else {
-            // photoelectric absorption (also below the pair threshold)
-            Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, p.e, AGG, dacc);
-            acc += p.e;
-            code = 3;
+            prob += LinearGet(pt.pair[im], p.e) * rho * lmax;
+            if (r1 < prob && p.e > 2.0f * kEMC2f) {
+              code = 2;
+            } else {
+              // photoelectric absorption (also below the pair threshold)
+              Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, p.e, AGG, dacc);
+              acc += p.e;
+              code = 3;
+            }
           }
         }
       }
     }
   }
+  S.id[k].w = pst;
   if (code == 3) {
     atomicAdd(a.histE + p.slot, acc);
   } else {
