@@ -65,9 +65,17 @@ void PutSplines(const std::vector<const Curve*>& curves, std::vector<SplineT<R>*
     std::vector<double> b, cc, d;
     SplineCoefficients(c->x, c->y, b, cc, d);
     offs.push_back(all.size());
-    for (size_t i = 0; i < c->x.size(); ++i) {
-      all.push_back(R(c->x[i])); all.push_back(R(c->y[i]));
-      all.push_back(R(b[i])); all.push_back(R(cc[i])); all.push_back(R(d[i]));
+    if (sizeof(R) == sizeof(double)) {   // FP64: n x {x, y, b, c, d}
+      for (size_t i = 0; i < c->x.size(); ++i) {
+        all.push_back(R(c->x[i])); all.push_back(R(c->y[i]));
+        all.push_back(R(b[i])); all.push_back(R(cc[i])); all.push_back(R(d[i]));
+      }
+    } else {   // FP32: n 16-byte records {y, b, c, d}, then the n grid points
+      for (size_t i = 0; i < c->x.size(); ++i) {
+        all.push_back(R(c->y[i])); all.push_back(R(b[i])); all.push_back(R(cc[i])); all.push_back(R(d[i]));
+      }
+      for (size_t i = 0; i < c->x.size(); ++i) all.push_back(R(c->x[i]));
+      while (all.size() % 4 != 0) all.push_back(R(0));   // the next spline's records stay 16-byte aligned
     }
   }
   const size_t base = img.Put(all.data(), all.size() * sizeof(R));

@@ -21,7 +21,8 @@ constexpr uint8_t kVacuum = 255;   // material id of vacuum voxels
 // allocation per precision.
 // ---------------------------------------------------------------------------
 template <class R>
-struct SplineT {       // natural cubic spline on a log-uniform grid: n x {x,y,b,c,d}
+struct SplineT {       // natural cubic spline on a log-uniform grid: n x {x,y,b,c,d} (FP64);
+                       // n x {y,b,c,d} then n x x, 16-byte aligned (FP32)
   const R* p;
   int n;
   R logMin, invLogDelta, emin, emaxm;   // emaxm = emax - 1e-6 (loader clamp)

@@ -161,9 +161,9 @@ __device__ __forceinline__ float SplineLe(const SplineT<float>& s, float e, floa
   const float lc = (ec == e) ? le : __logf(ec);
   int il = int((lc - s.logMin) * s.invLogDelta);
   il = il < 0 ? 0 : (il > s.n - 2 ? s.n - 2 : il);
-  const float* q = s.p + 5 * il;
-  const float xv = ec - q[0];
-  return fmaxf(1.0E-20f, q[1] + xv * (q[2] + xv * (q[3] + xv * q[4])));
+  const float4 q = reinterpret_cast<const float4*>(s.p)[il];   // y, b, c, d
+  const float xv = ec - s.p[4 * s.n + il];
+  return fmaxf(1.0E-20f, q.x + xv * (q.y + xv * (q.z + xv * q.w)));
 }
 
 // ---------------------------------------------------------------------------
@@ -694,7 +694,7 @@ __device__ __forceinline__ void InitElectron(const ETables& et, const PState& p,
 }
 
 __global__ void __launch_bounds__(256) ElectronPhase(PhaseArgs a) {
-  extern __shared__ float sdata[];
+  extern __shared__ __align__(16) float sdata[];   // 16-byte spline records
   __shared__ ETables et;
   __shared__ JobF sjobs[16];
   const bool fewJobs = a.njobs <= 16;
@@ -1158,7 +1158,9 @@ static_assert(kSlots <= kRingSize, "a ring holds every slot");
 constexpr uint32_t kRingOfCode = 0x432105u;
 using SlotRings = Rings<kRings>;
 
-__host__ __device__ constexpr size_t BlockPhaseStaticBytes() { return sizeof(SlotArrays) + sizeof(SlotRings); }
+__host__ __device__ constexpr size_t BlockPhaseStaticBytes() {
+  return (sizeof(SlotArrays) + sizeof(SlotRings) + 15) & ~size_t(15);   // staged tables start 16-byte aligned
+}
 
 // dynamic shared memory of the block kernel: slots, rings, the electron tables
 // when staged, then the depth tally of `depthBins` bins
