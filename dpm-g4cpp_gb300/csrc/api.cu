@@ -196,6 +196,34 @@ int BuildImage(const HostTables& h, DevTables<R>& T, void** dptr) {
   return DPMX_OK;
 }
 
+// the largest material id of m[0..n) other than vacuum, into *out (zeroed
+// before); m 16-byte aligned, read 16 bytes per thread
+__device__ __forceinline__ unsigned MaxNonVacuum(uint32_t w) {
+  unsigned best = 0;
+#pragma unroll
+  for (int b = 0; b < 4; ++b) {
+    const unsigned v = (w >> (8 * b)) & 0xffu;
+    best = max(best, v == kVacuum ? 0u : v);
+  }
+  return best;
+}
+__global__ void __launch_bounds__(256) MaxMaterialKernel(const uint8_t* m, unsigned long long n, unsigned* out) {
+  unsigned best = 0;
+  const unsigned long long n16 = n / 16;
+  const uint4* q = reinterpret_cast<const uint4*>(m);
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += stride) {
+    const uint4 w = q[i];
+    best = max(max(MaxNonVacuum(w.x), MaxNonVacuum(w.y)), max(MaxNonVacuum(w.z), MaxNonVacuum(w.w)));
+  }
+  if (blockIdx.x == 0 && threadIdx.x < n - n16 * 16) {   // the last n % 16 bytes
+    const unsigned v = m[n16 * 16 + threadIdx.x];
+    best = max(best, v == kVacuum ? 0u : v);
+  }
+  best = __reduce_max_sync(0xffffffffu, best);
+  if ((threadIdx.x & 31) == 0 && best > 0) atomicMax(out, best);
+}
+
 }  // namespace
 
 namespace dpmx {
@@ -334,20 +362,26 @@ int dpmx_phantom_voxels(const dpmx_tables* t, int nx, int ny, int nz, double vx,
     return Fail(DPMX_ERR_ARG, "phantom dimensions must be 1..2047 (x, y) and 1..1023 (z)");
   if (!(vx > 0 && vy > 0 && vz > 0)) return Fail(DPMX_ERR_ARG, "voxel sizes must be positive");
   const size_t n = size_t(nx) * ny * nz;
-  int worst = 0;   // the largest material id other than vacuum
-  for (size_t i = 0; i < n; ++i) {
-    const int m = mat[i] == kVacuum ? 0 : mat[i];
-    worst = m > worst ? m : worst;
-  }
-  if (worst >= t->h.nmat) return Fail(DPMX_ERR_ARG, "material id beyond the data set");
+  std::unique_ptr<dpmx_phantom, void (*)(dpmx_phantom*)> p(new dpmx_phantom(), dpmx_phantom_free);
+  p->tables = t;
+  p->kind = 1;
+  // the material ids, and after them (16-byte aligned) the slot where the
+  // device writes the largest id other than vacuum: checked on the GPU
+  const size_t nal = (n + 15) & ~size_t(15);
+  CK(cudaMalloc(&p->d_mat, nal + 16));
+  CK(cudaMemcpy(p->d_mat, mat, n, cudaMemcpyHostToDevice));
+  unsigned* dworst = reinterpret_cast<unsigned*>(p->d_mat + nal);
+  CK(cudaMemset(dworst, 0, sizeof(unsigned)));
+  const unsigned long long n16 = n / 16;
+  const int blocks = int(std::max<unsigned long long>(1, std::min<unsigned long long>((n16 + 255) / 256, 152ULL * 8)));
+  MaxMaterialKernel<<<blocks, 256>>>(p->d_mat, n, dworst);
+  CK(cudaGetLastError());
+  unsigned worst = 0;
+  CK(cudaMemcpy(&worst, dworst, sizeof(unsigned), cudaMemcpyDeviceToHost));
+  if (int(worst) >= t->h.nmat) return Fail(DPMX_ERR_ARG, "material id beyond the data set");
   auto lut = std::make_shared<std::vector<float>>(256, 0.0f);
   for (int m = 0; m < t->h.nmat; ++m) (*lut)[m] = float(t->h.density[m]);
   auto hostMat = std::make_shared<std::vector<uint8_t>>(mat, mat + n);
-  std::unique_ptr<dpmx_phantom> p(new dpmx_phantom());
-  p->tables = t;
-  p->kind = 1;
-  CK(cudaMalloc(&p->d_mat, n));
-  CK(cudaMemcpy(p->d_mat, mat, n, cudaMemcpyHostToDevice));
   GridGeom& g = p->grid;
   g.nx = nx; g.ny = ny; g.nz = nz;
   g.vx = vx; g.vy = vy; g.vz = vz;

@@ -120,3 +120,21 @@ def test_photon_kernels_give_the_same_histories(tables_wlb, dpm, kind):
     assert abs(a.sum() / b.sum() - 1.0) < 1e-5
     close = np.isclose(a, b, rtol=1e-4, atol=1e-9 * a.max())
     assert close.mean() > 0.999, close.mean()
+
+
+@pytest.mark.parametrize("shape", [(16, 16, 16), (7, 5, 3), (1, 1, 1), (33, 17, 9)])
+def test_material_ids_checked_on_upload(tables_wlb, dpm, shape):
+    """ids beyond the data set are refused wherever they sit (also in the
+    last bytes of an array whose size is no multiple of 16); vacuum is not"""
+    nmat = tables_wlb.num_materials
+    m = np.zeros(shape, dtype=np.uint8)
+    m.reshape(-1)[-1] = 255
+    dpm.Phantom.voxels(tables_wlb, m, 2.0).close()
+    m.reshape(-1)[-1] = nmat - 1
+    dpm.Phantom.voxels(tables_wlb, m, 2.0).close()
+    for pos in (0, m.size // 2, m.size - 1):
+        bad = np.zeros(shape, dtype=np.uint8)
+        bad.reshape(-1)[pos] = nmat
+        with pytest.raises(dpm.DpmxError) as e:
+            dpm.Phantom.voxels(tables_wlb, bad, 2.0)
+        assert e.value.code == dpm.ERR_ARG
