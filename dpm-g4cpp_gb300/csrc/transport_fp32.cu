@@ -4,13 +4,13 @@
 // transported in two phases: all photons (Woodcock tracking), then all
 // electrons/positrons (condensed-history stepping). Each phase is one
 // persistent launch, in one of two forms:
-//  * block-batched (the default): a block keeps a few hundred particles in shared
-//    memory; each particle runs its pending interaction, grouped by
-//    interaction type so that a warp runs one kind at a time, or is refilled
-//    from the phase's work counter, and then takes one step. Electrons wait
-//    in per-type rings that warps take from whenever they are free
-//    (ElectronPhaseB); photons move in block-wide iterations over compacted
-//    lists (PhotonPhaseB);
+//  * block-batched (the default): a block keeps a few hundred particles in
+//    shared memory, each waiting on a ring (a shared-memory queue) by what it
+//    does next; a warp takes up to 32 particles of one ring whenever it is
+//    free, runs that interaction (or refills them from the phase's work
+//    counter) and one step, and puts each on the ring of its next action, so
+//    a warp runs one kind of interaction at a time and no warp waits for
+//    another (ElectronPhaseB, PhotonPhaseB);
 //  * one particle per lane, refilled from the work counter when it ends
 //    (ElectronPhase, PhotonPhase).
 // Secondaries are appended to the next generation's queues with
