@@ -981,6 +981,7 @@ __global__ void __launch_bounds__(256) ElectronPhase(PhaseArgs a) {
 // ---------------------------------------------------------------------------
 constexpr int kSlots = 416;   // 3 blocks leave the SM 164 KB of shared memory and the rest to L1
 constexpr int kBlockMinBlocks = 3;      // resident blocks per SM the kernel is compiled for
+constexpr int kBlockThreads = 320;      // threads per block (a multiple of 32): 64 registers, 30 warps per SM
 constexpr bool kTablesInSmem = false;  // electron tables staged per block, else read through L1
 constexpr uint32_t kFHinge = 4u, kFPositron = 16u;
 constexpr int8_t kMatUnknown = -2;   // the slot's voxel changed since its material was read
@@ -1539,7 +1540,7 @@ __device__ __forceinline__ bool RefillSlot(const PhaseArgs& a, const ETables& et
 }
 
 template <int AGG>
-__global__ void __launch_bounds__(256, kBlockMinBlocks) ElectronPhaseB(PhaseArgs a) {
+__global__ void __launch_bounds__(kBlockThreads, kBlockMinBlocks) ElectronPhaseB(PhaseArgs a) {
   extern __shared__ __align__(16) unsigned char dyn[];
   SlotArrays& S = *reinterpret_cast<SlotArrays*>(dyn);
   SlotRings& R = *reinterpret_cast<SlotRings*>(dyn + sizeof(SlotArrays));
@@ -1630,6 +1631,7 @@ __global__ void __launch_bounds__(256, kBlockMinBlocks) ElectronPhaseB(PhaseArgs
 constexpr int kPSlots = 352;   // 4 blocks leave the SM 164 KB of shared memory and the rest to L1
 constexpr int kPhotonStepsPerTake = 3;   // Woodcock steps a photon takes per turn while they are delta steps
 constexpr int kPBlockMinBlocks = 4;
+constexpr int kPBlockThreads = 256;   // threads per block (a multiple of 32)
 
 // shared-memory state of the resident photons, in 16-byte records
 struct PSlotArrays {
@@ -1847,7 +1849,7 @@ __device__ __forceinline__ bool PhotonRefillSlot(const PhaseArgs& a, const JobF*
 }
 
 template <int AGG>
-__global__ void __launch_bounds__(256, kPBlockMinBlocks) PhotonPhaseB(PhaseArgs a) {
+__global__ void __launch_bounds__(kPBlockThreads, kPBlockMinBlocks) PhotonPhaseB(PhaseArgs a) {
   extern __shared__ __align__(16) unsigned char dyn[];
   PSlotArrays& S = *reinterpret_cast<PSlotArrays*>(dyn);
   PSlotRings& R = *reinterpret_cast<PSlotRings*>(dyn + sizeof(PSlotArrays));
@@ -2127,8 +2129,8 @@ int PhotonBlockBlocksPerSM() { return kPBlockMinBlocks; }
 
 cudaError_t LaunchPhotonPhaseBlock(const PhaseArgs& a, int blocks, cudaStream_t st) {
   const size_t smem = PhotonBlockSmemBytes(a.depthBins);
-  if (a.aggregate) PhotonPhaseB<1><<<blocks, 256, smem, st>>>(a);
-  else PhotonPhaseB<0><<<blocks, 256, smem, st>>>(a);
+  if (a.aggregate) PhotonPhaseB<1><<<blocks, kPBlockThreads, smem, st>>>(a);
+  else PhotonPhaseB<0><<<blocks, kPBlockThreads, smem, st>>>(a);
   return cudaGetLastError();
 }
 
@@ -2150,8 +2152,8 @@ cudaError_t PrepareBlockPhase(const DevTables<float>& T) {
 
 cudaError_t LaunchElectronPhaseBlock(const PhaseArgs& a, int blocks, cudaStream_t st) {
   const size_t smem = BlockPhaseSmemBytesFor(a.T, a.depthBins);
-  if (a.aggregate) ElectronPhaseB<1><<<blocks, 256, smem, st>>>(a);
-  else ElectronPhaseB<0><<<blocks, 256, smem, st>>>(a);
+  if (a.aggregate) ElectronPhaseB<1><<<blocks, kBlockThreads, smem, st>>>(a);
+  else ElectronPhaseB<0><<<blocks, kBlockThreads, smem, st>>>(a);
   return cudaGetLastError();
 }
 
