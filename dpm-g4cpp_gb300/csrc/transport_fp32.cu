@@ -976,8 +976,8 @@ __global__ void __launch_bounds__(256) ElectronPhase(PhaseArgs a) {
 // bounded-queue scheme of D. Vyukov: a producer waits until its cell is empty
 // for its lap, a consumer until it is full for its lap, so neither can take
 // the other lap's entry. At most one operation of each warp is pending on a
-// cell, so a cell never lags its newest reservation by more than 8 laps and 6
-// bits tell the laps apart.
+// cell, so a cell never lags its newest reservation by more laps than the
+// block has warps (at most 32), and 6 bits tell the laps apart.
 // ---------------------------------------------------------------------------
 constexpr int kSlots = 416;   // 3 blocks leave the SM 164 KB of shared memory and the rest to L1
 constexpr int kBlockMinBlocks = 3;      // resident blocks per SM the kernel is compiled for
@@ -998,11 +998,12 @@ struct SlotArrays {
   double acc[kSlots];
   int8_t mat[kSlots];   // material of the slot's current voxel (-1: vacuum)
 };
-constexpr long long kWaitCycles = 4LL << 30;   // bound of one wait (~2 s): then the block gives up
+constexpr long long kWaitCycles = 4LL << 30;   // bound of one wait (~2 s): then the warp gives up
 constexpr int kRingBits = 9;
 constexpr int kRingSize = 1 << kRingBits;   // cells per ring: at least the slots of a block
 constexpr uint32_t kCellSlot = uint32_t(kRingSize) - 1u, kCellFull = uint32_t(kRingSize);
 
+static_assert(kBlockThreads <= 32 * 32, "a ring cell's 6-bit lap covers at most 32 pending warps");
 template <int NR>
 struct Rings {
   uint16_t cell[NR][kRingSize];
