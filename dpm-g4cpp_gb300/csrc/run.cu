@@ -671,7 +671,8 @@ int Autotune(const dpmx_tables* t, const dpmx_job* jobs, int njobs, const Cfg ba
   // electron kernel; the photon kernel stays the run's (the two photon
   // kernels round some FP32 results differently)
   struct Cand { int threads, bps, agg, eblock, pblock; };
-  // the phase kernels are compiled for at most 256 threads per block
+  // (threads and blocks per SM shape the lane kernels, compiled for at most
+  // 256 threads per block; the block-batched kernels have fixed shapes)
   const Cand cands[] = {{256, 3, 0, 0, -1}, {256, 3, 1, 0, -1}, {256, 2, 0, 0, -1}, {128, 6, 0, 0, -1},
                         {256, 3, 0, 1, -1}, {256, 3, 1, 1, -1}, {256, 2, 0, 1, -1}};
   double bestMs = 1e30;
