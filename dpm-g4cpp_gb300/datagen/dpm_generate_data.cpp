@@ -25,10 +25,15 @@
 // Physics used in place of the Geant4 models (each is a published, analytic or
 // tabulated description; none is a port of Geant4 code):
 //   * elastic e- scattering: screened Rutherford cross section per element
-//     with Moliere's screening parameter; the inelastic Z(Z+1)/Z^2 scattering
-//     power correction is applied as in the reference (ElectronData.hh:219-221);
+//     with Moliere's screening parameter, times the Mott (spin) factor of
+//     McKinley and Feshbach (Phys. Rev. 74 (1948) 1759) in place of the
+//     partial-wave cross sections the reference takes from Geant4; the
+//     inelastic Z(Z+1)/Z^2 scattering power correction is applied as in the
+//     reference (ElectronData.hh:219-221);
 //   * collision stopping power: the restricted Berger-Seltzer (ICRU Report 37)
-//     formula for electrons with the Sternheimer-Peierls density effect;
+//     formula for electrons with the density effect of Sternheimer, Berger and
+//     Seltzer (At. Data Nucl. Data Tables 30 (1984) 261) for the tabulated
+//     materials, Sternheimer-Peierls' general formula for the others;
 //   * bremsstrahlung: the Seltzer-Berger scaled DCS tables (NIST, the same data
 //     the reference ships in SBTables/data/NIST_BREM) read from --sb-dir; the
 //     restricted radiative stopping power, the brem IMFP and the brem sampling
@@ -146,9 +151,17 @@ Material BuildMaterial(const MaterialDef& d) {
 }
 
 // ---------------------------------------------------------------------------
-// Elastic scattering: screened Rutherford DCS with Moliere's screening.
-//   dsigma/dmu = pi (Z r_e mc^2/(p beta c))^2 / (mu + A)^2, mu = (1-cos)/2
-//   sigma_el = pi k^2 / (A (1+A)),   sigma_1 = 2 pi k^2 [ln((1+A)/A) - 1/(1+A)]
+// Elastic scattering: screened Rutherford DCS with Moliere's screening, times
+// the McKinley-Feshbach ratio of the Mott to the Rutherford cross section,
+//   dsigma/dmu = pi k^2 R(mu) / (mu + A)^2,   k = Z r_e mc^2/(p beta c),
+//   R(mu) = 1 + pi alpha Z beta sqrt(mu) (1 - sqrt(mu)) - beta^2 mu,
+//   mu = (1-cos)/2 = sin^2(theta/2).
+// With K_p = int_0^1 mu^p / (mu + A)^2 dmu (closed forms below):
+//   sigma_el = pi k^2 [K_0 + c (K_1/2 - K_1) - beta^2 K_1]
+//   sigma_1  = 2 pi k^2 [K_1 + c (K_3/2 - K_2) - beta^2 K_2],  c = pi alpha Z beta
+// (R = 1 gives the screened Rutherford sigma_el = pi k^2/(A(1+A)) and
+// sigma_1 = 2 pi k^2 [ln((1+A)/A) - 1/(1+A)].) The factor lowers the first
+// transport cross section of water by 4-6 % at 0.2-5 MeV.
 // ---------------------------------------------------------------------------
 double MoliereA(int Z, double T) {
   const double pc2   = T * (T + 2.0 * kEMC2);            // (pc)^2
@@ -164,8 +177,15 @@ void ElasticXS(int Z, double T, double& sEl, double& sTr1) {
   const double beta2 = pc2 / ((T + kEMC2) * (T + kEMC2));
   const double k     = Z * kRe * kEMC2 / std::sqrt(pc2 * beta2);
   const double A     = MoliereA(Z, T);
-  sEl  = kPi * k * k / (A * (1.0 + A));
-  sTr1 = 2.0 * kPi * k * k * (std::log1p(1.0 / A) - 1.0 / (1.0 + A));
+  const double c     = kPi * kAlpha * Z * std::sqrt(beta2);
+  const double sa    = std::sqrt(A), at = std::atan(1.0 / sa), L = std::log1p(1.0 / A);
+  const double K0  = 1.0 / (A * (1.0 + A));
+  const double Kh  = at / sa - 1.0 / (1.0 + A);               // p = 1/2 (mu = t^2)
+  const double K1  = L - 1.0 / (1.0 + A);
+  const double K3h = 2.0 - 3.0 * sa * at + A / (1.0 + A);     // p = 3/2
+  const double K2  = 1.0 - 2.0 * A * L + A / (1.0 + A);
+  sEl  = kPi * k * k * (K0 + c * (Kh - K1) - beta2 * K1);
+  sTr1 = 2.0 * kPi * k * k * (K1 + c * (K3h - K2) - beta2 * K2);
 }
 
 // macroscopic elastic and first transport cross sections [1/mm] (no scpc)
@@ -281,9 +301,35 @@ void BremQuantities(const Material& m, const SBData& sb, double T, double gcut,
 // ---------------------------------------------------------------------------
 // Collision stopping power (restricted Berger-Seltzer formula, ICRU 37)
 // ---------------------------------------------------------------------------
+// density-effect parameters of Sternheimer, Berger and Seltzer (At. Data
+// Nucl. Data Tables 30 (1984) 261): the table's I [eV], Cbar, x0, x1, a, m,
+// delta0. Cbar = 1 + 2 ln(I / plasma energy) moves with the material's I.
+struct SternheimerParams { double I, C, x0, x1, a, m, d0; };
+const std::map<std::string, SternheimerParams>& SternheimerTable() {
+  static const std::map<std::string, SternheimerParams> t = {
+    {"G4_WATER", {75.0, 3.5017, 0.2400, 2.8004, 0.09116, 3.4773, 0.0}},
+    {"G4_AIR", {85.7, 10.5961, 1.7418, 4.2759, 0.10914, 3.3994, 0.0}},
+    {"G4_Ti", {233.0, 4.4450, 0.0957, 3.0386, 0.15643, 3.0302, 0.12}},
+    {"G4_W", {727.0, 5.4059, 0.2167, 3.4960, 0.15509, 2.8447, 0.14}},
+    {"G4_BONE_COMPACT_ICRU", {91.9, 3.3390, 0.0944, 3.0201, 0.05822, 3.6419, 0.0}},
+    {"G4_BONE_CORTICAL_ICRP", {106.4, 3.6488, 0.1161, 3.0919, 0.06198, 3.5919, 0.0}},
+    {"G4_LUNG_ICRP", {75.3, 3.4708, 0.2261, 2.8001, 0.08588, 3.5353, 0.0}},
+  };
+  return t;
+}
+
 double DensityEffect(const Material& m, double T) {
-  // Sternheimer-Peierls general parameters (condensed media unless rho < 0.01)
   const double I = m.def.I_eV;
+  const double x = std::log10(std::sqrt(T * (T + 2.0 * kEMC2)) / kEMC2);
+  const auto it = SternheimerTable().find(m.def.name);
+  if (it != SternheimerTable().end()) {
+    const SternheimerParams& p = it->second;
+    const double C = p.C + 2.0 * std::log(I / p.I);
+    if (x < p.x0) return p.d0 > 0.0 ? p.d0 * std::pow(10.0, 2.0 * (x - p.x0)) : 0.0;
+    if (x < p.x1) return 4.606 * x - C + p.a * std::pow(p.x1 - x, p.m);
+    return 4.606 * x - C;
+  }
+  // Sternheimer-Peierls general parameters (condensed media unless rho < 0.01)
   // plasma energy 28.816 sqrt(rho <Z/A>) eV, with rho <Z/A> = electrons per cm3 / N_A
   const double plasma = 28.816 * std::sqrt(m.nElectrons * 1.0e3 / kNA);
   const double Cbar = 1.0 + 2.0 * std::log(I / plasma);
@@ -303,7 +349,6 @@ double DensityEffect(const Material& m, double T) {
   }
   const double mexp = 3.0;
   const double a = (Cbar - 4.606 * x0) / std::pow(x1 - x0, mexp);
-  const double x = std::log10(std::sqrt(T * (T + 2.0 * kEMC2)) / kEMC2);
   if (x < x0) return 0.0;
   if (x < x1) return 4.606 * x - Cbar + a * std::pow(x1 - x, mexp);
   return 4.606 * x - Cbar;
