@@ -41,6 +41,18 @@ def test_batched_equals_separate(tables_wlb, dpm):
         assert st.histories == jobs[j].histories
 
 
+def test_many_jobs_equal_separate(tables_wlb, dpm):
+    """more jobs than the phase kernels keep in shared memory (16): their job
+    records are read from global memory, with the same results"""
+    jobs, keep = small_jobs(dpm, tables_wlb, n=20)
+    batched = dpm.run(tables_wlb, jobs, batches=2)
+    for j in (0, 7, 15, 16, 19):
+        alone = dpm.run(tables_wlb, [jobs[j]], batches=2).tally(0)[:2]
+        assert_same([batched.tally(j)[:2]], [alone])
+        st = batched.stats(j)
+        assert st.lost == 0 and st.residual_violations == 0 and st.histories == jobs[j].histories
+
+
 def test_schedule_invariance(tables_wlb, dpm):
     jobs, keep = small_jobs(dpm, tables_wlb, n=3)
     base = tallies(dpm.run(tables_wlb, jobs, batches=2), 3)
