@@ -27,8 +27,20 @@ int HistLen(int maxIz);
     }                                                                                          \
   } while (0)
 
+// a non-blocking stream owned by one call, destroyed with it
+struct StreamGuard {
+  cudaStream_t st = nullptr;
+  cudaError_t Create() { return cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking); }
+  ~StreamGuard() {
+    if (st) cudaStreamDestroy(st);
+  }
+};
+
 struct JobOut;
-// returns a job's device buffers (dose and dose^2 to the scratch pool, the rest freed)
+// returns a job's device buffers to the scratch pool. A run has finished all
+// its own work on them when dpmx_run returns, so this waits for nothing; the
+// caller's own use of dpmx_result_tally_device pointers must be complete
+// before the result is freed.
 void ReleaseJobOut(JobOut& o);
 
 struct JobOut {

@@ -189,15 +189,21 @@ int dpmx_influence_build(const dpmx_result* r, int job, double threshold, dpmx_c
   *out = nullptr;
   const JobOut& o = r->jobs[job];
   if (!o.d_btally) return Fail(DPMX_ERR_ARG, "the run did not tag beamlets (tag_beamlets = 0)");
+  // the build runs on a stream of its own and takes its temporaries from the
+  // stream-ordered allocator, so it waits for nothing but its own work
+  StreamGuard sg;
+  CK(sg.Create());
+  const cudaStream_t st = sg.st;
   const long long nvox = o.nvox;
   const int nb = o.nbeamlets;
   unsigned long long* dmax = nullptr;
-  CK(cudaMalloc(&dmax, sizeof(unsigned long long)));
-  CK(cudaMemset(dmax, 0, sizeof(unsigned long long)));
-  CK(LaunchMaxAbs(o.d_btally, nvox * nb, dmax, 0));
+  CK(cudaMallocAsync(&dmax, sizeof(unsigned long long), st));
+  CK(cudaMemsetAsync(dmax, 0, sizeof(unsigned long long), st));
+  CK(LaunchMaxAbs(o.d_btally, nvox * nb, dmax, st));
   unsigned long long bits = 0;
-  CK(cudaMemcpy(&bits, dmax, sizeof(bits), cudaMemcpyDeviceToHost));
-  cudaFree(dmax);
+  CK(cudaMemcpyAsync(&bits, dmax, sizeof(bits), cudaMemcpyDeviceToHost, st));
+  CK(cudaFreeAsync(dmax, st));
+  CK(cudaStreamSynchronize(st));
   double mx;
   std::memcpy(&mx, &bits, sizeof(mx));
   const double thr = threshold > 0.0 ? threshold * mx : 0.0;
@@ -206,49 +212,50 @@ int dpmx_influence_build(const dpmx_result* r, int job, double threshold, dpmx_c
   a->cols = nb;
   CK(cudaMalloc(&a->rowPtr, (nvox + 1) * sizeof(int64_t)));
   long long* cnt = nullptr;
-  CK(cudaMalloc(&cnt, (nvox + 1) * sizeof(long long)));
-  CK(cudaMemset(cnt, 0, (nvox + 1) * sizeof(long long)));
-  CK(LaunchCountNnz(o.d_btally, nvox, nb, thr, cnt, 0));
+  CK(cudaMallocAsync(&cnt, (nvox + 1) * sizeof(long long), st));
+  CK(cudaMemsetAsync(cnt, 0, (nvox + 1) * sizeof(long long), st));
+  CK(LaunchCountNnz(o.d_btally, nvox, nb, thr, cnt, st));
   size_t tmpBytes = 0;
-  cub::DeviceScan::ExclusiveSum(nullptr, tmpBytes, cnt, reinterpret_cast<long long*>(a->rowPtr), nvox + 1);
+  cub::DeviceScan::ExclusiveSum(nullptr, tmpBytes, cnt, reinterpret_cast<long long*>(a->rowPtr), nvox + 1, st);
   void* tmp = nullptr;
-  CK(cudaMalloc(&tmp, tmpBytes));
-  CK(cub::DeviceScan::ExclusiveSum(tmp, tmpBytes, cnt, reinterpret_cast<long long*>(a->rowPtr), nvox + 1));
-  cudaFree(tmp);
-  cudaFree(cnt);
+  CK(cudaMallocAsync(&tmp, tmpBytes, st));
+  CK(cub::DeviceScan::ExclusiveSum(tmp, tmpBytes, cnt, reinterpret_cast<long long*>(a->rowPtr), nvox + 1, st));
+  CK(cudaFreeAsync(tmp, st));
+  CK(cudaFreeAsync(cnt, st));
   long long nnz = 0;
-  CK(cudaMemcpy(&nnz, a->rowPtr + nvox, sizeof(long long), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpyAsync(&nnz, a->rowPtr + nvox, sizeof(long long), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
   a->nnz = nnz;
   CK(cudaMalloc(&a->col, std::max<long long>(1, nnz) * sizeof(int32_t)));
   CK(cudaMalloc(&a->val, std::max<long long>(1, nnz) * sizeof(float)));
-  CK(LaunchFillCsr(o.d_btally, nvox, nb, thr, reinterpret_cast<const long long*>(a->rowPtr), a->col, a->val, 0));
+  CK(LaunchFillCsr(o.d_btally, nvox, nb, thr, reinterpret_cast<const long long*>(a->rowPtr), a->col, a->val, st));
   // the same entries by column, in row order within a column
   const int nchunks = int((nvox + kColChunk - 1) / kColChunk);
   const long long nblk = (long long)nb * nchunks;
   long long* ccnt = nullptr;
   long long* coff = nullptr;
-  CK(cudaMalloc(&ccnt, nblk * sizeof(long long)));
-  CK(cudaMalloc(&coff, nblk * sizeof(long long)));
-  ColCountKernel<<<int(nblk), 256>>>(o.d_btally, nvox, nchunks, thr, ccnt);
+  CK(cudaMallocAsync(&ccnt, nblk * sizeof(long long), st));
+  CK(cudaMallocAsync(&coff, nblk * sizeof(long long), st));
+  ColCountKernel<<<int(nblk), 256, 0, st>>>(o.d_btally, nvox, nchunks, thr, ccnt);
   CK(cudaGetLastError());
   tmpBytes = 0;
-  cub::DeviceScan::ExclusiveSum(nullptr, tmpBytes, ccnt, coff, nblk);
-  CK(cudaMalloc(&tmp, tmpBytes));
-  CK(cub::DeviceScan::ExclusiveSum(tmp, tmpBytes, ccnt, coff, nblk));
-  cudaFree(tmp);
+  cub::DeviceScan::ExclusiveSum(nullptr, tmpBytes, ccnt, coff, nblk, st);
+  CK(cudaMallocAsync(&tmp, tmpBytes, st));
+  CK(cub::DeviceScan::ExclusiveSum(tmp, tmpBytes, ccnt, coff, nblk, st));
+  CK(cudaFreeAsync(tmp, st));
   CK(cudaMalloc(&a->colPtr, (nb + 1) * sizeof(int64_t)));
   CK(cudaMalloc(&a->rowT, std::max<long long>(1, nnz) * sizeof(int32_t)));
   CK(cudaMalloc(&a->valT, std::max<long long>(1, nnz) * sizeof(float)));
-  ColFillKernel<<<int(nblk), 256>>>(o.d_btally, nvox, nchunks, thr, coff, a->rowT, a->valT);
+  ColFillKernel<<<int(nblk), 256, 0, st>>>(o.d_btally, nvox, nchunks, thr, coff, a->rowT, a->valT);
   CK(cudaGetLastError());
-  ColPtrKernel<<<1, 256>>>(coff, nb, nchunks, nnz, a->colPtr);
+  ColPtrKernel<<<1, 256, 0, st>>>(coff, nb, nchunks, nnz, a->colPtr);
   CK(cudaGetLastError());
   // enough column slices to fill the GPU with blocks of A^T y
   a->splits = int(std::max<long long>(1, (4LL * 152 * 4 + nb - 1) / nb));
   CK(cudaMalloc(&a->partial, (long long)nb * a->splits * sizeof(double)));
-  CK(cudaDeviceSynchronize());
-  cudaFree(ccnt);
-  cudaFree(coff);
+  CK(cudaFreeAsync(ccnt, st));
+  CK(cudaFreeAsync(coff, st));
+  CK(cudaStreamSynchronize(st));
   *out = a.release();
   return DPMX_OK;
 }

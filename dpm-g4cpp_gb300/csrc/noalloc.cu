@@ -15,8 +15,10 @@
 // contents, so each call clears the parts that must start at zero. Calls that
 // overlap on the GPU (on different streams or host threads) race on it and
 // must be serialised by the caller. The first call on a device looks the
-// array's device address up (cudaGetSymbolAddress); make that first call
-// before any stream capture.
+// array's device address up (cudaGetSymbolAddress) and keeps it for the life
+// of the process; make that first call before any stream capture. A
+// cudaDeviceReset destroys the array with the context, so no reset may come
+// between calls. Each call synchronises its stream before it returns.
 #include <cmath>
 #include <mutex>
 #include <string>
@@ -29,6 +31,7 @@ namespace {
 // scratch layout (bytes): [0, 256) RunCounters, [256, 512) deepest bin (int),
 // [512, 1024) material densities, [1024, ...) batch tally of kNoAllocMaxBins bins
 constexpr int kNoAllocMaxBins = 8192;
+constexpr int kSlabMaxBins = 1023;       // the depth-bin limit of dpmx_phantom_slab
 constexpr size_t kOffCounters = 0, kOffMaxIz = 256, kOffDensity = 512, kOffTally = 1024;
 constexpr size_t kScratchBytes = kOffTally + size_t(kNoAllocMaxBins) * sizeof(double);
 static_assert(sizeof(RunCounters) <= 256, "counters must fit their scratch slot");
@@ -69,12 +72,13 @@ extern "C" int dpmx_simulate_noalloc(const dpmx_tables* t, int nprimary, double 
   if (bins > kNoAllocMaxBins)
     return Fail(DPMX_ERR_ARG, "dpmx_simulate_noalloc: bins = " + std::to_string(bins) + " exceeds the maximum of " +
                                   std::to_string(kNoAllocMaxBins) + " depth bins of its fixed scratch");
-  // depth bins the reference world needs (z <= 100 mm): as dpmx_phantom_slab
+  // depth bins the reference world needs (z <= 100 mm), with the same limit
+  // as dpmx_phantom_slab so that both entry points accept the same voxel sizes
   const int need = int(std::ceil((100.0 - 0.5 * lbox) / lbox - 1.0e-9)) + 1;
+  if (need > kSlabMaxBins) return Fail(DPMX_ERR_ARG, "voxel size too small for the slab geometry");
   if (bins < need)
     return Fail(DPMX_ERR_ARG, "dpmx_simulate_noalloc: bins = " + std::to_string(bins) + " is below the " +
                                   std::to_string(need) + " depth bins of a " + std::to_string(lbox) + " mm geometry");
-  if (need > kNoAllocMaxBins) return Fail(DPMX_ERR_ARG, "dpmx_simulate_noalloc: voxel size too small for the scratch");
   for (int iz = 0; iz < need; ++iz)
     if (SlabMaterialAt(geom_index, 1.0 / lbox, iz) >= t->h.nmat)
       return Fail(DPMX_ERR_ARG, "the data set has fewer materials than the slab geometry needs");

@@ -582,7 +582,7 @@ int RunFp64(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
   return DPMX_OK;
 }
 
-int PrepareOutputs(const dpmx_job* jobs, int njobs, bool tag, std::vector<JobOut>& outs) {
+int PrepareOutputs(const dpmx_job* jobs, int njobs, bool tag, cudaStream_t st, std::vector<JobOut>& outs) {
   outs.assign(njobs, JobOut());
   for (int j = 0; j < njobs; ++j) {
     const dpmx_phantom* ph = jobs[j].phantom;
@@ -602,15 +602,17 @@ int PrepareOutputs(const dpmx_job* jobs, int njobs, bool tag, std::vector<JobOut
     CK(ScratchPool::Instance().Get(o.tallySize * sizeof(double), &p));
     o.d_dose2 = static_cast<double*>(p);
     if (o.slab) {
-      CK(cudaMalloc(&o.d_steps, o.tallySize * sizeof(double)));
-      CK(cudaMemset(o.d_steps, 0, o.tallySize * sizeof(double)));
+      CK(ScratchPool::Instance().Get(o.tallySize * sizeof(double), &p));
+      o.d_steps = static_cast<double*>(p);
+      CK(cudaMemsetAsync(o.d_steps, 0, o.tallySize * sizeof(double), st));
     }
     if (tag && !o.slab) {
       const dpmx_source& s = jobs[j].source;
       o.nbeamlets = (s.shape == 2) ? std::max(1, s.nbx * s.nby) : 1;
       const size_t n = size_t(o.nbeamlets) * size_t(o.nvox);
-      CK(cudaMalloc(&o.d_btally, n * sizeof(double)));
-      CK(cudaMemset(o.d_btally, 0, n * sizeof(double)));
+      CK(ScratchPool::Instance().Get(n * sizeof(double), &p));
+      o.d_btally = static_cast<double*>(p);
+      CK(cudaMemsetAsync(o.d_btally, 0, n * sizeof(double), st));
     }
   }
   return DPMX_OK;
@@ -686,7 +688,7 @@ int Autotune(const dpmx_tables* t, const dpmx_job* jobs, int njobs, const Cfg ba
     if (c.pblock >= 0) cfg.pblock = c.pblock;
     cfg.chunk = sample;
     std::vector<JobOut> outs;
-    if (int rc = PrepareOutputs(sj.data(), njobs, false, outs)) return rc;
+    if (int rc = PrepareOutputs(sj.data(), njobs, false, st, outs)) return rc;
     double ms = 0;
     long long nl = 0;
     const int rc = RunFp32(t, sj.data(), njobs, 1, cfg, false, false, st, outs, &ms, &nl);
@@ -702,12 +704,10 @@ int Autotune(const dpmx_tables* t, const dpmx_job* jobs, int njobs, const Cfg ba
 
 namespace dpmx {
 void ReleaseJobOut(JobOut& o) {
-  // nothing may still write the pooled buffers when they go back
-  cudaDeviceSynchronize();
-  if (o.d_dose) ScratchPool::Instance().Put(o.d_dose);
-  if (o.d_dose2) ScratchPool::Instance().Put(o.d_dose2);
-  cudaFree(o.d_steps);
-  cudaFree(o.d_btally);
+  // every run synchronises its stream before it returns, so no library work
+  // still uses these blocks: they go back to the pool without a device-wide wait
+  for (double* p : {o.d_dose, o.d_dose2, o.d_steps, o.d_btally})
+    if (p) ScratchPool::Instance().Put(p);
   o.d_dose = o.d_dose2 = o.d_steps = o.d_btally = nullptr;
 }
 }  // namespace dpmx
@@ -732,7 +732,7 @@ int dpmx_run(const dpmx_tables* t, const dpmx_job* jobs, int njobs, const dpmx_r
   std::unique_ptr<dpmx_result> r(new dpmx_result());
   r->batches = o.batches;
   const bool tag = o.tag_beamlets && o.precision == DPMX_FP32_EVENT;
-  int rc = PrepareOutputs(jobs, njobs, tag, r->jobs);
+  int rc = PrepareOutputs(jobs, njobs, tag, st, r->jobs);
   if (!rc) {
     if (o.precision == DPMX_FP64_PLAIN) {
       rc = RunFp64(t, jobs, njobs, o.batches, true, st, r->jobs, &r->ms, &r->launches, nullptr);
@@ -987,7 +987,7 @@ int dpmx_simulate_histories(const dpmx_tables* t, int nprimary, double eprimary,
   job.histories = nprimary;
   job.seed = seed;
   std::vector<JobOut> outs;
-  int rc = PrepareOutputs(&job, 1, false, outs);
+  int rc = PrepareOutputs(&job, 1, false, 0, outs);
   double* d_he = nullptr;
   if (!rc && cudaMalloc(&d_he, std::max(1, nprimary) * sizeof(double)) != cudaSuccess) rc = Fail(DPMX_ERR_NOMEM, "alloc");
   double ms = 0;

@@ -191,11 +191,14 @@ int dpmx_simulate(const dpmx_tables* t, int nprimary, double eprimary, int isele
  * cudaMalloc would synchronise the device). No counterpart in the reference.
  * edep, edep2 (may be NULL) and steps are caller-owned DEVICE arrays of `bins`
  * doubles (depth bins of lbox); bins must cover the geometry's depth bins and
- * may not exceed 8192. The library's scratch is a fixed 65 KB device array
- * shared by all calls: calls that overlap on the GPU race and must be
- * serialised; the first call on a device looks the array up and should come
- * before any stream capture. Runs on `stream` (NULL: default stream) and
- * returns after it has finished. */
+ * may not exceed 8192; lbox has the same lower limit as dpmx_phantom_slab
+ * (at most 1023 depth bins). The library's scratch is a fixed 65 KB device
+ * array shared by all calls: calls that overlap on the GPU race and must be
+ * serialised. The first call on a device looks the array up (and keeps its
+ * address until the process exits, so no cudaDeviceReset may come between
+ * calls); it should come before any stream capture. Runs on `stream` (NULL:
+ * default stream), synchronises that stream and reads the run's counters
+ * back before it returns. */
 int dpmx_simulate_noalloc(const dpmx_tables* t, int nprimary, double eprimary, int iselectron, double lbox,
                           int geom_index, uint64_t seed, double* edep, double* edep2, double* steps, int bins,
                           int* hist_len, void* stream);

@@ -4,9 +4,10 @@
 #   libdpm_ref.so  : Simulation/src/*.cc + oracle/ref_shim.cc (C entry points)
 #   dpm_Simulate   : the reference CLI (dpm_Simulate.cc), glibc getopt_long
 # The outputs are test infrastructure only (golden vectors, oracle pinning).
-# Usage: oracle/build_ref.sh [reference-root]   (default /root/reference)
+# Usage: oracle/build_ref.sh [reference-root]
+#   (default $DPM_REFERENCE_ROOT, else the build container's mount point)
 set -euo pipefail
-REF="${1:-/root/reference}"
+REF="${1:-${DPM_REFERENCE_ROOT:-/root/reference}}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 if [ ! -d "$REF/Simulation/src" ]; then

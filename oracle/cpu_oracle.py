@@ -22,13 +22,24 @@ def build(force=False):
     """Compiles the oracle restatement with g++ (IEEE arithmetic, no contraction)."""
     src = os.path.join(HERE, "dpm_oracle.cc")
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
-        subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-shared", "-fPIC", src, "-o", LIB],
+        # compile beside the library and rename: a process that loads it
+        # meanwhile sees the old file or the new one, never a partial one
+        tmp = "%s.%d.tmp" % (LIB, os.getpid())
+        subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-shared", "-fPIC", src, "-o", tmp],
                        check=True)
+        os.replace(tmp, LIB)
     return LIB
 
 
-def build_ref(reference_root="/root/reference"):
+def reference_root():
+    """The reference checkout the oracle recipes read: $DPM_REFERENCE_ROOT,
+    else the path where the build container mounts it."""
+    return os.environ.get("DPM_REFERENCE_ROOT", "/root/reference")
+
+
+def build_ref(reference_root=None):
     """Builds oracle/_ref from the reference sources if they are present."""
+    reference_root = reference_root or globals()["reference_root"]()
     if not os.path.isdir(os.path.join(reference_root, "Simulation", "src")):
         return None
     subprocess.run([os.path.join(HERE, "build_ref.sh"), reference_root], check=True, stdout=subprocess.DEVNULL)

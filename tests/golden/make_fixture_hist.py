@@ -4,14 +4,14 @@ dpm_Simulate on Geant4-built data, 15 MeV e- pencil beam, water/Ti/bone/water
 slabs of config 3, 1 mm bins). Columns: bin index, depth [cm], energy deposit
 [MeV cm2/g] per history, scoring steps per history; plus the mean deposit.
 
-    python tests/golden/make_fixture_hist.py [reference-root]
+    python tests/golden/make_fixture_hist.py [reference-root]   (default $DPM_REFERENCE_ROOT)
 """
 import os
 import sys
 
 import numpy as np
 
-ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("DPM_REFERENCE_ROOT", "/root/reference")
 src = os.path.join(ref, "tests", "WaterTiBoneWater_15MeV", "hist.sim")
 rows, mean = [], None
 for line in open(src):

@@ -33,7 +33,8 @@ SLAB_RUNS = [
 ]
 
 
-def main(ref_root="/root/reference"):
+def main(ref_root=None):
+    ref_root = ref_root or cpu_oracle.reference_root()
     cpu_oracle.build_ref(ref_root)
     ref = cpu_oracle.Reference(DATA)
     rng = np.random.default_rng(2024)

@@ -43,6 +43,18 @@ def test_noalloc_matches_allocating_entry_point(tables_c3, dpm, first):
         assert not ed[hl:].any() and not st[hl:].any()
 
 
+def test_noalloc_at_the_smallest_voxel_size(tables_c3, dpm):
+    """0.1 mm voxels: 1001 depth bins, close to the 1023-bin limit that both
+    entry points share; a buffer of the full 8192 bins is accepted."""
+    lib = dpm.library()
+    for _ in range(2):
+        ref_e, ref_s = dpm.simulate(tables_c3, 300, 15.0, True, 0.1, 3, seed=43, precision=dpm.FP64_PLAIN)
+        ed, ed2, st, hl = call_noalloc(lib, tables_c3, 300, 15.0, True, 0.1, 3, 43, bins=8192)
+        assert hl == len(ref_e) and hl > 900
+        np.testing.assert_allclose(ed[:hl], ref_e, rtol=1e-12, atol=1e-12)
+        np.testing.assert_array_equal(st[:hl], ref_s)
+
+
 def test_noalloc_rejects_sizes_beyond_its_scratch(tables_c3, dpm):
     lib = dpm.library()
     import torch
@@ -53,3 +65,9 @@ def test_noalloc_rejects_sizes_beyond_its_scratch(tables_c3, dpm):
     assert b"8192" in lib.dpmx_last_error()
     rc = lib.dpmx_simulate_noalloc(tables_c3.handle, 10, 15.0, 1, 1.0, 3, 1, p, None, p, 16, None, None)
     assert rc == dpm.ERR_ARG    # fewer bins than the 1 mm geometry needs
+    # below 0.098 mm the slab geometry needs more than 1023 depth bins: both
+    # entry points reject it
+    rc = lib.dpmx_simulate_noalloc(tables_c3.handle, 10, 15.0, 1, 0.09, 3, 1, p, None, p, 8192, None, None)
+    assert rc == dpm.ERR_ARG and b"too small" in lib.dpmx_last_error()
+    with pytest.raises(dpm.DpmxError):
+        dpm.simulate(tables_c3, 10, 15.0, True, 0.09, 3, seed=1)
