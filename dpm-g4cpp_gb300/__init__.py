@@ -24,7 +24,8 @@ from dataclasses import dataclass, field
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "lib", "libdpmx.so")
+# the in-tree build (builder.py), or another build of the same library named by $DPMX_LIBRARY
+LIB_PATH = os.environ.get("DPMX_LIBRARY") or os.path.join(_HERE, "lib", "libdpmx.so")
 
 FP64_PLAIN = 0
 FP32_EVENT = 1
@@ -67,6 +68,7 @@ class _Stats(C.Structure):
 
 _lib = None
 _dp = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
 
 
 def library():
@@ -129,6 +131,9 @@ def library():
         "dpmx_csr_free": (None, [P]),
         "dpmx_ring_selftest": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_uint64, C.c_longlong,
                                          C.POINTER(C.c_longlong)]),
+        "dpmx_rng_eval": (C.c_int, [_u32p, _u32p, C.c_int, _u32p,
+                                    np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS"), _dp]),
+        "dpmx_atomic_roof": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -153,7 +158,8 @@ def exported_symbols():
             "dpmx_result_free", "dpmx_scratch_release", "dpmx_result_write", "dpmx_model_histogram",
             "dpmx_simulate", "dpmx_simulate_noalloc", "dpmx_write_hist", "dpmx_sampler_eval", "dpmx_table_eval", "dpmx_simulate_histories",
             "dpmx_influence_build", "dpmx_csr_shape", "dpmx_csr_device", "dpmx_csr_spmv", "dpmx_csr_spmv_t",
-            "dpmx_csr_download", "dpmx_csr_free", "dpmx_ring_selftest"]
+            "dpmx_csr_download", "dpmx_csr_free", "dpmx_ring_selftest", "dpmx_rng_eval",
+            "dpmx_atomic_roof"]
 
 
 class Tables:
@@ -429,6 +435,31 @@ def ring_selftest(blocks=152, nslots=416, rounds=1000, seed=1, probe_cycles=1 <<
     out = (C.c_longlong * 4)()
     _check(library().dpmx_ring_selftest(int(blocks), int(nslots), int(rounds), int(seed), int(probe_cycles), out))
     return tuple(int(v) for v in out)
+
+
+def rng_eval(counters, keys):
+    """Philox-4x32-10 on the GPU (dpmx_rng_eval): for counters (n, 4) and keys
+    (n, 2) uint32, returns the blocks (n, 4) uint32, the FP32 transport's
+    uniforms of each word (n, 4) float32 and the FP64 form's uniforms of each
+    word pair (n, 2) float64."""
+    c = np.ascontiguousarray(counters, dtype=np.uint32).reshape(-1, 4)
+    k = np.ascontiguousarray(keys, dtype=np.uint32).reshape(-1, 2)
+    n = len(c)
+    if len(k) != n:
+        raise DpmxError(ERR_ARG, "one key per counter")
+    w = np.zeros((n, 4), dtype=np.uint32)
+    f = np.zeros((n, 4), dtype=np.float32)
+    d = np.zeros((n, 2), dtype=np.float64)
+    _check(library().dpmx_rng_eval(c.reshape(-1), k.reshape(-1), n, w.reshape(-1), f.reshape(-1), d.reshape(-1)))
+    return w, f, d
+
+
+def atomic_roof(nbins=1 << 22, per_thread=256):
+    """FP64 atomicAdd operations per second into an L2-resident array (the
+    dose tally's roof), measured on the current GPU."""
+    v = C.c_double(0.0)
+    _check(library().dpmx_atomic_roof(int(nbins), int(per_thread), C.byref(v)))
+    return v.value
 
 
 def scratch_release():

@@ -47,8 +47,22 @@ __device__ __forceinline__ uint4 philox(uint4 c, uint32_t k0, uint32_t k1) {
   return c;
 }
 
+// Philox words to uniforms on the open interval (0,1).
+// FP64: two words give 53 bits, the lowest forced to 1: (bits | 1) * 2^-53.
+__device__ __forceinline__ double UniformF64(uint32_t lo, uint32_t hi) {
+  const uint64_t bits = (uint64_t(hi) << 32) | lo;
+  return double((bits >> 11) | 1ull) * (1.0 / 9007199254740992.0);
+}
+// FP32: one word, converted with rounding toward zero and scaled by 2^-32, so
+// small uniforms keep all 32 bits of resolution (the smallest is 2^-32, and
+// -ln U reaches 22.2 mean free paths) while the largest, 1 - 2^-24, stays
+// below 1.
+__device__ __forceinline__ float UniformF32(uint32_t x) {
+  return __uint2float_rz(x | 1u) * 2.3283064365386963e-10f;
+}
+
 // One stream per history for the FP64 form: draw k of history h comes from
-// Philox block k/2 at counter {k/2, 0, 0, h}; two 32-bit words make a 52-bit
+// Philox block k/2 at counter {k/2, 0, 0, h}; two 32-bit words make a 53-bit
 // uniform on the open interval (0,1).
 struct HistoryRng {
   uint32_t k0, k1, hist, block;
@@ -65,8 +79,7 @@ struct HistoryRng {
     uint32_t lo, hi;
     if (have == 2) { lo = w.x; hi = w.y; } else { lo = w.z; hi = w.w; }
     --have;
-    const uint64_t bits = (uint64_t(hi) << 32) | lo;
-    return double((bits >> 11) | 1ull) * (1.0 / 9007199254740992.0);
+    return UniformF64(lo, hi);
   }
 };
 

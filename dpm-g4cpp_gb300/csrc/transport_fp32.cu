@@ -54,8 +54,8 @@ constexpr unsigned kMaxElectronSteps = 1u << 24;
 
 // ---------------------------------------------------------------------------
 // per-particle random numbers: Philox key = job seed, counter =
-// {block, uid_lo, uid_hi, history}; 4 uniforms per block, 23 random bits each
-// on the open interval (0,1)
+// {block, uid_lo, uid_hi, history}; 4 uniforms per block (UniformF32: one word
+// each, on the open interval (0,1))
 // ---------------------------------------------------------------------------
 struct PRng {
   uint32_t k0, k1, ctr, ulo, uhi, hist;
@@ -72,7 +72,7 @@ struct PRng {
     const uint32_t x = w.x;
     w.x = w.y; w.y = w.z; w.z = w.w;
     --have;
-    return float((x >> 8) | 1u) * 5.9604644775390625e-8f;
+    return UniformF32(x);
   }
   // stream id of the k-th secondary created at the current stream position
   __device__ __forceinline__ void Child(int k, uint32_t& lo, uint32_t& hi) const {

@@ -120,3 +120,95 @@ extern "C" int dpmx_ring_selftest(int blocks, int nslots, int rounds, uint64_t s
   for (int i = 0; i < 4; ++i) out[i] = (long long)h[i];
   return DPMX_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Random-number hook: the Philox-4x32-10 block of each (counter, key) and the
+// uniforms both transport forms make of it (UniformF32 of each word,
+// UniformF64 of each word pair), for known-answer tests
+// ---------------------------------------------------------------------------
+namespace dpmx {
+namespace {
+__global__ void RngEvalKernel(const uint32_t* ctr, const uint32_t* key, int n, uint32_t* words, float* u32,
+                              double* u64) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint4 c = make_uint4(ctr[4 * i], ctr[4 * i + 1], ctr[4 * i + 2], ctr[4 * i + 3]);
+  const uint4 w = philox(c, key[2 * i], key[2 * i + 1]);
+  words[4 * i] = w.x; words[4 * i + 1] = w.y; words[4 * i + 2] = w.z; words[4 * i + 3] = w.w;
+  u32[4 * i] = UniformF32(w.x); u32[4 * i + 1] = UniformF32(w.y);
+  u32[4 * i + 2] = UniformF32(w.z); u32[4 * i + 3] = UniformF32(w.w);
+  u64[2 * i] = UniformF64(w.x, w.y);
+  u64[2 * i + 1] = UniformF64(w.z, w.w);
+}
+
+// FP64 atomicAdd throughput into an L2-resident array: the roof of the dose
+// tally (one FP64 atomic per deposit). Every thread adds to pseudo-random bins
+// of `nbins` doubles; the launch fills the GPU (8 blocks of 256 per SM).
+__global__ void __launch_bounds__(256) AtomicRoofKernel(double* bins, uint32_t nbins, int per) {
+  uint32_t x = (blockIdx.x * blockDim.x + threadIdx.x) * 0x9E3779B9u + 1u;
+  for (int k = 0; k < per; ++k) {
+    x ^= x << 13; x ^= x >> 17; x ^= x << 5;     // xorshift32
+    atomicAdd(bins + (x % nbins), 1.0);
+  }
+}
+}  // namespace
+}  // namespace dpmx
+
+extern "C" int dpmx_rng_eval(const uint32_t* counters, const uint32_t* keys, int n, uint32_t* words, float* u32,
+                             double* u64) {
+  if (n < 0 || (n > 0 && (!counters || !keys || !words || !u32 || !u64)))
+    return Fail(DPMX_ERR_ARG, "bad random-number hook arguments");
+  if (n == 0) return DPMX_OK;
+  // one allocation: counters (4n), keys (2n), words (4n) as uint32, u32 (4n), u64 (2n)
+  const size_t bytes = size_t(n) * (10 * sizeof(uint32_t) + 4 * sizeof(float) + 2 * sizeof(double));
+  unsigned char* d = nullptr;
+  CK(cudaMalloc(&d, bytes));
+  uint32_t* dc = reinterpret_cast<uint32_t*>(d);
+  uint32_t* dk = dc + 4 * size_t(n);
+  uint32_t* dw = dk + 2 * size_t(n);
+  float* df = reinterpret_cast<float*>(dw + 4 * size_t(n));
+  double* dd = reinterpret_cast<double*>(df + 4 * size_t(n));   // 56n bytes in: 8-byte aligned
+  cudaError_t e = cudaMemcpy(dc, counters, 4 * size_t(n) * sizeof(uint32_t), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dk, keys, 2 * size_t(n) * sizeof(uint32_t), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    RngEvalKernel<<<(n + 255) / 256, 256>>>(dc, dk, n, dw, df, dd);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(words, dw, 4 * size_t(n) * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(u32, df, 4 * size_t(n) * sizeof(float), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(u64, dd, 2 * size_t(n) * sizeof(double), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  CK(e);
+  return DPMX_OK;
+}
+
+extern "C" int dpmx_atomic_roof(int nbins, int per_thread, double* atomics_per_s) {
+  if (nbins < 1 || nbins > (1 << 26) || per_thread < 1 || per_thread > (1 << 16) || !atomics_per_s)
+    return Fail(DPMX_ERR_ARG, "bad atomic-roof arguments");
+  StreamGuard sg;
+  CK(sg.Create());
+  double* d = nullptr;
+  CK(cudaMallocAsync(&d, size_t(nbins) * sizeof(double), sg.st));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t e = cudaMemsetAsync(d, 0, size_t(nbins) * sizeof(double), sg.st);
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  const int blocks = NumSMs() * 8;
+  if (e == cudaSuccess) {
+    AtomicRoofKernel<<<blocks, 256, 0, sg.st>>>(d, uint32_t(nbins), per_thread);   // warm-up
+    cudaEventRecord(e0, sg.st);
+    AtomicRoofKernel<<<blocks, 256, 0, sg.st>>>(d, uint32_t(nbins), per_thread);
+    cudaEventRecord(e1, sg.st);
+    e = cudaGetLastError();
+  }
+  float ms = 0.f;
+  if (e == cudaSuccess) e = cudaStreamSynchronize(sg.st);
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  cudaFreeAsync(d, sg.st);
+  cudaStreamSynchronize(sg.st);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  CK(e);
+  *atomics_per_s = double(blocks) * 256.0 * per_thread / (ms * 1e-3);
+  return DPMX_OK;
+}

@@ -221,6 +221,19 @@ int dpmx_table_eval(const dpmx_tables* t, int precision, int quantity, int imat,
 int dpmx_simulate_histories(const dpmx_tables* t, int nprimary, double eprimary, int iselectron, double lbox,
                             int geom_index, uint64_t seed, double* hist_edep, double* edep_hist, int cap);
 
+/* random numbers (replaces the reference's global mt19937, Random.hh:10-12,
+ * Random.cc:3-4, by counter-based Philox-4x32-10, Salmon et al. SC'11): for
+ * each i, the block philox(counters[4i..4i+3], keys[2i..2i+1]) into
+ * words[4i..], the FP32 transport's uniform of each word into u32[4i..], and
+ * the FP64 form's uniform of each word pair into u64[2i..]; host arrays */
+int dpmx_rng_eval(const uint32_t* counters, const uint32_t* keys, int n, uint32_t* words, float* u32,
+                  double* u64);
+/* measurement hook: FP64 atomicAdd throughput into `nbins` doubles (kept in
+ * L2 when nbins * 8 B fits it), every thread of a GPU-filling launch adding to
+ * per_thread pseudo-random bins; the roof of the dose tally's one atomic per
+ * deposit. No reference counterpart. */
+int dpmx_atomic_roof(int nbins, int per_thread, double* atomics_per_s);
+
 /* ---- model validation (the reference's modelValidationTests, testAPI.cc) ---- */
 #define DPMX_MODEL_BREM 0
 #define DPMX_MODEL_MOLLER 1

@@ -72,8 +72,19 @@ def lib():
                                             C.c_double, C.c_double, C.c_int, C.c_double, C.c_double, C.c_double,
                                             C.c_double, C.c_int, C.c_int, C.c_longlong, C.c_longlong, C.c_uint64, _dp,
                                             _dp, _dp, C.c_void_p]
+        u32 = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
+        L.oracle_philox.argtypes = [u32, u32, u32, C.c_int]
         _lib = L
     return _lib
+
+
+def philox(counters, keys):
+    """Philox-4x32-10 blocks of the oracle for counters (n, 4) and keys (n, 2)."""
+    c = np.ascontiguousarray(counters, dtype=np.uint32).reshape(-1)
+    k = np.ascontiguousarray(keys, dtype=np.uint32).reshape(-1)
+    out = np.zeros_like(c)
+    lib().oracle_philox(c, k, out, len(c) // 4)
+    return out.reshape(-1, 4)
 
 
 class Oracle:

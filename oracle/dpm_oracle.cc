@@ -969,6 +969,15 @@ int oracle_num_materials(void* h) { return static_cast<Tables*>(h)->nmat; }
 double oracle_density(void* h, int im) { return static_cast<Tables*>(h)->density[im]; }
 double oracle_cut(void* h, int which) { auto* T = static_cast<Tables*>(h); return which == 0 ? T->ecut : T->gcut; }
 
+// Philox-4x32-10 blocks: out[4i..] = philox(ctr[4i..], key[2i..])
+void oracle_philox(const uint32_t* ctr, const uint32_t* key, uint32_t* out, int n) {
+  for (int i = 0; i < n; ++i) {
+    uint32_t c[4] = {ctr[4 * i], ctr[4 * i + 1], ctr[4 * i + 2], ctr[4 * i + 3]};
+    Philox(c, key[2 * i], key[2 * i + 1]);
+    for (int j = 0; j < 4; ++j) out[4 * i + j] = c[j];
+  }
+}
+
 // quantity codes: 0 dedx, 1 itr1, 2 brem, 3 moller, 4 k1, 5 imfpMax, 6 tot, 7 compton, 8 pair
 void oracle_eval_table(void* h, int q, int imat, const double* e, double* out, int n) {
   auto* T = static_cast<Tables*>(h);
