@@ -134,6 +134,7 @@ def library():
         "dpmx_rng_eval": (C.c_int, [_u32p, _u32p, C.c_int, _u32p,
                                     np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS"), _dp]),
         "dpmx_atomic_roof": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),
+        "dpmx_job_histories": (C.c_int, [P, C.POINTER(_Job), _dp, C.c_void_p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -159,7 +160,7 @@ def exported_symbols():
             "dpmx_simulate", "dpmx_simulate_noalloc", "dpmx_write_hist", "dpmx_sampler_eval", "dpmx_table_eval", "dpmx_simulate_histories",
             "dpmx_influence_build", "dpmx_csr_shape", "dpmx_csr_device", "dpmx_csr_spmv", "dpmx_csr_spmv_t",
             "dpmx_csr_download", "dpmx_csr_free", "dpmx_ring_selftest", "dpmx_rng_eval",
-            "dpmx_atomic_roof"]
+            "dpmx_atomic_roof", "dpmx_job_histories"]
 
 
 class Tables:
@@ -521,6 +522,20 @@ def simulate_histories(tables, nprimary, eprimary=15.0, iselectron=True, lbox=1.
     _check(library().dpmx_simulate_histories(tables.handle, int(nprimary), float(eprimary), 1 if iselectron else 0,
                                              float(lbox), int(geom_index), int(seed), he, e, cap))
     return he[:nprimary], e
+
+
+def job_histories(tables, job, with_dose=False):
+    """FP64 form of one job on any phantom: each history's deposited energy
+    (and the job's dose tally when with_dose)."""
+    h = job.phantom.handle
+    j = _Job(h.value if hasattr(h, "value") else h, job.source._c(), int(job.histories), int(job.seed),
+             int(job.first_history))
+    he = np.zeros(max(1, int(job.histories)))
+    dose = np.zeros(job.phantom.tally_size) if with_dose else None
+    _check(library().dpmx_job_histories(tables.handle, C.byref(j), he,
+                                        None if dose is None else dose.ctypes.data))
+    he = he[:int(job.histories)]
+    return (he, dose) if with_dose else he
 
 
 def write_hist(tables, fname, geom_index, lbox, nprimary, edep_hist, step_hist):

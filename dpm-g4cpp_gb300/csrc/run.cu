@@ -1007,4 +1007,30 @@ int dpmx_simulate_histories(const dpmx_tables* t, int nprimary, double eprimary,
   return rc;
 }
 
+// test hook: one job of any phantom in the FP64 form, with each history's
+// deposited energy
+int dpmx_job_histories(const dpmx_tables* t, const dpmx_job* job, double* hist_edep, double* dose) {
+  if (!t || !job || !hist_edep) return Fail(DPMX_ERR_ARG, "bad arguments");
+  if (int rc = CheckJobs(t, job, 1)) return rc;
+  if (job->histories > (1LL << 26)) return Fail(DPMX_ERR_ARG, "at most 2^26 histories per call");
+  std::vector<JobOut> outs;
+  int rc = PrepareOutputs(job, 1, false, 0, outs);
+  double* d_he = nullptr;
+  const long long n = job->histories;
+  if (!rc && cudaMalloc(&d_he, std::max(1LL, n) * sizeof(double)) != cudaSuccess) rc = Fail(DPMX_ERR_NOMEM, "alloc");
+  double ms = 0;
+  long long nl = 0;
+  if (!rc) rc = RunFp64(t, job, 1, 1, true, 0, outs, &ms, &nl, d_he);
+  if (!rc || rc == DPMX_ERR_OVERFLOW) {
+    if (cudaMemcpy(hist_edep, d_he, n * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess && !rc)
+      rc = Fail(DPMX_ERR_CUDA, "copy of the per-history energies failed");
+    if (dose && cudaMemcpy(dose, outs[0].d_dose, outs[0].tallySize * sizeof(double), cudaMemcpyDeviceToHost) !=
+                    cudaSuccess && !rc)
+      rc = Fail(DPMX_ERR_CUDA, "copy of the dose failed");
+  }
+  cudaFree(d_he);
+  for (auto& o : outs) ReleaseJobOut(o);
+  return rc;
+}
+
 }  // extern "C"

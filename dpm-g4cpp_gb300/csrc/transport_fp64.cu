@@ -77,6 +77,10 @@ struct SlabGeo {
 };
 
 // Voxel box: the world is the box, vacuum outside (same push semantics)
+// Geom::DistanceToBoundary (Geom.cc:20-117) on the phantom's lattice: the
+// index from the position relative to the centre of voxel 0 (lower corner +
+// half a voxel), the distance to the walls from the position relative to the
+// voxel's centre, as the reference computes both for its own lattice
 struct GridGeo {
   GridGeom g;
   double ivx, ivy, ivz;
@@ -91,18 +95,21 @@ struct GridGeo {
         if (r[a] < o[a] || r[a] > o[a] + n[a] * s[a]) return -1.0;
       double tr[3];
       for (int a = 0; a < 3; ++a) {
-        i[a] = int(floor((r[a] - o[a]) * is[a]));
-        tr[a] = r[a] - o[a] - i[a] * s[a];
+        const double h = 0.5 * s[a];
+        const double q = r[a] - (o[a] + 0.5 * s[a]);
+        i[a] = int(floor((q + h) * is[a]));
+        tr[a] = q - i[a] * s[a];
       }
       double snext = 1.0E+20;
       bool pushed = false;
       for (int a = 0; a < 3 && !pushed; ++a) {
+        const double h = 0.5 * s[a];
         if (v[a] > 0.0) {
-          const double pd = s[a] - tr[a];
+          const double pd = h - tr[a];
           if (pd < kHalfTol) { r[a] += kTol; pushed = true; }
           else { const double q = pd / v[a]; if (q < snext) snext = q; }
         } else if (v[a] < 0.0) {
-          const double pd = tr[a];
+          const double pd = h + tr[a];
           if (pd < kHalfTol) { r[a] -= kTol; pushed = true; }
           else { const double q = -pd / v[a]; if (q < snext) snext = q; }
         }

@@ -221,6 +221,12 @@ int dpmx_table_eval(const dpmx_tables* t, int precision, int quantity, int imat,
 int dpmx_simulate_histories(const dpmx_tables* t, int nprimary, double eprimary, int iselectron, double lbox,
                             int geom_index, uint64_t seed, double* hist_edep, double* edep_hist, int cap);
 
+/* FP64 form of one job on any phantom (voxels included) with each history's
+ * deposited energy in hist_edep (job->histories values, at most 2^26) and,
+ * if dose is not NULL, the job's tally (dpmx_phantom_tally_size values);
+ * history h uses the per-history random stream with index first_history + h,
+ * as the oracle's Philox mode does */
+int dpmx_job_histories(const dpmx_tables* t, const dpmx_job* job, double* hist_edep, double* dose);
 /* random numbers (replaces the reference's global mt19937, Random.hh:10-12,
  * Random.cc:3-4, by counter-based Philox-4x32-10, Salmon et al. SC'11): for
  * each i, the block philox(counters[4i..4i+3], keys[2i..2i+1]) into

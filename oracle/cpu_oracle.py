@@ -71,7 +71,9 @@ def lib():
                                             np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS"), C.c_int, C.c_int,
                                             C.c_double, C.c_double, C.c_int, C.c_double, C.c_double, C.c_double,
                                             C.c_double, C.c_int, C.c_int, C.c_longlong, C.c_longlong, C.c_uint64, _dp,
-                                            _dp, _dp, C.c_void_p]
+                                            _dp, _dp, C.c_void_p, C.c_void_p]
+        L.oracle_simulate_voxel_slabref.argtypes = [P, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int,
+                                                    C.c_uint32, _dp, _dp, C.c_int, _dp]
         u32 = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
         L.oracle_philox.argtypes = [u32, u32, u32, C.c_int]
         _lib = L
@@ -119,6 +121,17 @@ class Oracle:
         m = lib().oracle_simulate_slab(self._h, n, e, 1 if iselectron else 0, lbox, geom_index, seed, ed, st, cap, stats)
         return ed[:m], st[:m], stats
 
+    def simulate_voxel_slabref(self, n, e, iselectron=True, lbox=1.0, geom_index=3, seed=123, cap=4096):
+        """The reference Simulate workload (mt19937 stream) on a 3-D voxel
+        phantom laid out as the reference's lattice; returns the depth tally
+        (edep, steps) with the reference's histogram length, and stats."""
+        ed = np.zeros(cap)
+        st = np.zeros(cap)
+        stats = np.zeros(4)
+        m = lib().oracle_simulate_voxel_slabref(self._h, n, e, 1 if iselectron else 0, lbox, geom_index, seed, ed,
+                                                st, cap, stats)
+        return ed[:m], st[:m], stats
+
     def simulate_slab_philox(self, n, e, iselectron=True, lbox=1.0, geom_index=3, seed=12345, first=0, cap=4096):
         """Same workload with the per-history Philox streams of the FP64 GPU form;
         returns (edep, steps, per-history deposit, stats)."""
@@ -130,10 +143,12 @@ class Oracle:
                                               ed, st, cap, he, stats)
         return ed[:m], st[:m], he[:n], stats
 
-    def simulate_voxel(self, mat, voxel_size, source, nhist, seed, first=0, density=None):
+    def simulate_voxel(self, mat, voxel_size, source, nhist, seed, first=0, density=None, tagged=False):
         """Voxel phantom (nz, ny, nx) uint8 (optionally with float32 densities
         per voxel) with a source (dict like the product's Source); returns
-        (dose[nz,ny,nx], per-history energy, stats)."""
+        (dose[nz,ny,nx], per-history deposited energy, stats), and with
+        tagged=True (beamlet-grid sources) also the dose per beamlet
+        [nbeamlets, nz, ny, nx]."""
         m = np.ascontiguousarray(mat, dtype=np.uint8)
         rho = None if density is None else np.ascontiguousarray(density, dtype=np.float32).reshape(-1)
         nz, ny, nx = m.shape
@@ -142,10 +157,16 @@ class Oracle:
         he = np.zeros(max(1, nhist))
         stats = np.zeros(4)
         s = source
+        bt = None
+        if tagged:
+            nb = max(1, s["nbx"] * s["nby"]) if s["shape"] == 2 else 1
+            bt = np.zeros((nb, nz, ny, nx))
         lib().oracle_simulate_voxel(self._h, nx, ny, nz, float(v[0]), float(v[1]), float(v[2]), m.reshape(-1),
                                     s["particle"], s["spectrum"], s["e0"], s["e1"], s["shape"], s["cx"], s["cy"],
                                     s["fx"], s["fy"], s["nbx"], s["nby"], first, nhist, seed, dose, he, stats,
-                                    None if rho is None else rho.ctypes.data)
+                                    None if rho is None else rho.ctypes.data, None if bt is None else bt.ctypes.data)
+        if tagged:
+            return dose.reshape(nz, ny, nx), he[:nhist], stats, bt
         return dose.reshape(nz, ny, nx), he[:nhist], stats
 
 
@@ -191,3 +212,54 @@ class Reference:
     def simulate_cli(self, n, e, iselectron, lbox, geom_index, fname, seed=123):
         self.L.ref_seed(seed)
         self.L.ref_simulate_cli(self._h, n, e, 1 if iselectron else 0, lbox, geom_index, str(fname).encode())
+
+
+# ---------------------------------------------------------------------------
+# Parallel batches of the voxel transport (a spawned process pool, so that it
+# is safe to start after the GPU has been used)
+# ---------------------------------------------------------------------------
+_worker_oracles = {}
+
+
+def _voxel_batch(args):
+    data_dir, mat, voxel, source, n, seed, first, density, tagged = args
+    o = _worker_oracles.get(data_dir)
+    if o is None:
+        o = _worker_oracles[data_dir] = Oracle(data_dir)
+    r = o.simulate_voxel(mat, voxel, source, n, seed, first=first, density=density, tagged=tagged)
+    return (r[3] if tagged else r[0]), r[2]
+
+
+def voxel_batches(data_dir, mat, voxel, source, per, batches, seed, first=0, density=None, processes=None,
+                  tagged=False, keep=False):
+    """Runs `batches` oracle batches of `per` histories each (batch k: history
+    ids first + k*per ...) on the host cores. Returns the per-history mean
+    dose, its standard error from the batch spread (both shaped like mat, or
+    [nbeamlets, *mat.shape] per beamlet with tagged=True), and the summed
+    stats [deposited, escaped, sub-steps, max stack depth]; with keep=True
+    also every batch's per-history dose, stacked in batch order."""
+    import multiprocessing as mp
+    build()            # once, here: the workers then load the built library
+    processes = processes or min(batches, os.cpu_count() or 1)
+    tasks = [(str(data_dir), mat, voxel, source, per, seed, first + k * per, density, tagged)
+             for k in range(batches)]
+    s1 = s2 = None
+    stats = np.zeros(4)
+    kept = []
+    with mp.get_context("spawn").Pool(processes) as pool:
+        for dose, st in (pool.imap if keep else pool.imap_unordered)(_voxel_batch, tasks):
+            if keep:
+                kept.append(dose / per)
+            if s1 is None:
+                s1 = np.zeros(dose.shape)
+                s2 = np.zeros(dose.shape)
+            d = dose / per
+            s1 += d
+            s2 += d * d
+            stats[:3] += st[:3]
+            stats[3] = max(stats[3], st[3])
+    mean = s1 / batches
+    var = np.maximum(s2 / batches - mean * mean, 0.0) * batches / max(batches - 1, 1)
+    if keep:
+        return mean, np.sqrt(var / batches), stats, np.stack(kept)
+    return mean, np.sqrt(var / batches), stats

@@ -555,8 +555,13 @@ struct SlabGeom {
 };
 
 // A 3-D voxel phantom: nx*ny*nz voxels of size (vx,vy,vz) whose lower corner
-// is at (x0,y0,z0). Outside the box is vacuum. Same boundary push semantics as
-// Geom::DistanceToBoundary, with the world equal to the phantom box.
+// is at (x0,y0,z0). Outside the world box is vacuum. The boundary arithmetic
+// is Geom::DistanceToBoundary's (Geom.cc:20-117) on a lattice whose voxel of
+// index 0 is centred at c (index = floor((r - c + s/2) / s), position relative
+// to the voxel centre, distance s/2 -/+ that), so that the reference's own
+// lattice (c = 0, world |x|,|y| <= 100 mm, -lbox <= z <= 100 mm) reproduces
+// Geom bit for bit. By default c is the centre of the phantom's first voxel,
+// the array starts at index 0 and the world is the phantom box.
 struct VoxelGeom {
   int nx, ny, nz;
   double x0, y0, z0, vx, vy, vz;
@@ -567,29 +572,49 @@ struct VoxelGeom {
   double* tag;       // optional per-history accumulator (energy check)
   const float* rho = nullptr;   // per-voxel density or null
   double wscale = 1.0;          // Woodcock majorant scale for densities above nominal
+  double c[3] = {0, 0, 0};      // centre of the voxel of lattice index 0
+  int lo[3] = {0, 0, 0};        // lattice index of the array's first voxel
+  double wlo[3] = {0, 0, 0}, whi[3] = {0, 0, 0};   // world box
+  double* depth = nullptr;      // optional depth tally (energy, steps) in Geom::Score's order
+  double* dsteps = nullptr;
+  int dsize = 20;               // its length by Geom::Score's growth rule (+10 past a bin beyond it)
+  double* btally = nullptr;     // optional beamlet-tagged tally [beamlet][voxel]
+  int beamlet = 0;              // beamlet of the current history
   static constexpr double kTol = 1.0E-4;
+  void SetDefaultLattice() {
+    const double o[3] = {x0, y0, z0}, s[3] = {vx, vy, vz};
+    const int n[3] = {nx, ny, nz};
+    for (int a = 0; a < 3; ++a) {
+      c[a] = o[a] + 0.5 * s[a];
+      lo[a] = 0;
+      wlo[a] = o[a];
+      whi[a] = o[a] + n[a] * s[a];
+    }
+  }
   double DistanceToBoundary(double* r, const double* v, int* i) const {
     const double kHalfTol = 0.5 * kTol;
-    const double o[3] = {x0, y0, z0}, s[3] = {vx, vy, vz}, is[3] = {ivx, ivy, ivz};
-    const int n[3] = {nx, ny, nz};
-    for (;;) {
+    const double s[3] = {vx, vy, vz}, is[3] = {ivx, ivy, ivz};
+    for (;;) {   // Geom.cc recurses after a push; loop instead
       for (int a = 0; a < 3; ++a) {
-        if (r[a] < o[a] || r[a] > o[a] + n[a] * s[a]) return -1.0;
+        if (r[a] < wlo[a] || r[a] > whi[a]) return -1.0;
       }
       double tr[3];
       for (int a = 0; a < 3; ++a) {
-        i[a] = (int)std::floor((r[a] - o[a]) * is[a]);
-        tr[a] = r[a] - o[a] - i[a] * s[a];     // in [0, s)
+        const double h = 0.5 * s[a];
+        const double q = r[a] - c[a];
+        i[a] = (int)std::floor((q + h) * is[a]);
+        tr[a] = q - i[a] * s[a];     // in [-h, h)
       }
       double snext = 1.0E+20;
       bool pushed = false;
       for (int a = 0; a < 3 && !pushed; ++a) {
+        const double h = 0.5 * s[a];
         if (v[a] > 0.0) {
-          const double pd = s[a] - tr[a];
+          const double pd = h - tr[a];
           if (pd < kHalfTol) { r[a] += kTol; pushed = true; }
           else { const double q = pd / v[a]; if (q < snext) snext = q; }
         } else if (v[a] < 0.0) {
-          const double pd = tr[a];
+          const double pd = h + tr[a];
           if (pd < kHalfTol) { r[a] -= kTol; pushed = true; }
           else { const double q = -pd / v[a]; if (q < snext) snext = q; }
         }
@@ -597,23 +622,37 @@ struct VoxelGeom {
       if (!pushed) return snext;
     }
   }
-  bool Inside(const int* i) const { return i[0] >= 0 && i[0] < nx && i[1] >= 0 && i[1] < ny && i[2] >= 0 && i[2] < nz; }
+  size_t Flat(const int* i) const {
+    return (size_t(i[2] - lo[2]) * ny + size_t(i[1] - lo[1])) * nx + size_t(i[0] - lo[0]);
+  }
+  bool Inside(const int* i) const {
+    return i[0] >= lo[0] && i[0] < lo[0] + nx && i[1] >= lo[1] && i[1] < lo[1] + ny && i[2] >= lo[2] &&
+           i[2] < lo[2] + nz;
+  }
   // material 255 is vacuum: index -1 (SimDPMLike.cc:88-93)
   int MaterialIndex(const int* i) const {
     if (!Inside(i)) return -1;
-    const uint8_t m = mat[(size_t(i[2]) * ny + i[1]) * nx + i[0]];
+    const uint8_t m = mat[Flat(i)];
     return m == 255 ? -1 : int(m);
   }
   double Density(int imat) const { return imat > -1 ? T->density[imat] : 1.0E-40; }
   // Geom::GetVoxelMaterialDensity(iVoxel) (Geom.hh:89-92), with per-voxel
   // densities when given
   double DensityAt(const int* i, int imat) const {
-    if (rho && imat > -1) return double(rho[(size_t(i[2]) * ny + i[1]) * nx + i[0]]);
+    if (rho && imat > -1) return double(rho[Flat(i)]);
     return Density(imat);
   }
   double Wscale() const { return wscale; }
   void Score(double e, const int* i) {
-    if (Inside(i)) dose[(size_t(i[2]) * ny + i[1]) * nx + i[0]] += e;
+    if (!Inside(i)) return;
+    dose[Flat(i)] += e;
+    if (btally) btally[size_t(beamlet) * nx * ny * nz + Flat(i)] += e;
+    if (depth) {   // Geom::Score (Geom.cc:120-130): by depth bin, in deposit order
+      const int iz = i[2] - lo[2];
+      if (iz >= dsize) dsize = iz + 10;
+      depth[iz] += e;
+      dsteps[iz] += 1.0;
+    }
   }
 };
 
@@ -1068,16 +1107,74 @@ int oracle_simulate_slab_philox(void* h, long long first, int nprimary, double e
   return n;
 }
 
+// The reference CLI workload (pencil beam from (0,0,-lbox/2) along +z,
+// mt19937 stream, SimDPMLike.cc:57-247) on a 3-D voxel phantom laid out as the
+// reference's own lattice: voxels of lbox centred at integer multiples of lbox
+// (lattice index 0 at the origin), x and y indices -k..k and z indices 0..nz-1
+// covering the world |x|,|y| <= 100 mm, -lbox <= z <= 100 mm (Geom.cc:20-28,
+// Geom.hh:107-109), each voxel holding the slab material of its depth
+// (Geom.cc:133-164). The depth tally (Geom::Score order) is returned in
+// edep/steps (cap bins), its length by Geom::Score's rule as the return value.
+int oracle_simulate_voxel_slabref(void* h, int nprimary, double eprimary, int iselectron, double lbox,
+                                  int geomIndex, uint32_t seed, double* edep, double* steps, int cap, double* stats) {
+  auto* T = static_cast<Tables*>(h);
+  const double invL = 1.0 / lbox, halfL = 0.5 * lbox;
+  const int k = int(std::ceil((100.0 - halfL) * invL - 1.0e-9));       // lateral indices -k..k
+  const int nz = int(std::ceil((100.0 - halfL) * invL - 1.0e-9)) + 1;  // depth indices 0..nz-1
+  const int nx = 2 * k + 1;
+  SlabGeom slab(lbox, T, geomIndex);
+  std::vector<uint8_t> mat(size_t(nx) * nx * nz);
+  for (int iz = 0; iz < nz; ++iz) {
+    const int ib[3] = {0, 0, iz};
+    const int m = slab.MaterialIndex(ib);
+    std::fill(mat.begin() + size_t(iz) * nx * nx, mat.begin() + size_t(iz + 1) * nx * nx,
+              uint8_t(m < 0 ? 255 : m));
+  }
+  std::vector<double> dose(mat.size(), 0.0), depth(nz, 0.0), dsteps(nz, 0.0);
+  VoxelGeom g{nx, nx, nz, -(k + 0.5) * lbox, -(k + 0.5) * lbox, -halfL, lbox, lbox, lbox, invL, invL, invL,
+              mat.data(), T, dose.data(), nullptr};
+  for (int a = 0; a < 3; ++a) g.c[a] = 0.0;
+  g.lo[0] = g.lo[1] = -k;
+  g.lo[2] = 0;
+  g.wlo[0] = g.wlo[1] = -100.0;
+  g.whi[0] = g.whi[1] = 100.0;
+  g.wlo[2] = -lbox;
+  g.whi[2] = 100.0;
+  g.depth = depth.data();
+  g.dsteps = dsteps.data();
+  MtRng rng(seed);
+  Sim<VoxelGeom, MtRng> sim(*T, g, rng);
+  for (int ip = 0; ip < nprimary; ++ip) {
+    Track p{};
+    p.ekin = eprimary;
+    p.type = iselectron ? -1 : 0;
+    p.dir[2] = 1.0;
+    p.pos[2] = -halfL;
+    p.mat = -1;
+    sim.History(p);
+  }
+  const int n = g.dsize;
+  for (int i = 0; i < std::min(n, cap); ++i) {
+    edep[i] = i < nz ? depth[i] : 0.0;
+    steps[i] = i < nz ? dsteps[i] : 0.0;
+  }
+  if (stats) { stats[0] = sim.st.deposited; stats[1] = sim.st.escaped; stats[2] = double(sim.st.steps); stats[3] = sim.st.maxDepth; }
+  return n;
+}
+
 // Voxel-phantom run with a beam source, Philox stream per history. The dose
 // array (nx*ny*nz, zero-filled by the caller) receives the deposited energy
-// [MeV]. If per_batch_dose2 is given, histories are split into nbatch equal
-// batches and sum over batches of (batch deposit)^2 is accumulated per voxel.
+// [MeV] and hist_edep (optional) each history's deposited energy; btally
+// (optional, nbx*nby*nx*ny*nz) the dose per beamlet of a beamlet-grid source,
+// each history's deposits under its beamlet.
 int oracle_simulate_voxel(void* h, int nx, int ny, int nz, double vx, double vy, double vz, const uint8_t* mat,
                           int particle, int spectrum, double e0, double e1, int shape, double cx, double cy,
                           double fx, double fy, int nbx, int nby, long long first, long long nhist, uint64_t seed,
-                          double* dose, double* hist_edep, double* stats, const float* rho) {
+                          double* dose, double* hist_edep, double* stats, const float* rho, double* btally) {
   auto* T = static_cast<Tables*>(h);
   VoxelGeom g{nx, ny, nz, -0.5 * nx * vx, -0.5 * ny * vy, 0.0, vx, vy, vz, 1.0 / vx, 1.0 / vy, 1.0 / vz, mat, T, dose, nullptr};
+  g.SetDefaultLattice();
+  g.btally = btally;
   if (rho) {
     // the same majorant scale as the library: max density / nominal density
     g.rho = rho;
@@ -1092,10 +1189,10 @@ int oracle_simulate_voxel(void* h, int nx, int ny, int nz, double vx, double vy,
     const long long hid = first + i;
     rng.BeginHistory(uint64_t(hid));
     Track p{};
-    SamplePrimary(s, 0.0, rng, hid, p);
-    const double before = sim.st.deposited, esc = sim.st.escaped;
+    g.beamlet = SamplePrimary(s, 0.0, rng, hid, p);
+    const double before = sim.st.deposited;
     sim.History(p);
-    if (hist_edep) hist_edep[i] = (sim.st.deposited - before) + (sim.st.escaped - esc);
+    if (hist_edep) hist_edep[i] = sim.st.deposited - before;
   }
   if (stats) { stats[0] = sim.st.deposited; stats[1] = sim.st.escaped; stats[2] = double(sim.st.steps); stats[3] = sim.st.maxDepth; }
   return 0;

@@ -1,0 +1,97 @@
+"""The target's gate on the precision workload, against the CPU oracle.
+
+Geometry of the precision form (water body, G4_LUNG_ICRP slab z = 60-120 mm,
+G4_BONE_COMPACT_ICRU cylinder r = 15 mm along y at x = 0, z = 180 mm, 10x10 cm2
+photon beam with energy uniform in 1-20 MeV, seed 7) at 4 mm voxels, so that
+the oracle (the reference's FP64 transport, SimDPMLike.cc:40-791, tallied per
+voxel as Geom::Score does per depth bin, Geom.cc:120-130) finishes in seconds
+on the host cores.
+
+* FP32 transport with FP64 tallies against the oracle, voxel by voxel in the
+  voxels above 10 % of Dmax: >= 95 % within combined 2 sigma (t-corrected for
+  sigmas estimated from batches; 95.45 % expected), dose-weighted mean signed
+  difference <= 1 %, mean |difference| in excess of the statistical
+  expectation <= 1 %, summed dose within 1 %.
+* FP64 form against the oracle history by history (both draw the same
+  per-history Philox stream): the share of histories whose deposited energy
+  differs beyond rounding is counted and bounded.
+"""
+import importlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import DATA_WLB
+
+pytestmark = pytest.mark.gpu
+
+VOXEL = 4.0
+SHAPE = dict(nx=64, ny=64, nz=128, v=VOXEL)
+GPU_HIST, GPU_BATCHES = 40_000_000, 50
+ORACLE_PER, ORACLE_BATCHES = 250_000, 48
+
+
+def _source_dict(s):
+    return dict(particle=s.particle, spectrum=s.spectrum, e0=s.e0, e1=s.e1, shape=s.shape, cx=s.cx, cy=s.cy,
+                fx=s.fx, fy=s.fy, nbx=s.nbx, nby=s.nby)
+
+
+def _report(name, stats):
+    """keeps the measured figures beside the test output (printed; also written
+    to $DPM_TEST_REPORT_DIR when set)"""
+    print(name, json.dumps(stats))
+    d = os.environ.get("DPM_TEST_REPORT_DIR")
+    if d:
+        os.makedirs(d, exist_ok=True)
+        with open(os.path.join(d, name + ".json"), "w") as f:
+            json.dump(stats, f, indent=1)
+
+
+def test_fp32_dose_grid_vs_oracle(tables_wlb, dpm, orc):
+    wl = importlib.import_module("dpm-g4cpp_gb300.workloads")
+    dc = importlib.import_module("dpm-g4cpp_gb300.dosecheck")
+    m = wl.precision_phantom(**SHAPE)
+    src = wl.precision_source()
+    # oracle first: its spawned workers run on the host cores. Another seed
+    # than the GPU's (a primary's first Philox blocks would otherwise be the
+    # same on both sides), so that the two estimates are independent
+    o, so, ost = orc.voxel_batches(DATA_WLB, m, VOXEL, _source_dict(src), ORACLE_PER, ORACLE_BATCHES, 1007)
+    ph = dpm.Phantom.voxels(tables_wlb, m, VOXEL)
+    res = dpm.run(tables_wlb, [dpm.Job(ph, src, GPU_HIST, 7)], batches=GPU_BATCHES)
+    st = res.stats(0)
+    assert st.lost == 0 and st.residual_violations == 0, st
+    d, d2, _ = res.tally(0)
+    g, sg = dc.batch_estimate(d, d2, GPU_BATCHES, GPU_HIST)
+    r = dc.compare(g, sg, GPU_BATCHES, o.reshape(-1), so.reshape(-1), ORACLE_BATCHES)
+    r.update(gpu_histories=GPU_HIST, oracle_histories=ORACLE_PER * ORACLE_BATCHES, voxel_mm=VOXEL,
+             deposited_per_history_gpu=st.edep / GPU_HIST,
+             deposited_per_history_oracle=ost[0] / (ORACLE_PER * ORACLE_BATCHES))
+    _report("precision_gate_fp32_vs_oracle", r)
+    assert r["voxels"] > 50000
+    assert r["within_2sigma"] >= 0.95, r
+    assert abs(r["mean_signed_pct"]) <= 1.0, r
+    assert r["mean_abs_excess_pct"] <= 1.0, r
+    assert abs(r["total_ratio"] - 1.0) <= 0.01, r
+
+
+def test_fp64_voxel_histories_vs_oracle(tables_wlb, oracle_wlb, dpm):
+    """identical per-history streams: a history differs from the oracle's only
+    where a last-bit difference of a transcendental (CUDA's against glibc's)
+    flips a branch; such histories are counted and must stay rare"""
+    wl = importlib.import_module("dpm-g4cpp_gb300.workloads")
+    m = wl.precision_phantom(**SHAPE)
+    src = wl.precision_source()
+    n = 20000
+    ph = dpm.Phantom.voxels(tables_wlb, m, VOXEL)
+    he, dose = dpm.job_histories(tables_wlb, dpm.Job(ph, src, n, 77), with_dose=True)
+    o, ho, _ = oracle_wlb.simulate_voxel(m, VOXEL, _source_dict(src), n, 77)
+    same = np.isclose(he, ho, rtol=1e-9, atol=1e-12)
+    r = {"histories": n, "diverging": int((~same).sum()), "diverging_share": float(1 - same.mean()),
+         "matching_deposit_ratio": float(he[same].sum() / ho[same].sum()),
+         "dose_ratio": float(dose.sum() / o.sum())}
+    _report("precision_fp64_histories_vs_oracle", r)
+    assert r["diverging_share"] <= 0.02, r
+    assert abs(r["matching_deposit_ratio"] - 1.0) < 1e-9, r
+    assert abs(r["dose_ratio"] - 1.0) < 5e-3, r

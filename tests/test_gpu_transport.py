@@ -5,9 +5,15 @@
   their deposited energies agree to rounding unless a 1-ulp difference of a
   transcendental flips a branch.
 * FP32 event form, statistically: the depth dose per bin agrees with the FP64
-  oracle within combined 2 sigma for >= 95 % of the bins above 10 % of Dmax,
-  mean |diff| <= 1 % there, and every history conserves energy.
+  oracle within combined 2 sigma (t-corrected for sigmas from 10 batches, so
+  95.45 % of the bins above 10 % of Dmax are expected within it; with ~100
+  bins the observed share may fall 3 binomial standard deviations below that,
+  and no further), mean |diff| beyond statistics <= 1 % there, and every
+  history conserves energy.
 """
+import importlib
+import math
+
 import numpy as np
 import pytest
 
@@ -53,18 +59,17 @@ def total_dose_z(g, n_g, batches, per):
     return (g[:m][mask].sum() - tot_b.mean()) / s
 
 
-def compare_depth_dose(g, sg, o, so):
-    """For the bins above 10% of Dmax: fraction within combined 2 sigma, the
-    mean |relative difference| in excess of the statistical expectation
-    (E|N(0, s)| = 0.8 s per bin), and the mean signed relative difference."""
+def compare_depth_dose(g, sg, o, so, batches=10):
+    """For the bins above 10% of Dmax: the fraction within the t-corrected
+    combined 2 sigma, the lowest fraction that 3 binomial standard deviations
+    allow for that many bins, the mean |relative difference| in excess of the
+    statistical expectation, and the mean signed relative difference."""
+    dc = importlib.import_module("dpm-g4cpp_gb300.dosecheck")
     m = min(len(g), len(o))
-    g, sg, o, so = g[:m], sg[:m], o[:m], so[:m]
-    mask = o > 0.1 * o.max()
-    s = np.sqrt(sg[mask] ** 2 + so[mask] ** 2)
-    z = np.abs(g[mask] - o[mask]) / s
-    rel = (g[mask] - o[mask]) / o[mask]
-    noise = np.mean(0.8 * s / o[mask])
-    return np.mean(z < 2.0), max(0.0, np.mean(np.abs(rel)) - noise), np.mean(rel)
+    r = dc.compare(g[:m], sg[:m], batches, o[:m], so[:m], batches)
+    p, n = r["expected_within_2sigma"], r["voxels"]
+    floor = p - 3.0 * math.sqrt(p * (1.0 - p) / n)
+    return r["within_2sigma"], floor, r["mean_abs_excess_pct"] / 100.0, r["mean_signed_voxel_pct"] / 100.0
 
 
 @pytest.mark.parametrize("ise", [True, False])
@@ -77,8 +82,8 @@ def test_fp64_depth_dose_statistical(tables_c3, oracle_c3, dpm, ise):
     assert res.stats(0).lost == 0
     per = 10000 if ise else 20000
     o, so, ob = oracle_batches(oracle_c3, 10, per, 15.0, ise, 3, 100)
-    frac, excess, bias = compare_depth_dose(d / n, batch_sigma(d, d2, 10) / n, o, so)
-    assert frac >= 0.85, frac
+    frac, floor, excess, bias = compare_depth_dose(d / n, batch_sigma(d, d2, 10) / n, o, so)
+    assert frac >= floor, (frac, floor)
     assert excess < 0.01, excess    # mean |diff| beyond statistics: <= 1 %
     z = total_dose_z(d / n, n, ob, per)
     assert abs(z) < 3.5, (z, bias)  # no systematic offset of the integral dose
@@ -95,8 +100,8 @@ def test_fp32_depth_dose_vs_oracle(tables_c3, oracle_c3, dpm, ise):
     assert st.lost == 0 and st.residual_violations == 0, st
     per = 10000 if ise else 20000
     o, so, ob = oracle_batches(oracle_c3, 10, per, 15.0, ise, 3, 200)
-    frac, excess, bias = compare_depth_dose(d / n, batch_sigma(d, d2, 10) / n, o, so)
-    assert frac >= 0.85, frac
+    frac, floor, excess, bias = compare_depth_dose(d / n, batch_sigma(d, d2, 10) / n, o, so)
+    assert frac >= floor, (frac, floor)
     assert excess < 0.01, excess    # mean |diff| beyond statistics: <= 1 %
     z = total_dose_z(d / n, n, ob, per)
     assert abs(z) < 3.5, (z, bias)  # no systematic offset of the integral dose

@@ -36,6 +36,20 @@ def test_slab_transport_bit_exact(golden, oracle_c3, run):
     np.testing.assert_array_equal(st, golden["slab_%s_steps" % name])
 
 
+@pytest.mark.parametrize("run", SLAB_RUNS, ids=[r[0] for r in SLAB_RUNS])
+def test_voxel_geometry_reproduces_reference_geom(golden, oracle_c3, run):
+    """The oracle's 3-D voxel geometry, laid out as the reference's own lattice
+    (voxels of lbox centred on integer multiples of lbox, world |x|,|y| <= 100
+    mm and -lbox <= z <= 100 mm, Geom.cc:20-28, each voxel holding the slab
+    material of its depth, Geom.cc:133-164), reproduces the unmodified
+    reference's depth histograms bit for bit: the voxel boundary arithmetic,
+    3-D material lookup and 3-D scoring are Geom's."""
+    name, ise, e, lbox, geom, n, seed = run
+    ed, st, stats = oracle_c3.simulate_voxel_slabref(n, e, ise, lbox, geom, seed)
+    np.testing.assert_array_equal(ed, golden["slab_%s_edep" % name])
+    np.testing.assert_array_equal(st, golden["slab_%s_steps" % name])
+
+
 def test_restated_loop_matches_unmodified_simulate(golden):
     """The full-precision history loop used for the goldens reproduces the
     unmodified Simulate's hist.sim (5 significant digits)."""
