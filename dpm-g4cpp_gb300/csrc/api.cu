@@ -172,6 +172,7 @@ int BuildImage(const HostTables& h, DevTables<R>& T, void** dptr) {
     std::vector<R> uab(size_t(ne) * ns * 4, R(0));
     for (size_t i = 0; i < size_t(ne) * ns; ++i) {
       uab[4 * i] = R(h.gsU[i]); uab[4 * i + 1] = R(h.gsPA[i]); uab[4 * i + 2] = R(h.gsPB[i]);
+      uab[4 * i + 3] = R(1.0 - h.gsU[i]);   // 1 - u for the FP32 sampler's well-conditioned form
     }
     std::vector<R> e(h.gsE.begin(), h.gsE.end()), a(h.gsA.begin(), h.gsA.end());
     fx.Add(reinterpret_cast<const void**>(&T.gs.uab), img.Put(uab.data(), uab.size() * sizeof(R)));

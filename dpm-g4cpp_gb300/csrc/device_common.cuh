@@ -201,6 +201,52 @@ __device__ __forceinline__ R SampleGS(const GSSetT<R>& g, R ep, R r1, R r2) {
   return R(1) - R(2) * a * u / (R(1) - u + a);
 }
 
+// FP32 form of the GS deflection: the same bin choices and ratin
+// interpolation, carried out both for u and for w = 1 - u (the table keeps
+// 1 - u, rounded from FP64, in each record's fourth slot). The transform
+// mu = 1 - 2 a u / (1 - u + a) magnifies an error of u near u = 1 by ~2/a
+// (a is ~1e-3 at high energies), so mu is formed from
+//   1 - mu = 2 a u / (w + a),   1 + mu = 2 w (1 + a) / (w + a),
+// each a product and quotient of well-known values, and sin(theta) is
+// sqrt((1 - mu)(1 + mu)) from those two rather than from a rounded mu.
+__device__ __forceinline__ void SampleGSAngle(const GSSetT<float>& g, float ep, float r1, float r2, float& cost,
+                                              float& sint) {
+  const float le = mlog(ep);
+  float ph = (le - g.logMinE) * g.invLogDeltaE;
+  int ielow = int(ph);
+  ielow = ielow < 0 ? 0 : (ielow > g.numE - 2 ? g.numE - 2 : ielow);
+  int ie = ielow;
+  ph -= float(ielow);
+  if (r1 < ph) ++ie;
+  const float dc = g.deltaCum;
+  int il = int(r2 / dc);
+  il = il > g.numS - 2 ? g.numS - 2 : il;
+  const float resid = r2 - float(il) * dc;
+  const float4 q0 = reinterpret_cast<const float4*>(g.uab)[size_t(ie) * g.numS + il];
+  const float4 q1 = reinterpret_cast<const float4*>(g.uab)[size_t(ie) * g.numS + il + 1];
+  const float pa = q0.y, pb = q0.z;
+  const float dum1 = (1.0f + pa + pb) * dc * resid;
+  const float dum2 = dc * dc + pa * dc * resid + pb * resid * resid;
+  const float f = dum1 / dum2;
+  const float u = q0.x + f * (q1.x - q0.x);
+  const float w = q0.w + f * (q1.w - q0.w);
+  const float a0 = g.a[ielow], a1 = g.a[ielow + 1];
+  const float e0 = g.e[ielow], e1 = g.e[ielow + 1];
+  const float a = (a1 - a0) / (e1 - e0) * (ep - e0) + a0;
+  const float inv = 1.0f / (w + a);
+  const float om = fmaxf(0.0f, 2.0f * a * u * inv);             // 1 - mu
+  const float op = fmaxf(0.0f, 2.0f * w * (1.0f + a) * inv);    // 1 + mu
+  cost = u < 0.5f ? 1.0f - om : op - 1.0f;
+  cost = fmaxf(-1.0f, fminf(1.0f, cost));
+  sint = fminf(1.0f, sqrtf(om * op));
+}
+template <>
+__device__ __forceinline__ float SampleGS<float>(const GSSetT<float>& g, float ep, float r1, float r2) {
+  float c, s;
+  SampleGSAngle(g, ep, r1, r2, c, s);
+  return c;
+}
+
 // SimDPMLike.cc:638-652: rotate (u,v,w) from the frame of (u1,u2,u3) to the lab
 template <class R>
 __device__ __forceinline__ void RotateToLab(R& u, R& v, R& w, R u1, R u2, R u3) {

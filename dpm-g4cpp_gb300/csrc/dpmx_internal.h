@@ -45,7 +45,7 @@ struct AliasSetT {     // numE tables of numS points on a log energy grid
   R minE, logMinE, invLogDeltaE;
 };
 template <class R>
-struct GSSetT {        // GS ratin tables: numE x numS x {u,a,b,pad}
+struct GSSetT {        // GS ratin tables: numE x numS x {u, a, b, 1 - u}
   const R* uab;
   const R* e;          // energy grid
   const R* a;          // transformation parameter per energy

@@ -924,9 +924,8 @@ __global__ void __launch_bounds__(256) ElectronPhase(PhaseArgs a) {
             if (s.hinge) {
               // GS angular deflection at the hinge (SimDPMLike.cc:731-750)
               const float r2 = rng.U(), r1 = rng.U();
-              const float d = SampleGS(T.gs, s.ekin0, r1, r2);
-              const float cost = fmaxf(-1.0f, fminf(1.0f, d));
-              const float sint = sqrtf(fmaxf(0.f, (1.0f - cost) * (1.0f + cost)));
+              float cost, sint;
+              SampleGSAngle(T.gs, s.ekin0, r1, r2, cost, sint);
               const float phi = 2.0f * kPIf * rng.U();
               float sn, cs;
               __sincosf(phi, &sn, &cs);
@@ -1394,9 +1393,8 @@ __device__ __forceinline__ void EventHinge(const PhaseArgs& a, const JobF* jobs,
   PRng rng;
   SlotRng(S, k, jobs[JobOfSub(fl >> 8)], p.hist, rng);
   const float r2 = rng.U(), r1 = rng.U();
-  const float d = SampleGS(a.T.gs, s.ekin0, r1, r2);
-  const float cost = fmaxf(-1.0f, fminf(1.0f, d));
-  const float sint = sqrtf(fmaxf(0.f, (1.0f - cost) * (1.0f + cost)));
+  float cost, sint;
+  SampleGSAngle(a.T.gs, s.ekin0, r1, r2, cost, sint);
   const float phi = 2.0f * kPIf * rng.U();
   float sn, cs;
   __sincosf(phi, &sn, &cs);

@@ -66,3 +66,54 @@ def test_backward_matches_finite_differences(setup):
             e[i] = eps
             fd[i] = (loss(w + e).item() - loss(w - e).item()) / (2 * eps)
     np.testing.assert_allclose(grad, fd, rtol=1e-5, atol=1e-8 * np.abs(fd).max())
+
+
+def test_influence_matrix_vs_cpu_built(tables_wlb, dpm, orc):
+    """A built on the CPU by the oracle (the reference's FP64 transport with
+    each history's deposits tallied under its beamlet) against A built on the
+    GPU (FP32 transport, FP64 accumulation, FP32 CSR values), both as dose per
+    history from independent random streams: column by column, voxel by voxel
+    within the t-corrected combined 2 sigma in each column's voxels above 10 %
+    of its maximum, and the products A^T g for a target-shaped g within 4
+    combined standard deviations per beamlet and 1 % on average."""
+    from conftest import DATA_WLB
+    wl = importlib.import_module("dpm-g4cpp_gb300.workloads")
+    dc = importlib.import_module("dpm-g4cpp_gb300.dosecheck")
+    m, src, target = wl.differentiation_setup(n=32, v=4.0)
+    src.nbx = src.nby = 4
+    src.fx = src.fy = 10.0
+    nb = 16
+    s = dict(particle=src.particle, spectrum=src.spectrum, e0=src.e0, e1=src.e1, shape=src.shape, cx=src.cx,
+             cy=src.cy, fx=src.fx, fy=src.fy, nbx=src.nbx, nby=src.nby)
+    KO, PER_O = 32, 200_000
+    o, so, _, ob = orc.voxel_batches(DATA_WLB, m, 4.0, s, PER_O, KO, 1007, tagged=True, keep=True)
+    o, so, ob = o.reshape(nb, -1), so.reshape(nb, -1), ob.reshape(KO, nb, -1)
+    ph = dpm.Phantom.voxels(tables_wlb, m, 4.0)
+    KG, PER_G = 16, 400_000
+    gb = []
+    for k in range(KG):
+        res = dpm.run(tables_wlb, [dpm.Job(ph, src, PER_G, 3, first_history=k * PER_G)], batches=1,
+                      tag_beamlets=True)
+        A = res.influence(0).to_scipy().toarray().astype(np.float64)      # [voxels, beamlets]
+        gb.append(A.T / PER_G)
+        res.close()
+    gb = np.stack(gb)                                                      # [KG, beamlets, voxels]
+    g, sg = gb.mean(0), gb.std(0, ddof=1) / np.sqrt(KG)
+    within, voxels = 0.0, 0
+    for b in range(nb):
+        r = dc.compare(g[b], sg[b], KG, o[b], so[b], KO)
+        within += r["within_2sigma"] * r["voxels"]
+        voxels += r["voxels"]
+        assert abs(r["mean_signed_pct"]) < 2.0, (b, r)
+    p = dc.P_2SIGMA
+    floor = p - 3.0 * np.sqrt(p * (1 - p) / voxels)
+    assert within / voxels >= floor, (within / voxels, floor, voxels)
+    # A^T g per batch on both sides
+    w = target.reshape(-1) + 0.1
+    xo, xg = ob @ w, gb @ w                                                # [K, beamlets]
+    mo, mg = xo.mean(0), xg.mean(0)
+    se = np.sqrt(xo.var(0, ddof=1) / KO + xg.var(0, ddof=1) / KG)
+    z = (mg - mo) / se
+    print("A^T g z-scores", np.round(z, 2), "coverage", within / voxels)
+    assert np.all(np.abs(z) < 4.0), z
+    assert abs(np.mean((mg - mo) / mo)) < 0.01
