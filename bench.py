@@ -11,6 +11,13 @@ steps = the workload's 1e8 histories) with 10 statistical batches.
 --impl reference times the CPU oracle (the restatement of the reference's
 double-precision transport) on the host cores on a bounded sample of the same
 workload. Under torchrun each rank runs its own history range (weak scaling).
+
+Besides the timed steps the line carries, measured outside the timed region:
+the plain FP64 GPU form on the same workload (`fp64_gpu`, and `vs_fp64_gpu` =
+value / its histories/s), a voxel-by-voxel dose check of the FP32 form
+against it (`dose_check`), Gy-voxels/s, and the roofline of the dominant
+kernel against four roofs (instruction issue, L2 FP64 atomics, FP32 pipe,
+DRAM), `bound` naming the one it is closest to.
 """
 import argparse
 import importlib
@@ -27,19 +34,11 @@ DATA = os.path.join(ROOT, "data", "water_lung_bone")
 METRIC = "histories/s"
 WORKLOAD = "precision form: 128x128x256 x 2 mm water/lung-slab/bone-cylinder phantom, 10x10 cm2 photon beam U[1,20] MeV"
 
-# algorithmic bytes per unit (FP32 form): an electron sub-step reads 4 spline
-# segments of 5 floats (80 B), one material byte, and updates one FP64 tally
-# bin (16 B read+write); a photon step reads 3 linear-table points (24 B) and
-# one material byte; a queued particle is written once and read once (2 x 52 B)
-BYTES_E_STEP = 80 + 1 + 16
-BYTES_P_STEP = 24 + 1
-BYTES_PARTICLE = 2 * 52
-# FP32 work per unit: an electron sub-step is ~100 flops, a Woodcock photon
-# step ~35 (the transport is bounded by FP32/SFU issue and latency, not HBM)
-FLOPS_E_STEP = 100
-FLOPS_P_STEP = 35
 # nominal FP32 rate: 152 SMs x 128 lanes x 2 (FMA) x 2.07 GHz
 FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
+# instruction issue: 4 schedulers per SM, one warp instruction per cycle each
+ISSUE_PER_SM_CYCLE = 4
+SMS = 152
 
 
 def parse():
@@ -51,6 +50,8 @@ def parse():
     ap.add_argument("--hist", type=float, default=1e7, help="histories per step and GPU")
     ap.add_argument("--cpu-hist", type=int, default=200000, help="oracle histories per CPU worker and step")
     ap.add_argument("--batches", type=int, default=10, help="statistical batches per step")
+    ap.add_argument("--fp64-hist", type=float, default=2e6, help="histories of the FP64 GPU arm")
+    ap.add_argument("--check-hist", type=float, default=2e7, help="FP32 histories of the dose check")
     return ap.parse_args()
 
 
@@ -148,6 +149,63 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def roofline_of(dpm, pr, eblock, pblock, clk):
+    """The dominant phase kernel against four roofs, from a profiled run's
+    per-phase times and unit counts and the per-unit counters that ncu
+    measured for that kernel (profiles/counters.json):
+      issue      warp instructions / s against 4 per SM and cycle at the SM
+                 clock measured during the timed region
+      l2_atomic  tally atomics / s (one FP64 atomicAdd per electron sub-step
+                 at most) against dpmx_atomic_roof on this GPU
+      fp32       FP32 flops / s against the nominal FP32 rate
+      dram       DRAM bytes / s (ncu traffic per unit) against MEASURED_PEAKS
+    `bound` is the roof with the largest fraction."""
+    with open(os.path.join(ROOT, "profiles", "counters.json")) as f:
+        counters = json.load(f)
+    if pr["electron_ms"] >= pr["photon_ms"]:
+        kname = "ElectronPhaseB" if eblock else "ElectronPhase"
+        kms, nl, units = pr["electron_ms"], pr["electron_launches"], pr["electron_steps"]
+        atomics = pr["electron_steps"]
+    else:
+        kname = "PhotonPhaseB" if pblock else "PhotonPhase"
+        kms, nl, units = pr["photon_ms"], pr["photon_launches"], pr["photon_steps"]
+        atomics = None
+    c = counters.get(kname, {})
+    secs = kms * 1e-3
+    sm_mhz = clk.get("sm_mhz") or 2070.0
+    roofs = {}
+    if c.get("warp_inst_per_unit"):
+        ach = c["warp_inst_per_unit"] * units / secs / 1e9
+        peak = SMS * ISSUE_PER_SM_CYCLE * sm_mhz * 1e6 / 1e9
+        roofs["issue"] = {"achieved": ach, "peak": peak, "unit": "Gwarp-inst/s", "frac": ach / peak,
+                          "peak_source": "4 warp instructions per SM per cycle at the measured SM clock"}
+    if atomics:
+        peak = dpm.atomic_roof() / 1e9
+        ach = atomics / secs / 1e9
+        roofs["l2_atomic"] = {"achieved": ach, "peak": peak, "unit": "G FP64 atomics/s", "frac": ach / peak,
+                              "peak_source": "measured (dpmx_atomic_roof, 32 MB array)"}
+    if c.get("fp32_flops_per_unit"):
+        ach = c["fp32_flops_per_unit"] * units / secs / 1e12
+        roofs["fp32"] = {"achieved": ach, "peak": FP32_NOMINAL_TFLOPS, "unit": "TFLOP/s",
+                         "frac": ach / FP32_NOMINAL_TFLOPS, "peak_source": "nominal"}
+    traffic = None
+    if c.get("dram_bytes_per_unit"):
+        peak, kind = measured_peaks()
+        traffic = c["dram_bytes_per_unit"] * units / max(1.0, nl)
+        ach = c["dram_bytes_per_unit"] * units / secs / 1e9
+        roofs["dram"] = {"achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak, "peak_source": kind}
+    bound = max(roofs, key=lambda k: roofs[k]["frac"]) if roofs else None
+    top = roofs.get(bound, {})
+    return {"bound": bound, "kernel": kname, "achieved": top.get("achieved"), "peak": top.get("peak"),
+            "unit": top.get("unit"), "frac": top.get("frac"), "traffic": traffic, "roofs": roofs,
+            "avg_launch_ms": kms / max(1.0, nl), "units_per_launch": units / max(1.0, nl),
+            "unit_name": c.get("unit"),
+            "electron_phase_share": pr["electron_ms"] / max(1e-9, pr["total_ms"]),
+            "photon_phase_share": pr["photon_ms"] / max(1e-9, pr["total_ms"]),
+            "electron_steps_per_s": pr["electron_steps"] / max(1e-9, pr["electron_ms"] * 1e-3),
+            "photon_steps_per_s": pr["photon_steps"] / max(1e-9, pr["photon_ms"] * 1e-3)}
+
+
 # ---------------------------------------------------------------------------
 def main():
     a = parse()
@@ -222,7 +280,8 @@ def main():
     stats = []
     torch.cuda.synchronize()
     for k in range(a.steps):
-        flush.fill_(float(k))          # L2 flush between timed steps (outside the events)
+        with torch.cuda.stream(stream):
+            flush.fill_(float(k))      # L2 flush between timed steps, on the timed stream, before its events
         ev[k][0].record(stream)
         r = one(k)
         ev[k][1].record(stream)
@@ -266,39 +325,29 @@ def main():
     eblock = r.config["electron_kernel"] == 1
     pblock = r.config["photon_kernel"] == 1
     r.close()
-    peak, peak_kind = measured_peaks()
-    e_bytes = pr["electron_steps"] * BYTES_E_STEP + pr["electrons"] * BYTES_PARTICLE
-    p_bytes = pr["photon_steps"] * BYTES_P_STEP + pr["photons"] * BYTES_PARTICLE
-    if pr["electron_ms"] >= pr["photon_ms"]:
-        kname = "ElectronPhaseB" if eblock else "ElectronPhase"
-        kms, kbytes, nl = pr["electron_ms"], e_bytes, pr["electron_launches"]
-        kflops = pr["electron_steps"] * FLOPS_E_STEP
-        kunits = pr["electron_steps"]
-    else:
-        kname = "PhotonPhaseB" if pblock else "PhotonPhase"
-        kms, kbytes, nl = pr["photon_ms"], p_bytes, pr["photon_launches"]
-        kflops = pr["photon_steps"] * FLOPS_P_STEP
-        kunits = pr["photon_steps"]
-    achieved = kbytes / (kms * 1e-3) / 1e9
-    # DRAM bytes per launch from an ncu capture, given per unit (sub-step) so
-    # that it scales to this launch size
-    traffic = None
-    tf = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tf):
-        with open(tf) as f:
-            per_unit = json.load(f).get(kname, {}).get("dram_bytes_per_unit")
-        if per_unit:
-            traffic = per_unit * kunits / max(1.0, nl)
-    fp32 = kflops / (kms * 1e-3) / 1e12
-    roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
-                "fp32_issue": {"achieved": fp32, "peak": FP32_NOMINAL_TFLOPS, "unit": "TFLOP/s",
-                               "frac": fp32 / FP32_NOMINAL_TFLOPS, "peak_source": "nominal"},
-                "algorithmic_bytes_per_launch": kbytes / max(1.0, nl), "avg_launch_ms": kms / max(1.0, nl),
-                "electron_phase_share": pr["electron_ms"] / max(1e-9, pr["total_ms"]),
-                "photon_phase_share": pr["photon_ms"] / max(1e-9, pr["total_ms"]),
-                "electron_steps_per_s": pr["electron_steps"] / max(1e-9, pr["electron_ms"] * 1e-3),
-                "photon_steps_per_s": pr["photon_steps"] / max(1e-9, pr["photon_ms"] * 1e-3)}
+    roofline = roofline_of(dpm, pr, eblock, pblock, clk)
+
+    # the plain FP64 GPU form on the same workload and a voxel-by-voxel dose
+    # check of the FP32 form against it (both outside the timed region)
+    dc = importlib.import_module("dpm-g4cpp_gb300.dosecheck")
+    H64, B = int(a.fp64_hist), 40
+    r64 = dpm.run(tables, [dpm.Job(ph, src, H64, seed_of(200))], precision=dpm.FP64_PLAIN, batches=B,
+                  stream=stream.cuda_stream)
+    fp64_rate = world * H64 / (r64.elapsed_ms * 1e-3)
+    d64, d64b, _ = r64.tally(0)
+    r64.close()
+    Hc = int(a.check_hist)
+    rc_ = dpm.run(tables, [dpm.Job(ph, src, Hc, seed_of(300))], batches=B, stream=stream.cuda_stream)
+    d32, d32b, _ = rc_.tally(0)
+    rc_.close()
+    m32, s32 = dc.batch_estimate(d32, d32b, B, Hc)
+    m64, s64 = dc.batch_estimate(d64, d64b, B, H64)
+    check = dc.compare(m32, s32, B, m64, s64, B)
+    check.update(fp32_histories=Hc, fp64_histories=H64, batches=B, against="fp64_gpu")
+    # Gy-voxels/s: the dose summed over voxels per history [Gy], times histories/s
+    rho = np.array([tables.density(int(i)) for i in range(tables.num_materials)], dtype=np.float64)
+    mass_kg = rho[mat.reshape(-1)] * (2.0 ** 3) * 1e-3 * 1e-3     # g/cm3 x mm3 -> kg
+    gy_per_hist = float((m32.reshape(-1) * 1.602176634e-13 / mass_kg).sum())
 
     cpu = None
     if rank == 0:
@@ -315,6 +364,11 @@ def main():
             "config": {"workload": WORKLOAD, "histories_per_step": H, "batches": a.batches, "phantom": [256, 128, 128],
                        "voxel_mm": 2.0, "seed": 7, "l2": "flushed between steps (256 MB write)"},
             "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+            "fp64_gpu": {"value": fp64_rate, "unit": "histories/s", "histories": H64,
+                         "form": "plain FP64, one thread per history (dpmx FP64_PLAIN)"},
+            "vs_fp64_gpu": value / fp64_rate, "dose_check": check,
+            "gy_voxels_per_s": {"value": gy_per_hist * value, "unit": "Gy-voxels/s",
+                                "definition": "sum over voxels of the dose per history [Gy] x histories/s"},
             "energy_check": {"max_residual_mev": st.max_residual, "violations": st.residual_violations,
                              "lost": st.lost},
         }))
