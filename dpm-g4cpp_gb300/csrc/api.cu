@@ -184,6 +184,7 @@ int BuildImage(const HostTables& h, DevTables<R>& T, void** dptr) {
     T.gs.logMinE = R(lmin);
     T.gs.invLogDeltaE = R(1.0 / (std::log(h.gsE[1]) - lmin));
     T.gs.deltaCum = R(1.0 / (ns - 1));
+    T.gs.deltaCumLo = R(1.0 / (ns - 1) - double(T.gs.deltaCum));
   }
   fx.Add(reinterpret_cast<const void**>(&T.elecBase), f0);
   T.elecCount = int((elecEnd - f0) / sizeof(R));

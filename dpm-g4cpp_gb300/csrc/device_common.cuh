@@ -205,10 +205,16 @@ __device__ __forceinline__ R SampleGS(const GSSetT<R>& g, R ep, R r1, R r2) {
 // interpolation, carried out both for u and for w = 1 - u (the table keeps
 // 1 - u, rounded from FP64, in each record's fourth slot). The transform
 // mu = 1 - 2 a u / (1 - u + a) magnifies an error of u near u = 1 by ~2/a
-// (a is ~1e-3 at high energies), so mu is formed from
-//   1 - mu = 2 a u / (w + a),   1 + mu = 2 w (1 + a) / (w + a),
-// each a product and quotient of well-known values, and sin(theta) is
-// sqrt((1 - mu)(1 + mu)) from those two rather than from a rounded mu.
+// (a is ~1e-3 at high energies), so:
+//  * the position in the ratin bin and its distance to the bin's upper edge,
+//    r2 - il/(n-1) and (il+1)/(n-1) - r2, come from FMAs with the bin width
+//    split into a float and its rest (an FP32 product il * dc alone is off by
+//    ~3e-8, all of the distance near the bin's edge);
+//  * the interpolation weight f and 1 - f = (s (dc - b r)) / dum2 are both
+//    formed without cancellation, and u = u0 + f (u1 - u0),
+//    w = w1 + (1 - f) (w0 - w1) add terms of one sign;
+//  * mu comes from 1 - mu = 2 a u / (w + a) and 1 + mu = 2 w (1 + a) / (w + a),
+//    and sin(theta) = sqrt((1 - mu)(1 + mu)) from those two.
 __device__ __forceinline__ void SampleGSAngle(const GSSetT<float>& g, float ep, float r1, float r2, float& cost,
                                               float& sint) {
   const float le = mlog(ep);
@@ -218,18 +224,22 @@ __device__ __forceinline__ void SampleGSAngle(const GSSetT<float>& g, float ep, 
   int ie = ielow;
   ph -= float(ielow);
   if (r1 < ph) ++ie;
-  const float dc = g.deltaCum;
+  const float dc = g.deltaCum, dcl = g.deltaCumLo;
   int il = int(r2 / dc);
   il = il > g.numS - 2 ? g.numS - 2 : il;
-  const float resid = r2 - float(il) * dc;
+  const float fil = float(il), fil1 = float(il + 1);
+  const float resid = fmaf(-fil, dc, r2) - fil * dcl;           // r2 - il / (n-1)
+  const float rest = fmaxf(0.0f, fmaf(fil1, dc, -r2) + fil1 * dcl);   // (il+1) / (n-1) - r2
   const float4 q0 = reinterpret_cast<const float4*>(g.uab)[size_t(ie) * g.numS + il];
   const float4 q1 = reinterpret_cast<const float4*>(g.uab)[size_t(ie) * g.numS + il + 1];
   const float pa = q0.y, pb = q0.z;
   const float dum1 = (1.0f + pa + pb) * dc * resid;
   const float dum2 = dc * dc + pa * dc * resid + pb * resid * resid;
-  const float f = dum1 / dum2;
+  const float idum2 = 1.0f / dum2;
+  const float f = dum1 * idum2;
+  const float fc = fmaxf(0.0f, rest * (dc - pb * resid) * idum2);   // 1 - f
   const float u = q0.x + f * (q1.x - q0.x);
-  const float w = q0.w + f * (q1.w - q0.w);
+  const float w = q1.w + fc * (q0.w - q1.w);
   const float a0 = g.a[ielow], a1 = g.a[ielow + 1];
   const float e0 = g.e[ielow], e1 = g.e[ielow + 1];
   const float a = (a1 - a0) / (e1 - e0) * (ep - e0) + a0;

@@ -51,6 +51,7 @@ struct GSSetT {        // GS ratin tables: numE x numS x {u, a, b, 1 - u}
   const R* a;          // transformation parameter per energy
   int numE, numS;
   R logMinE, invLogDeltaE, deltaCum;
+  R deltaCumLo;        // 1/(numS-1) - deltaCum (FP32: the rest of the bin width)
 };
 
 template <class R>

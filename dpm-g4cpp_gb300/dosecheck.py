@@ -41,33 +41,42 @@ def _t_quantile(p, dof):
 
 def compare(a, sa, ba, b, sb, bb, threshold=0.1):
     """Statistics of estimate a (mean, standard error, batch count) against b
-    in the voxels where b exceeds `threshold` of its maximum.
+    in the voxels whose dose exceeds `threshold` of the maximum dose.
+
+    The voxels are chosen on the inverse-variance-weighted mean m of a and b,
+    which (for normal noise) is independent of a - b: choosing them on b
+    alone would keep the voxels where b's noise went up and bias a - b low by
+    an amount that grows with b's noise. Relative differences are taken
+    against m for the same reason.
 
     Returns a dict: voxels compared, the fraction within the t-corrected
     combined 2 sigma, the mean signed difference (dose-weighted: the summed
-    difference over the summed dose of b, which noise in b does not bias; the
-    plain mean of the per-voxel relative differences is given beside it), the
-    mean |relative difference| and its excess over the statistical
-    expectation (E|N(0,s)| = sqrt(2/pi) s per voxel), the largest |relative
-    difference|, the ratio of the summed doses and its z-score."""
+    difference over the summed dose; the plain mean of the per-voxel relative
+    differences is given beside it), the mean |relative difference| and its
+    excess over the statistical expectation (E|N(0,s)| = sqrt(2/pi) s per
+    voxel), the largest |relative difference|, the ratio of the summed doses
+    and its z-score."""
     a, sa, b, sb = (np.asarray(x, dtype=np.float64).reshape(-1) for x in (a, sa, b, sb))
-    mask = b > threshold * b.max()
-    a, sa, b, sb = a[mask], sa[mask], b[mask], sb[mask]
+    wa = 1.0 / np.maximum(sa * sa, 1e-300)
+    wb = 1.0 / np.maximum(sb * sb, 1e-300)
+    m = (wa * a + wb * b) / (wa + wb)
+    mask = m > threshold * m.max()
+    a, sa, b, sb, m = a[mask], sa[mask], b[mask], sb[mask], m[mask]
     s2 = sa * sa + sb * sb
     s = np.sqrt(s2)
     den = sa ** 4 / max(ba - 1, 1) + sb ** 4 / max(bb - 1, 1)
     dof = np.where(den > 0, s2 * s2 / np.maximum(den, 1e-300), 1e9)
     tq = _t_quantile(0.5 + 0.5 * P_2SIGMA, np.maximum(dof, 1.0))
     ok = np.abs(a - b) <= tq * s
-    rel = (a - b) / b
-    noise = math.sqrt(2.0 / math.pi) * s / b
+    rel = (a - b) / m
+    noise = math.sqrt(2.0 / math.pi) * s / m
     tot_a, tot_b = a.sum(), b.sum()
     tot_s = math.sqrt(float((sa ** 2).sum() + (sb ** 2).sum()))   # voxels treated as independent
     return {
         "voxels": int(mask.sum()),
         "within_2sigma": float(ok.mean()),
         "expected_within_2sigma": P_2SIGMA,
-        "mean_signed_pct": 100.0 * float((tot_a - tot_b) / tot_b),
+        "mean_signed_pct": 100.0 * float((tot_a - tot_b) / m.sum()),
         "mean_signed_voxel_pct": 100.0 * float(rel.mean()),
         "mean_abs_pct": 100.0 * float(np.abs(rel).mean()),
         "mean_abs_noise_pct": 100.0 * float(noise.mean()),
@@ -75,5 +84,5 @@ def compare(a, sa, ba, b, sb, bb, threshold=0.1):
         "max_abs_pct": 100.0 * float(np.abs(rel).max()),
         "total_ratio": float(tot_a / tot_b),
         "total_z": float((tot_a - tot_b) / tot_s) if tot_s > 0 else 0.0,
-        "mean_rel_sigma_pct": 100.0 * float((s / b).mean()),
+        "mean_rel_sigma_pct": 100.0 * float((s / m).mean()),
     }
