@@ -150,7 +150,46 @@ int BuildImage(const HostTables& h, DevTables<R>& T, void** dptr) {
   PutSplines<R>(cs, outs, img, fx, h.brem[0].x.front(), h.brem[0].x.back(), f2, n2);
   PutSplines<R>({&h.k1}, {&T.k1}, img, fx, h.k1.x.front(), h.k1.x.back(), f3, n3);
   PutSplines<R>({&h.moller}, {&T.moller}, img, fx, h.moller.x.front(), h.moller.x.back(), f4, n4);
-  const size_t elecEnd = f4 + n4 * sizeof(R);
+  size_t elecEnd = f4 + n4 * sizeof(R);
+  if (sizeof(R) == sizeof(float)) {
+    // dE/dx and 1/lambda_1 share the electron energy grid (the reference's data
+    // files write both on it): one 32-byte record per bin serves a sub-step's
+    // two lookups at one energy
+    std::vector<R> all;
+    std::vector<size_t> offs;
+    for (int m = 0; m < h.nmat; ++m) {
+      const Curve& a = h.dedx[m];
+      const Curve& b = h.itr1[m];
+      bool same = a.x.size() == b.x.size();
+      for (size_t i = 0; same && i < a.x.size(); ++i) same = std::abs(a.x[i] - b.x[i]) <= 1e-12 * a.x[i];
+      if (!same)
+        return Fail(DPMX_ERR_PARSE, "eloss_rdedx.dat and el_itr1mfp.dat of material " + std::to_string(m) +
+                                        " are not on one energy grid");
+      std::vector<double> ab, ac, ad, bb, bc, bd;
+      SplineCoefficients(a.x, a.y, ab, ac, ad);
+      SplineCoefficients(b.x, b.y, bb, bc, bd);
+      offs.push_back(all.size());
+      for (size_t i = 0; i < a.x.size(); ++i) {
+        all.push_back(R(a.y[i])); all.push_back(R(ab[i])); all.push_back(R(ac[i])); all.push_back(R(ad[i]));
+        all.push_back(R(b.y[i])); all.push_back(R(bb[i])); all.push_back(R(bc[i])); all.push_back(R(bd[i]));
+      }
+      for (size_t i = 0; i < a.x.size(); ++i) all.push_back(R(a.x[i]));
+      while (all.size() % 4 != 0) all.push_back(R(0));
+    }
+    const size_t base = img.Put(all.data(), all.size() * sizeof(R));
+    for (int m = 0; m < h.nmat; ++m) {
+      SplinePairT<R>& s = T.di[m];
+      const Curve& a = h.dedx[m];
+      s.n = int(a.x.size());
+      const double lmin = std::log(a.x[0]);
+      s.logMin = R(lmin);
+      s.invLogDelta = R(1.0 / (std::log(a.x[1]) - lmin));
+      s.emin = R(h.dedx[0].x.front());
+      s.emaxm = R(h.dedx[0].x.back() - 1.0E-6);
+      fx.Add(reinterpret_cast<const void**>(&s.p), base + offs[m] * sizeof(R));
+    }
+    elecEnd = base + all.size() * sizeof(R);
+  }
   // photon linear tables, contiguous
   const size_t photBegin = (img.bytes.size() + 255) & ~size_t(255);
   PutLinear<R>(h.imfpMax, T.imfpMax, img, fx, h.imfpMax.x.front(), h.imfpMax.x.back());

@@ -28,6 +28,14 @@ struct SplineT {       // natural cubic spline on a log-uniform grid: n x {x,y,b
   R logMin, invLogDelta, emin, emaxm;   // emaxm = emax - 1e-6 (loader clamp)
 };
 template <class R>
+struct SplinePairT {   // FP32 only: two splines of a material on one log-uniform grid (dE/dx and
+                       // 1/lambda_1), n x {y,b,c,d of the first, y,b,c,d of the second} in
+                       // 32-byte records, then the n grid points
+  const R* p;
+  int n;
+  R logMin, invLogDelta, emin, emaxm;
+};
+template <class R>
 struct LinearT {       // linear interpolation on a uniform grid: n x {x,y} (FP64), n x y (FP32)
   const R* p;
   int n;
@@ -60,6 +68,7 @@ struct DevTables {
   R ecut, gcut;
   R density[kMaxMat], mollerScale[kMaxMat];
   SplineT<R> dedx[kMaxMat], itr1[kMaxMat], brem[kMaxMat], k1, moller;
+  SplinePairT<R> di[kMaxMat];   // FP32: dedx and itr1 of each material in one record per bin
   LinearT<R> imfpMax, tot[kMaxMat], comp[kMaxMat], pair[kMaxMat];
   AliasSetT<R> kn, mol, sb[kMaxMat];
   GSSetT<R> gs;

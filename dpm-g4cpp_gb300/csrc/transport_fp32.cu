@@ -95,6 +95,7 @@ struct PTables {
 // shared-memory copies of the electron spline tables
 struct ETables {
   SplineT<float> dedx[kMaxMat], itr1[kMaxMat], brem[kMaxMat], k1, moller;
+  SplinePairT<float> di[kMaxMat];   // dE/dx and 1/lambda_1 in one record per bin (read in place)
 };
 
 __device__ __forceinline__ SplineT<float> Rebase(const SplineT<float>& s, const float* gbase, float* sbase) {
@@ -111,6 +112,7 @@ __device__ void StageElectronTables(const DevTables<float>& T, float* sdata, ETa
       et->dedx[m] = Rebase(T.dedx[m], T.elecBase, sdata);
       et->itr1[m] = Rebase(T.itr1[m], T.elecBase, sdata);
       et->brem[m] = Rebase(T.brem[m], T.elecBase, sdata);
+      et->di[m] = T.di[m];   // read in place
     }
     et->k1 = Rebase(T.k1, T.elecBase, sdata);
     et->moller = Rebase(T.moller, T.elecBase, sdata);
@@ -150,6 +152,7 @@ __device__ void BindElectronTables(const DevTables<float>& T, ETables* et) {
     et->dedx[m] = T.dedx[m];
     et->itr1[m] = T.itr1[m];
     et->brem[m] = T.brem[m];
+    et->di[m] = T.di[m];
   }
   et->k1 = T.k1;
   et->moller = T.moller;
@@ -164,6 +167,25 @@ __device__ __forceinline__ float SplineLe(const SplineT<float>& s, float e, floa
   const float4 q = reinterpret_cast<const float4*>(s.p)[il];   // y, b, c, d
   const float xv = ec - s.p[4 * s.n + il];
   return fmaxf(1.0E-20f, q.x + xv * (q.y + xv * (q.z + xv * q.w)));
+}
+
+// dE/dx and 1/lambda_1 at e (log le) from one 32-byte record: the same
+// arithmetic as SplineLe on each, one index computation and one grid point
+struct DedxItr1 {
+  float dedx, itr1;
+};
+__device__ __forceinline__ DedxItr1 SplinePairLe(const SplinePairT<float>& s, float e, float le) {
+  const float ec = fminf(s.emaxm, fmaxf(s.emin, e));
+  const float lc = (ec == e) ? le : __logf(ec);
+  int il = int((lc - s.logMin) * s.invLogDelta);
+  il = il < 0 ? 0 : (il > s.n - 2 ? s.n - 2 : il);
+  const float4* r = reinterpret_cast<const float4*>(s.p) + 2 * il;
+  const float4 q = r[0], t = r[1];
+  const float xv = ec - s.p[8 * s.n + il];
+  DedxItr1 o;
+  o.dedx = fmaxf(1.0E-20f, q.x + xv * (q.y + xv * (q.z + xv * q.w)));
+  o.itr1 = fmaxf(1.0E-20f, t.x + xv * (t.y + xv * (t.z + xv * t.w)));
+  return o;
 }
 
 // ---------------------------------------------------------------------------
@@ -1296,11 +1318,16 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
     const float ecut = T.ecut;
     const float rho = VoxelRho(J, T, p.ix, p.iy, p.iz, im);
     step = s.sGeom;
+    // dE/dx and 1/lambda_1 at E and at the mid-step energy, each pair from
+    // one record; a step that no event shortens ends with the same mid-step
+    // energy, whose dE/dx is then already at hand
     const float le = __logf(p.e);
-    float dedx = SplineLe(et.dedx[im], p.e, le) * rho;
+    const DedxItr1 atE = SplinePairLe(et.di[im], p.e, le);
+    float dedx = atE.dedx * rho;
     float emid = fmaxf(p.e - 0.5f * step * dedx, ecut);
     const float lm = __logf(emid);
-    float dTr1 = SplineLe(et.itr1[im], emid, lm) * rho;
+    const DedxItr1 atMid = SplinePairLe(et.di[im], emid, lm);
+    float dTr1 = atMid.itr1 * rho;
     const float dMol = s.invMol * T.mollerScale[im] * rho;
     const float dBrem = SplineLe(et.brem[im], emid, lm) * rho;
     const float sBrem = s.nBrem / dBrem;
@@ -1309,7 +1336,7 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
     if (sMol < step) { step = sMol; what = 2; }
     float sEl = s.nTr1 / dTr1;
     if (sEl < step) {
-      sEl = s.nTr1 / (SplineLe(et.itr1[im], p.e, le) * rho);
+      sEl = s.nTr1 / (atE.itr1 * rho);
       emid = fmaxf(p.e - 0.5f * sEl * dedx, ecut);
       dTr1 = SplineLe(et.itr1[im], emid, __logf(emid)) * rho;
       sEl = fminf(step, s.nTr1 / dTr1);
@@ -1319,8 +1346,12 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
     s.nBrem = (what == 1) ? 0.f : s.nBrem - step * dBrem;
     s.nMol = (what == 2) ? 0.f : s.nMol - step * dMol;
     s.nTr1 = (what == 3) ? 0.f : s.nTr1 - step * dTr1;
-    emid = fmaxf(p.e - 0.5f * step * dedx, ecut);
-    dedx = SplineLe(et.dedx[im], emid, __logf(emid)) * rho;
+    if (what == 0) {
+      dedx = atMid.dedx * rho;
+    } else {
+      emid = fmaxf(p.e - 0.5f * step * dedx, ecut);
+      dedx = SplineLe(et.dedx[im], emid, __logf(emid)) * rho;
+    }
     const float de = step * dedx;
     const float ef = p.e - de;
     if (ef < ecut) {

@@ -1,6 +1,6 @@
 """Measurements of the five workloads beyond the headline benchmark.
 
-    python dpm-g4cpp_gb300/measure.py [precision|slab|batching|differentiation|full] ... [--quick]
+    python dpm-g4cpp_gb300/measure.py [precision|slab|batching|differentiation|full|phases] ... [--quick]
 
 Each prints one JSON line. The workloads are synthetic, with the shapes of the
 reference's configurations:
@@ -15,6 +15,8 @@ reference's configurations:
   differentiation 128^3 phantom, 20x20 grid of 6 MeV beamlets: beamlet-tagged
                   run, CSR influence matrix, A w and A^T g, a few gradient steps
   full            512x512x256 x 1 mm CT-like phantom, 16 jobs, 1e9 histories
+  phases          the precision workload at --hist histories with every phase
+                  launch timed: the unit counts behind a profiler capture
 """
 import argparse
 import importlib
@@ -40,28 +42,15 @@ def emit(d):
     print(json.dumps(d), flush=True)
 
 
-def batch_mean_sigma(dose, dose2, n, batches):
-    """Per-history mean and its standard error from the batch sums."""
-    per = n / batches
-    s1 = dose / per
-    s2 = dose2 / (per * per)
-    mean = s1 / batches
-    var = np.maximum(s2 - s1 * s1 / batches, 0.0) / (batches * (batches - 1))
-    return mean, np.sqrt(var)
+dc = importlib.import_module("dpm-g4cpp_gb300.dosecheck")
 
 
-def compare(d1, s1, d2, s2, frac=0.1):
-    """Agreement of two dose estimates in the voxels above frac of the maximum."""
-    m = d2 > frac * d2.max()
-    diff = d1[m] - d2[m]
-    sc = np.sqrt(s1[m] ** 2 + s2[m] ** 2)
-    rel = diff / d2[m]
-    return {"voxels": int(m.sum()), "mean_signed_pct": float(100 * rel.mean()),
-            "mean_abs_pct": float(100 * np.abs(rel).mean()),
-            "noise_mean_abs_pct": float(100 * math.sqrt(2 / math.pi) * (sc / d2[m]).mean()),
-            "max_abs_pct": float(100 * np.abs(rel).max()),
-            "within_2sigma": float((np.abs(diff) <= 2 * sc).mean()),
-            "total_ratio": float(d1.sum() / d2.sum())}
+def compare(d1, q1, n1, d2, q2, n2, batches=10):
+    """Agreement of two runs' dose estimates (tallies of `batches` batches) in
+    the voxels above 10 % of the maximum (dosecheck.compare)."""
+    a, sa = dc.batch_estimate(d1, q1, batches, n1)
+    b, sb = dc.batch_estimate(d2, q2, batches, n2)
+    return dc.compare(a, sa, batches, b, sb, batches)
 
 
 def run_timed(tables, jobs, **kw):
@@ -83,14 +72,12 @@ def slab(quick):
     r32, w32 = run_timed(t, [dpm.Job(ph, src, n32, 12345)], batches=10)
     a64, q64, _ = r64.tally(0)
     a32, q32, _ = r32.tally(0)
-    m64, s64 = batch_mean_sigma(a64, q64, n64, 10)
-    m32, s32 = batch_mean_sigma(a32, q32, n32, 10)
     emit({"workload": "slab: 15 MeV e- pencil, Water/Ti/Bone/Water, 1 mm bins",
           "fp64_hist_per_s": n64 / (r64.elapsed_ms * 1e-3), "fp32_hist_per_s": n32 / (r32.elapsed_ms * 1e-3),
           "speedup_fp32_over_fp64": (n32 / r32.elapsed_ms) / (n64 / r64.elapsed_ms),
           "fp64_histories": n64, "fp32_histories": n32,
           "edep_per_history_fp64": r64.stats(0).edep / n64, "edep_per_history_fp32": r32.stats(0).edep / n32,
-          "dose_fp32_vs_fp64": compare(m32, s32, m64, s64)})
+          "dose_fp32_vs_fp64": compare(a32, q32, n32, a64, q64, n64)})
 
 
 def precision(quick):
@@ -104,15 +91,26 @@ def precision(quick):
     r32, _ = run_timed(t, [dpm.Job(ph, src, n32, 7)], batches=10)
     a64, q64, _ = r64.tally(0)
     a32, q32, _ = r32.tally(0)
-    m64, s64 = batch_mean_sigma(a64, q64, n64, 10)
-    m32, s32 = batch_mean_sigma(a32, q32, n32, 10)
     st = r32.stats(0)
     emit({"workload": "precision: 128x128x256 x 2 mm, 10x10 cm2 photons U[1,20] MeV",
           "fp64_hist_per_s": n64 / (r64.elapsed_ms * 1e-3), "fp32_hist_per_s": n32 / (r32.elapsed_ms * 1e-3),
           "speedup_fp32_over_fp64": (n32 / r32.elapsed_ms) / (n64 / r64.elapsed_ms),
           "fp64_histories": n64, "fp32_histories": n32,
           "energy_check": {"max_residual_mev": st.max_residual, "violations": st.residual_violations, "lost": st.lost},
-          "dose_fp32_vs_fp64": compare(m32, s32, m64, s64)})
+          "dose_fp32_vs_fp64": compare(a32, q32, n32, a64, q64, n64)})
+
+
+def phases(quick, hist=1e6):
+    """The precision workload at `hist` histories, run twice (the first warms
+    up); the second run launches every phase kernel outside a graph and
+    prints its phase profile: the electron sub-steps and photon steps of
+    exactly the launches a profiler captures from that run."""
+    t = dpm.Tables(DATA_WLB)
+    ph = dpm.Phantom.voxels(t, wl.precision_phantom(), 2.0)
+    src = wl.precision_source()
+    for k in range(2):
+        r = dpm.run(t, [dpm.Job(ph, src, int(hist), 7 + k)], batches=10, profile_phases=True)
+    emit({"workload": "precision phases", "histories": int(hist), "profile": r.profile, "config": r.config})
 
 
 def batching(quick):
@@ -221,9 +219,10 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("what", nargs="*", default=["slab", "precision", "batching", "differentiation", "full"])
     ap.add_argument("--quick", action="store_true", help="reduced sizes")
+    ap.add_argument("--hist", type=float, default=1e6, help="histories of the phases run")
     a = ap.parse_args()
     fns = {"slab": slab, "precision": precision, "batching": batching, "differentiation": differentiation,
-           "full": full}
+           "full": full, "phases": lambda q: phases(q, a.hist)}
     for w in a.what:
         fns[w](a.quick)
         dpm.scratch_release()
