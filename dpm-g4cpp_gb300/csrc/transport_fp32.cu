@@ -1338,7 +1338,7 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
     if (sEl < step) {
       sEl = s.nTr1 / (atE.itr1 * rho);
       emid = fmaxf(p.e - 0.5f * sEl * dedx, ecut);
-      dTr1 = SplineLe(et.itr1[im], emid, __logf(emid)) * rho;
+      dTr1 = SplinePairLe(et.di[im], emid, __logf(emid)).itr1 * rho;
       sEl = fminf(step, s.nTr1 / dTr1);
       step = sEl;
       what = 3;
@@ -1346,12 +1346,8 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
     s.nBrem = (what == 1) ? 0.f : s.nBrem - step * dBrem;
     s.nMol = (what == 2) ? 0.f : s.nMol - step * dMol;
     s.nTr1 = (what == 3) ? 0.f : s.nTr1 - step * dTr1;
-    if (what == 0) {
-      dedx = atMid.dedx * rho;
-    } else {
-      emid = fmaxf(p.e - 0.5f * step * dedx, ecut);
-      dedx = SplineLe(et.dedx[im], emid, __logf(emid)) * rho;
-    }
+    emid = fmaxf(p.e - 0.5f * step * dedx, ecut);
+    dedx = SplinePairLe(et.di[im], emid, __logf(emid)).dedx * rho;
     const float de = step * dedx;
     const float ef = p.e - de;
     if (ef < ecut) {
