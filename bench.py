@@ -50,8 +50,8 @@ def parse():
     ap.add_argument("--hist", type=float, default=1e7, help="histories per step and GPU")
     ap.add_argument("--cpu-hist", type=int, default=200000, help="oracle histories per CPU worker and step")
     ap.add_argument("--batches", type=int, default=10, help="statistical batches per step")
-    ap.add_argument("--fp64-hist", type=float, default=2e6, help="histories of the FP64 GPU arm")
-    ap.add_argument("--check-hist", type=float, default=2e7, help="FP32 histories of the dose check")
+    ap.add_argument("--fp64-hist", type=float, default=1e7, help="histories of the FP64 GPU arm")
+    ap.add_argument("--check-hist", type=float, default=4e7, help="FP32 histories of the dose check")
     return ap.parse_args()
 
 
