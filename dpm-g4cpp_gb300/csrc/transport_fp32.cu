@@ -1627,7 +1627,11 @@ __global__ void __launch_bounds__(kBlockThreads, kBlockMinBlocks) ElectronPhaseB
       default:
         break;
     }
-    const int code = live ? StepSlot<AGG>(a, et, jobs, S, k, esc, nsteps, dacc) : 5;
+    // a slot that keeps stepping takes up to K sub-steps before it goes back
+    // to a ring (one call site; lanes whose slot had an event wait)
+    int code = live ? 0 : 5;
+    for (int rep = 0; rep < 2 && __any_sync(kFull, code == 0); ++rep)
+      if (code == 0) code = StepSlot<AGG>(a, et, jobs, S, k, esc, nsteps, dacc);
     // the ring of the slot's next action; a finished slot goes back to the
     // idle ring while there is work left, else it retires (q == kRings)
     int q = -1;
