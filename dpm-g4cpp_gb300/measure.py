@@ -17,6 +17,8 @@ reference's configurations:
   full            512x512x256 x 1 mm CT-like phantom, 16 jobs, 1e9 histories
   phases          the precision workload at --hist histories with every phase
                   launch timed: the unit counts behind a profiler capture
+  deposit         deposited energy per history, FP32 against FP64, for photon
+                  and electron sources (ten runs of each form, --seed)
 """
 import argparse
 import importlib
@@ -111,6 +113,34 @@ def phases(quick, hist=1e6):
     for k in range(2):
         r = dpm.run(t, [dpm.Job(ph, src, int(hist), 7 + k)], batches=10, profile_phases=True)
     emit({"workload": "precision phases", "histories": int(hist), "profile": r.profile, "config": r.config})
+
+
+def deposit(quick, seed0=11):
+    """Deposited energy per history, FP32 event form against the plain FP64
+    form, per source, on a 128x128x256 x 2 mm water box: ten independent runs
+    of each form (4e6 FP32 and 1e6 FP64 histories each, a tenth with --quick),
+    the mean and its standard error from their spread."""
+    t = dpm.Tables(DATA_WLB)
+    water = np.zeros((256, 128, 128), dtype=np.uint8)
+    ph = dpm.Phantom.voxels(t, water, 2.0)
+    broad = dict(particle=0, spectrum=0, shape=1, fx=100.0, fy=100.0)
+    cases = [("photons 1-20 MeV", wl.precision_source())]
+    cases += [("photons %g MeV" % e, dpm.Source(e0=e, e1=e, **broad)) for e in (2.0, 6.0, 10.0, 15.0, 19.0)]
+    cases += [("electrons %g MeV" % e, dpm.Source(particle=-1, e0=e, e1=e)) for e in (15.0, 19.0)]
+    K = 10
+    n32, n64 = (400_000, 100_000) if quick else (4_000_000, 1_000_000)
+    for name, src in cases:
+        out = {}
+        for prec, n in ((dpm.FP32_EVENT, n32), (dpm.FP64_PLAIN, n64)):
+            v = []
+            for k in range(K):
+                r = dpm.run(t, [dpm.Job(ph, src, n, seed0 + k, first_history=k * n)], precision=prec, batches=1)
+                v.append(r.stats(0).edep / n)
+                r.close()
+            out[prec] = (float(np.mean(v)), float(np.std(v, ddof=1) / math.sqrt(K)))
+        (a, sa), (b, sb) = out[dpm.FP32_EVENT], out[dpm.FP64_PLAIN]
+        emit({"workload": "deposited energy per history, water box", "source": name, "fp32_mev": a, "fp64_mev": b,
+              "diff_pct": 100.0 * (a - b) / b, "z": (a - b) / math.hypot(sa, sb)})
 
 
 def batching(quick):
@@ -220,9 +250,10 @@ def main():
     ap.add_argument("what", nargs="*", default=["slab", "precision", "batching", "differentiation", "full"])
     ap.add_argument("--quick", action="store_true", help="reduced sizes")
     ap.add_argument("--hist", type=float, default=1e6, help="histories of the phases run")
+    ap.add_argument("--seed", type=int, default=11, help="first seed of the deposit runs")
     a = ap.parse_args()
     fns = {"slab": slab, "precision": precision, "batching": batching, "differentiation": differentiation,
-           "full": full, "phases": lambda q: phases(q, a.hist)}
+           "full": full, "phases": lambda q: phases(q, a.hist), "deposit": lambda q: deposit(q, a.seed)}
     for w in a.what:
         fns[w](a.quick)
         dpm.scratch_release()
