@@ -1,6 +1,7 @@
 """Builds the native parts of the package in place (no CMake):
 
   lib/libdpmx.so          CUDA kernels (sm_103a) + host C++ behind include/dpmx.h
+  lib/libdpmx_torch.so    torch.ops.dpmx operators over the influence matrix
   bin/dpm_simulate        drop-in for the reference `dpm_Simulate` CLI
   bin/dpm_generate_data   Geant4-free writer of the reference data files
 
@@ -101,9 +102,31 @@ def build_tools():
     return cli, gen
 
 
+TORCH_OPS = os.path.join(LIBDIR, "libdpmx_torch.so")
+
+
+def build_torch_ops():
+    """lib/libdpmx_torch.so: the torch.ops.dpmx operators (csrc/torch_ops.cpp),
+    compiled against the installed PyTorch and linked to libdpmx.so."""
+    src = os.path.join(CSRC, "torch_ops.cpp")
+    if not _stale(TORCH_OPS, [src, LIB, os.path.join(INCLUDE, "dpmx.h")]):
+        return TORCH_OPS
+    import torch
+    from torch.utils import cpp_extension as ce
+    abi = int(torch.compiled_with_cxx11_abi())
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-D_GLIBCXX_USE_CXX11_ABI=%d" % abi, "-I" + INCLUDE,
+           "-I/usr/local/cuda/include"]
+    cmd += ["-I" + p for p in ce.include_paths()]
+    cmd += [src, "-o", TORCH_OPS, "-L" + LIBDIR, "-ldpmx", "-Wl,-rpath,$ORIGIN"]
+    cmd += ["-L" + p for p in ce.library_paths()] + ["-lc10", "-lc10_cuda", "-ltorch_cpu", "-ltorch_cuda"]
+    _run(cmd)
+    return TORCH_OPS
+
+
 def build(verbose=False):
     lib = build_library(verbose)
     build_tools()
+    build_torch_ops()
     return lib
 
 

@@ -8,10 +8,30 @@ backward is A^T g; both products run in the library's CUDA kernels on torch's
 current stream, with FP64 vectors and FP64 accumulation.
 """
 import ctypes as C
+import os
 
 import numpy as np
 
 from . import _check, library
+
+_OPS = None
+
+
+def torch_ops():
+    """torch.ops.dpmx (lib/libdpmx_torch.so, built with the library): the
+    influence matrix as registered operators on the library's matrix handle:
+    influence_build(result, job, threshold) -> handle, csr_tensor(handle) ->
+    sparse CSR tensor, csr_matvec(handle, x), csr_rmatvec(handle, y),
+    csr_free(handle)."""
+    global _OPS
+    if _OPS is None:
+        import torch
+        path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib", "libdpmx_torch.so")
+        if not os.path.exists(path):
+            raise RuntimeError("torch operators %s not built (run build())" % path)
+        torch.ops.load_library(path)
+        _OPS = torch.ops.dpmx
+    return _OPS
 
 
 class InfluenceMatrix:
@@ -37,6 +57,11 @@ class InfluenceMatrix:
         data = np.zeros(max(1, self.nnz), dtype=np.float32)
         _check(library().dpmx_csr_download(self._h, indptr.ctypes.data, indices.ctypes.data, data.ctypes.data))
         return indptr, indices[:self.nnz], data[:self.nnz]
+
+    def to_torch(self):
+        """A as a torch sparse CSR tensor on the GPU (torch.ops.dpmx.csr_tensor)."""
+        h = self._h.value if hasattr(self._h, "value") else self._h
+        return torch_ops().csr_tensor(int(h))
 
     def to_scipy(self):
         """A as a scipy.sparse.csr_matrix on the host (FP32 values)."""

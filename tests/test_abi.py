@@ -38,3 +38,15 @@ def test_tools_built():
     builder.build()
     assert os.access(os.path.join(builder.BINDIR, "dpm_simulate"), os.X_OK)
     assert os.access(os.path.join(builder.BINDIR, "dpm_generate_data"), os.X_OK)
+
+
+def test_torch_operators_build_and_register():
+    """lib/libdpmx_torch.so builds against the installed PyTorch and registers
+    the torch.ops.dpmx operators (no GPU needed to load it)"""
+    import importlib
+    builder = importlib.import_module("dpm-g4cpp_gb300.builder")
+    builder.build()
+    inf = importlib.import_module("dpm-g4cpp_gb300.influence")
+    ops = inf.torch_ops()
+    for name in ["influence_build", "csr_tensor", "csr_matvec", "csr_rmatvec", "csr_free"]:
+        assert hasattr(ops, name), name

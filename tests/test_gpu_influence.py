@@ -117,3 +117,30 @@ def test_influence_matrix_vs_cpu_built(tables_wlb, dpm, orc):
     print("A^T g z-scores", np.round(z, 2), "coverage", within / voxels)
     assert np.all(np.abs(z) < 4.0), z
     assert abs(np.mean((mg - mo) / mo)) < 0.01
+
+
+def test_torch_operators(setup, tables_wlb, dpm):
+    """torch.ops.dpmx (the registered C++ operators over the library's matrix
+    handle) give the same matrix and the same products as the ctypes path"""
+    import torch
+    inf = importlib.import_module("dpm-g4cpp_gb300.influence")
+    ops = inf.torch_ops()
+    A = setup["A"]
+    S = A.to_scipy()
+    T = A.to_torch()
+    assert T.layout == torch.sparse_csr and tuple(T.shape) == (A.rows, A.cols)
+    np.testing.assert_array_equal(T.crow_indices().cpu().numpy(), S.indptr)
+    np.testing.assert_array_equal(T.col_indices().cpu().numpy(), S.indices)
+    np.testing.assert_array_equal(T.values().cpu().numpy(), S.data)
+    # a second matrix built through the operators from the same run
+    res = setup["res"]
+    rh = res._h.value if hasattr(res._h, "value") else res._h
+    h = ops.influence_build(int(rh), 0, 0.0)
+    try:
+        rng = np.random.default_rng(3)
+        x = torch.tensor(rng.random(A.cols), device="cuda")
+        g = torch.tensor(rng.random(A.rows), device="cuda")
+        assert torch.equal(ops.csr_matvec(h, x), A.matvec(x))
+        assert torch.equal(ops.csr_rmatvec(h, g), A.rmatvec(g))
+    finally:
+        ops.csr_free(h)
