@@ -213,6 +213,9 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
   const double budget = std::min(16.0e9, double(freeB) / 8.0);
   const int R = int(std::max(1.0, std::min(double(batches), budget / (8.0 * double(std::max(1LL, total))))));
   const int ngroups = (batches + R - 1) / R;
+  // the phase kernels address bins and slices with 32-bit offsets
+  if (double(R) * double(total) >= 4294967296.0 || double(total) >= 4294967296.0)
+    return Fail(DPMX_ERR_ARG, "the tallies of one run exceed 2^32 bins; run the jobs in smaller groups");
   const long long binStride = kInterleaveSlices ? R : 1, sliceStride = kInterleaveSlices ? 1 : total;
   double *tB, *dose, *dose2;
   if (int rc = buf.Get(&tB, size_t(R) * total)) return rc;

@@ -267,8 +267,10 @@ __device__ __forceinline__ void Score(const JobF& J, uint32_t meta, int ix, int 
     atomicAdd(d.n + b, 1u);
     return;
   }
-  const long long idx = J.tallyDepth ? (long long)iz : ((long long)iz * J.ny + iy) * J.nx + ix;
-  double* ptr = J.tally + (long long)slice * J.sstride + idx * J.tstride;
+  // bins and slices of a run stay below 2^32 doubles (checked when the run is
+  // planned): 32-bit index arithmetic, one widening for the address
+  const uint32_t idx = J.tallyDepth ? uint32_t(iz) : (uint32_t(iz) * uint32_t(J.ny) + uint32_t(iy)) * uint32_t(J.nx) + uint32_t(ix);
+  double* ptr = J.tally + (slice * uint32_t(J.sstride) + idx * uint32_t(J.tstride));
   if (agg) {
     cg::coalesced_group g = cg::coalesced_threads();
     cg::coalesced_group peers = cg::labeled_partition(g, (unsigned long long)ptr);
@@ -280,7 +282,7 @@ __device__ __forceinline__ void Score(const JobF& J, uint32_t meta, int ix, int 
   if (J.steps) atomicAdd(J.steps + iz, 1.0);
   if (J.btally) {
     const long long nvox = (long long)J.nx * J.ny * J.nz;
-    atomicAdd(J.btally + (long long)(hist % uint32_t(J.nbeamlets)) * nvox + idx, de);
+    atomicAdd(J.btally + (long long)(hist % uint32_t(J.nbeamlets)) * nvox + (long long)idx, de);
   }
 }
 
@@ -317,7 +319,8 @@ __device__ __forceinline__ void DepthAccFlush(const PhaseArgs& a, const JobF* jo
 
 // density of voxel (ix, iy, iz) of material im (Geom::GetVoxelMaterialDensity)
 __device__ __forceinline__ float VoxelRho(const JobF& J, const DevTables<float>& T, int ix, int iy, int iz, int im) {
-  return J.rho ? __ldg(J.rho + ((long long)iz * J.ny + iy) * J.nx + ix) : T.density[im];
+  return J.rho ? __ldg(J.rho + (uint32_t(iz) * uint32_t(J.ny) + uint32_t(iy)) * uint32_t(J.nx) + uint32_t(ix))
+               : T.density[im];
 }
 
 __device__ __forceinline__ bool InBox(const JobF& J, int ix, int iy, int iz) {
@@ -325,7 +328,8 @@ __device__ __forceinline__ bool InBox(const JobF& J, int ix, int iy, int iz) {
 }
 
 __device__ __forceinline__ int MaterialAt(const JobF& J, int ix, int iy, int iz) {
-  const uint8_t m = J.matByDepth ? __ldg(J.mat + iz) : __ldg(J.mat + ((long long)iz * J.ny + iy) * J.nx + ix);
+  const uint8_t m = J.matByDepth ? __ldg(J.mat + iz)
+                                 : __ldg(J.mat + (uint32_t(iz) * uint32_t(J.ny) + uint32_t(iy)) * uint32_t(J.nx) + uint32_t(ix));
   return m == kVacuum ? -1 : int(m);
 }
 
