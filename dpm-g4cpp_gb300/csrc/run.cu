@@ -406,20 +406,44 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
   CK(cudaEventCreate(&e1));
   int rc = DPMX_OK;
   if (useGraph) {
+    // The executable graph of the calling thread's previous run is kept: a new
+    // run of the same shape (jobs, chunk plan, buffers) only differs in kernel
+    // and copy parameters, which cudaGraphExecUpdate applies without
+    // instantiating again; any other run instantiates and replaces it. Runs of
+    // one thread do not overlap (each ends with a synchronisation), so the
+    // executable is never updated while in flight. It is not destroyed at
+    // thread exit (no CUDA calls while the process shuts down).
+    static thread_local cudaGraphExec_t tlExec = nullptr;
+    static thread_local int tlDev = -1;
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
     cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
     CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     rc = enqueue(st);
     cudaError_t ce = cudaStreamEndCapture(st, &graph);
     if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
     CK(ce);
-    CK(cudaGraphInstantiate(&exec, graph, 0));
+    bool updated = false;
+    if (tlExec && tlDev == dev) {
+      cudaGraphExecUpdateResultInfo info;
+      if (cudaGraphExecUpdate(tlExec, graph, &info) == cudaSuccess) {
+        updated = true;
+      } else {
+        cudaGetLastError();
+        cudaGraphExecDestroy(tlExec);
+        tlExec = nullptr;
+      }
+    }
+    if (!updated) {
+      const cudaError_t ie = cudaGraphInstantiate(&tlExec, graph, 0);
+      if (ie != cudaSuccess) { tlExec = nullptr; cudaGraphDestroy(graph); CK(ie); }
+      tlDev = dev;
+    }
+    cudaGraphDestroy(graph);
     CK(cudaEventRecord(e0, st));
-    CK(cudaGraphLaunch(exec, st));
+    CK(cudaGraphLaunch(tlExec, st));
     CK(cudaEventRecord(e1, st));
     CK(cudaStreamSynchronize(st));
-    cudaGraphExecDestroy(exec);
-    cudaGraphDestroy(graph);
   } else {
     CK(cudaEventRecord(e0, st));
     rc = enqueue(st);
