@@ -47,32 +47,39 @@ def _ellipsoid(shape, v, centre, semi):
     return ((xx - centre[0]) / semi[0]) ** 2 + ((yy - centre[1]) / semi[1]) ** 2 + ((zz - centre[2]) / semi[2]) ** 2 < 1
 
 
+def batching_job_spec(i, v=2.0, hist_range=(1e5, 1e7), scale=1.0):
+    """Job i of the batching workload, drawn from seed i: a cubic phantom with
+    edge in {32,64,96,128,192} voxels of v mm (water base), 3 ellipsoidal
+    inserts of a random material (water/lung/bone), an electron or photon beam
+    (p = 0.5) of a monoenergetic energy uniform in [4, 20] MeV covering the
+    central half of the entry face, and a history count log-uniform in
+    hist_range (times `scale`). Returns (mat[nz,ny,nx], Source, histories)."""
+    rng = np.random.default_rng(i)
+    edge = int(rng.choice([32, 64, 96, 128, 192]))
+    shape = (edge, edge, edge)
+    m = np.full(shape, WATER, dtype=np.uint8)
+    L = edge * v
+    for _ in range(3):
+        mat = int(rng.integers(0, 3))
+        centre = (rng.uniform(-0.3, 0.3) * L, rng.uniform(-0.3, 0.3) * L, rng.uniform(0.2, 0.8) * L)
+        semi = tuple(rng.uniform(0.05, 0.25) * L for _ in range(3))
+        m[_ellipsoid(shape, v, centre, semi)] = mat
+    particle = -1 if rng.random() < 0.5 else 0
+    energy = float(rng.uniform(4.0, 20.0))
+    hist = int(round(math.exp(rng.uniform(math.log(hist_range[0]), math.log(hist_range[1]))) * scale))
+    src = Source(particle=particle, spectrum=0, e0=energy, e1=energy, shape=1, fx=0.5 * L, fy=0.5 * L)
+    return m, src, max(1, hist)
+
+
 def batching_jobs(tables, njobs=64, v=2.0, hist_range=(1e5, 1e7), scale=1.0):
-    """64 independent jobs; job i draws from seed i a cubic phantom with edge in
-    {32,64,96,128,192} voxels of 2 mm (water base), 3 ellipsoidal inserts of a
-    random material (water/lung/bone), an electron or photon beam (p = 0.5) of
-    a monoenergetic energy uniform in [4, 20] MeV covering the central half of
-    the entry face, and a history count log-uniform in [1e5, 1e7] (times
-    `scale`). Returns (jobs, phantoms)."""
+    """The 64 independent jobs of the batching workload (batching_job_spec),
+    job i with seed i. Returns (jobs, phantoms)."""
     jobs, phantoms = [], []
     for i in range(njobs):
-        rng = np.random.default_rng(i)
-        edge = int(rng.choice([32, 64, 96, 128, 192]))
-        shape = (edge, edge, edge)
-        m = np.full(shape, WATER, dtype=np.uint8)
-        L = edge * v
-        for _ in range(3):
-            mat = int(rng.integers(0, 3))
-            centre = (rng.uniform(-0.3, 0.3) * L, rng.uniform(-0.3, 0.3) * L, rng.uniform(0.2, 0.8) * L)
-            semi = tuple(rng.uniform(0.05, 0.25) * L for _ in range(3))
-            m[_ellipsoid(shape, v, centre, semi)] = mat
-        particle = -1 if rng.random() < 0.5 else 0
-        energy = float(rng.uniform(4.0, 20.0))
-        hist = int(round(math.exp(rng.uniform(math.log(hist_range[0]), math.log(hist_range[1]))) * scale))
+        m, src, hist = batching_job_spec(i, v, hist_range, scale)
         ph = Phantom.voxels(tables, m, v)
-        src = Source(particle=particle, spectrum=0, e0=energy, e1=energy, shape=1, fx=0.5 * L, fy=0.5 * L)
         phantoms.append(ph)
-        jobs.append(Job(ph, src, max(1, hist), seed=i))
+        jobs.append(Job(ph, src, hist, seed=i))
     return jobs, phantoms
 
 

@@ -85,19 +85,21 @@ def test_history_split_sums_to_whole(tables_wlb, dpm):
 
 
 def test_fp64_batched_matches_oracle_voxel(tables_wlb, oracle_wlb, dpm):
-    """a small voxel job, FP64 form, history by history against the oracle"""
+    """a small voxel job, FP64 form, history by history against the oracle:
+    identical streams give identical histories except where a last-bit
+    difference of a transcendental flips a branch; those are counted"""
     wl = importlib.import_module("dpm-g4cpp_gb300.workloads")
     m = wl.precision_phantom(nx=24, ny=24, nz=48, v=5.0)
     ph = dpm.Phantom.voxels(tables_wlb, m, 5.0)
     src = wl.precision_source(field=60.0)
     n = 3000
-    res = dpm.run(tables_wlb, [dpm.Job(ph, src, n, 77)], precision=dpm.FP64_PLAIN, batches=1)
-    g = res.tally(0)[0]
+    he, g = dpm.job_histories(tables_wlb, dpm.Job(ph, src, n, 77), with_dose=True)
     s = dict(particle=src.particle, spectrum=src.spectrum, e0=src.e0, e1=src.e1, shape=src.shape, cx=src.cx,
              cy=src.cy, fx=src.fx, fy=src.fy, nbx=src.nbx, nby=src.nby)
-    o, he, _ = oracle_wlb.simulate_voxel(m, 5.0, s, n, 77)
-    # identical streams: the summed dose agrees to rounding except for the rare
-    # histories where a 1-ulp transcendental difference flips a branch
-    assert abs(g.sum() / o.sum() - 1) < 2e-3
-    close = np.isclose(g, o, rtol=1e-6, atol=1e-9 * o.max())
-    assert close.mean() > 0.8, close.mean()
+    o, ho, _ = oracle_wlb.simulate_voxel(m, 5.0, s, n, 77)
+    same = np.isclose(he, ho, rtol=1e-9, atol=1e-12)
+    assert (~same).sum() <= max(1, int(0.02 * n)), int((~same).sum())
+    assert abs(he[same].sum() / ho[same].sum() - 1) < 1e-9
+    # the run through dpmx_run gives the same dose as the per-history hook
+    res = dpm.run(tables_wlb, [dpm.Job(ph, src, n, 77)], precision=dpm.FP64_PLAIN, batches=1)
+    np.testing.assert_allclose(res.tally(0)[0].reshape(-1), g, rtol=1e-9, atol=1e-12 * g.max())

@@ -15,6 +15,12 @@ on the host cores.
 * FP64 form against the oracle history by history (both draw the same
   per-history Philox stream): the share of histories whose deposited energy
   differs beyond rounding is counted and bounded.
+* The other workloads' geometries, FP32 against the oracle in the same way:
+  four jobs of the batching workload (electron and photon beams on cubic
+  phantoms with lung and bone inserts) and the CT-like phantom of the
+  full-scale workload at 4 mm (body in air, lungs, spine, ribs; falling
+  photon spectrum), each held to the 2-sigma coverage that 3 binomial
+  standard deviations allow under 95.45 % for its voxel count.
 """
 import importlib
 import json
@@ -95,3 +101,64 @@ def test_fp64_voxel_histories_vs_oracle(tables_wlb, oracle_wlb, dpm):
     assert r["diverging_share"] <= 0.02, r
     assert abs(r["matching_deposit_ratio"] - 1.0) < 1e-9, r
     assert abs(r["dose_ratio"] - 1.0) < 5e-3, r
+
+
+# jobs of the batching workload (job i drawn from seed i): 64^3 e- 14.5 MeV,
+# 32^3 e- 9.0 MeV, 64^3 photons 14.1 MeV, 32^3 photons 5.0 MeV, each with
+# lung / bone ellipsoid inserts
+BATCH_JOBS = (21, 34, 36, 47)
+
+
+def test_batching_jobs_vs_oracle(tables_wlb, dpm, orc):
+    """four jobs of the batching workload in one FP32 run against the oracle,
+    job by job: coverage of the t-corrected 2 sigma no lower than 3 binomial
+    standard deviations under 95.45 %, dose-weighted mean difference and
+    excess |difference| within 1 %"""
+    wl = importlib.import_module("dpm-g4cpp_gb300.workloads")
+    dc = importlib.import_module("dpm-g4cpp_gb300.dosecheck")
+    specs = [wl.batching_job_spec(i) for i in BATCH_JOBS]
+    orcl = [orc.voxel_batches(DATA_WLB, m, 2.0, _source_dict(s), 40_000, 48, 1000 + i)
+            for i, (m, s, _) in zip(BATCH_JOBS, specs)]
+    phs = [dpm.Phantom.voxels(tables_wlb, m, 2.0) for m, _, _ in specs]
+    n = 4_000_000
+    res = dpm.run(tables_wlb, [dpm.Job(p, s, n, i) for p, (_, s, _), i in zip(phs, specs, BATCH_JOBS)], batches=40)
+    out = {}
+    for j, (o, so, _) in enumerate(orcl):
+        st = res.stats(j)
+        assert st.lost == 0 and st.residual_violations == 0, st
+        d, d2, _ = res.tally(j)
+        g, sg = dc.batch_estimate(d, d2, 40, n)
+        r = dc.compare(g, sg, 40, o.reshape(-1), so.reshape(-1), 48)
+        out["job%d" % BATCH_JOBS[j]] = r
+        p = r["expected_within_2sigma"]
+        assert r["within_2sigma"] >= p - 3.0 * np.sqrt(p * (1 - p) / r["voxels"]), (BATCH_JOBS[j], r)
+        assert abs(r["mean_signed_pct"]) <= 1.0, (BATCH_JOBS[j], r)
+        assert r["mean_abs_excess_pct"] <= 1.0, (BATCH_JOBS[j], r)
+    _report("batching_jobs_fp32_vs_oracle", out)
+
+
+def test_ct_phantom_vs_oracle(dpm, orc, gpu_lib):
+    """the CT-like phantom of the full-scale workload (water body in air, two
+    lungs, spine, ribs; 10x10 cm2 photons, p(E) ~ (20 - E) on 0.5-20 MeV) at 4
+    mm, FP32 against the oracle"""
+    from conftest import ROOT
+    wl = importlib.import_module("dpm-g4cpp_gb300.workloads")
+    dc = importlib.import_module("dpm-g4cpp_gb300.dosecheck")
+    data = os.path.join(ROOT, "data", "water_lung_bone_air")
+    m = wl.full_scale_phantom(nx=128, ny=128, nz=64, v=4.0)
+    src = wl.full_scale_source()
+    o, so, _ = orc.voxel_batches(data, m, 4.0, _source_dict(src), 250_000, 48, 1099)
+    t = dpm.Tables(data)
+    ph = dpm.Phantom.voxels(t, m, 4.0)
+    n = 40_000_000
+    res = dpm.run(t, [dpm.Job(ph, src, n, 99)], batches=40)
+    st = res.stats(0)
+    assert st.lost == 0 and st.residual_violations == 0, st
+    d, d2, _ = res.tally(0)
+    g, sg = dc.batch_estimate(d, d2, 40, n)
+    r = dc.compare(g, sg, 40, o.reshape(-1), so.reshape(-1), 48)
+    _report("ct_phantom_fp32_vs_oracle", r)
+    p = r["expected_within_2sigma"]
+    assert r["within_2sigma"] >= p - 3.0 * np.sqrt(p * (1 - p) / r["voxels"]), r
+    assert abs(r["mean_signed_pct"]) <= 1.0, r
+    assert r["mean_abs_excess_pct"] <= 1.0, r
