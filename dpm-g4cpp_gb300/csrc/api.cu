@@ -378,6 +378,7 @@ int dpmx_phantom_slab(const dpmx_tables* t, int geom_index, double lbox, dpmx_ph
   std::vector<uint8_t> m(nz);
   for (int iz = 0; iz < nz; ++iz) m[iz] = uint8_t(SlabMaterialAt(geom_index, invL, iz));
   CK(cudaMalloc(&p->d_mat, nz));
+  p->matOwner.reset(p->d_mat, [](uint8_t* q) { cudaFree(q); });
   CK(cudaMemcpy(p->d_mat, m.data(), nz, cudaMemcpyHostToDevice));
   GridGeom& g = p->grid;
   g.nx = nx; g.ny = nx; g.nz = nz;
@@ -410,6 +411,7 @@ int dpmx_phantom_voxels(const dpmx_tables* t, int nx, int ny, int nz, double vx,
   // device writes the largest id other than vacuum: checked on the GPU
   const size_t nal = (n + 15) & ~size_t(15);
   CK(cudaMalloc(&p->d_mat, nal + 16));
+  p->matOwner.reset(p->d_mat, [](uint8_t* q) { cudaFree(q); });
   CK(cudaMemcpy(p->d_mat, mat, n, cudaMemcpyHostToDevice));
   unsigned* dworst = reinterpret_cast<unsigned*>(p->d_mat + nal);
   CK(cudaMemset(dworst, 0, sizeof(unsigned)));
@@ -422,7 +424,6 @@ int dpmx_phantom_voxels(const dpmx_tables* t, int nx, int ny, int nz, double vx,
   if (int(worst) >= t->h.nmat) return Fail(DPMX_ERR_ARG, "material id beyond the data set");
   auto lut = std::make_shared<std::vector<float>>(256, 0.0f);
   for (int m = 0; m < t->h.nmat; ++m) (*lut)[m] = float(t->h.density[m]);
-  auto hostMat = std::make_shared<std::vector<uint8_t>>(mat, mat + n);
   GridGeom& g = p->grid;
   g.nx = nx; g.ny = ny; g.nz = nz;
   g.vx = vx; g.vy = vy; g.vz = vz;
@@ -435,8 +436,7 @@ int dpmx_phantom_voxels(const dpmx_tables* t, int nx, int ny, int nz, double vx,
   g.rho = nullptr;
   g.wscale = 1.0;
   p->tallySize = (long long)n;
-  p->binMaterial = hostMat;
-  p->materialDensity = lut;
+  p->materialDensity = lut;   // the ids stay on the device (matOwner)
   *out = p.release();
   return DPMX_OK;
 }
@@ -470,7 +470,7 @@ int dpmx_phantom_voxels_density(const dpmx_tables* t, int nx, int ny, int nz, do
 
 void dpmx_phantom_free(dpmx_phantom* p) {
   if (!p) return;
-  cudaFree(p->d_mat);
+  p->matOwner.reset();   // the device ids go when no result holds them either
   cudaFree(p->d_rho);
   delete p;
 }

@@ -157,11 +157,13 @@ struct dpmx_phantom {
   double lbox = 1.0;
   dpmx::GridGeom grid{};    // voxel box (slab presets are materialised too)
   uint8_t* d_mat = nullptr;
+  std::shared_ptr<uint8_t> matOwner;   // owns d_mat; results keep it for their dose outputs
   float* d_rho = nullptr;   // per-voxel densities (dpmx_phantom_voxels_density) or null
   long long tallySize = 0;
-  // host copies for the dose outputs, shared with the results that outlive
-  // the phantom: the density of every tally bin [g/cm3] (0 for vacuum), either
-  // given per bin or as material ids and a density per material
+  // for the dose outputs, shared with the results that outlive the phantom:
+  // the density of every tally bin [g/cm3] (0 for vacuum), either given per
+  // bin or as material ids (a host copy for slab presets; voxel phantoms keep
+  // theirs on the device, matOwner) and a density per material
   std::shared_ptr<const std::vector<float>> binDensity;
   std::shared_ptr<const std::vector<uint8_t>> binMaterial;
   std::shared_ptr<const std::vector<float>> materialDensity;   // 256 entries

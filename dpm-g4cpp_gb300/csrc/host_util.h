@@ -58,6 +58,7 @@ struct JobOut {
   double lbox = 1.0;
   std::shared_ptr<const std::vector<float>> binDensity;
   std::shared_ptr<const std::vector<uint8_t>> binMaterial;
+  std::shared_ptr<uint8_t> matDev;                     // material ids on the device (voxel phantoms)
   std::shared_ptr<const std::vector<float>> materialDensity;
   float BinDensity(long long i) const {
     return binDensity ? (*binDensity)[i] : (*materialDensity)[(*binMaterial)[i]];

@@ -621,6 +621,7 @@ int PrepareOutputs(const dpmx_job* jobs, int njobs, bool tag, cudaStream_t st, s
     o.lbox = ph->lbox;
     o.binDensity = ph->binDensity;
     o.binMaterial = ph->binMaterial;
+    o.matDev = ph->matOwner;
     o.materialDensity = ph->materialDensity;
     // dose and dose^2 come from the scratch pool; every run writes them whole
     void* p = nullptr;
@@ -786,12 +787,18 @@ int dpmx_result_tally(const dpmx_result* r, int job, double* dose, double* dose2
   if (!r || job < 0 || job >= int(r->jobs.size())) return Fail(DPMX_ERR_ARG, "bad job index");
   const JobOut& o = r->jobs[job];
   const size_t n = size_t(o.tallySize) * sizeof(double);
-  if (dose) CK(cudaMemcpy(dose, o.d_dose, n, cudaMemcpyDeviceToHost));
-  if (dose2) CK(cudaMemcpy(dose2, o.d_dose2, n, cudaMemcpyDeviceToHost));
+  // dose and dose^2 on two streams, so that two copy engines move them at once
+  StreamGuard s0, s1;
+  CK(s0.Create());
+  CK(s1.Create());
+  if (dose) CK(cudaMemcpyAsync(dose, o.d_dose, n, cudaMemcpyDeviceToHost, s0.st));
+  if (dose2) CK(cudaMemcpyAsync(dose2, o.d_dose2, n, cudaMemcpyDeviceToHost, s1.st));
   if (steps) {
-    if (o.d_steps) CK(cudaMemcpy(steps, o.d_steps, n, cudaMemcpyDeviceToHost));
+    if (o.d_steps) CK(cudaMemcpyAsync(steps, o.d_steps, n, cudaMemcpyDeviceToHost, s0.st));
     else std::memset(steps, 0, n);
   }
+  CK(cudaStreamSynchronize(s0.st));
+  CK(cudaStreamSynchronize(s1.st));
   return DPMX_OK;
 }
 
@@ -836,8 +843,15 @@ void dpmx_scratch_release(void) { ScratchPool::Instance().Release(-1); }
 int dpmx_result_write(const dpmx_result* r, int job, const char* path, int format) {
   if (!r || !path || job < 0 || job >= int(r->jobs.size())) return Fail(DPMX_ERR_ARG, "bad result, job or path");
   if (format != DPMX_DOSE_RAW && format != DPMX_DOSE_DEPTH) return Fail(DPMX_ERR_ARG, "unknown dose format");
-  const JobOut& o = r->jobs[job];
+  JobOut o = r->jobs[job];
   if (format == DPMX_DOSE_RAW && o.slab) return Fail(DPMX_ERR_ARG, "raw 3-D output needs a voxel phantom");
+  if (!o.binDensity && !o.binMaterial) {
+    // the material ids of a voxel phantom are kept on the device only
+    if (!o.matDev) return Fail(DPMX_ERR_ARG, "the job's phantom has no material ids");
+    auto ids = std::make_shared<std::vector<uint8_t>>(size_t(o.tallySize));
+    CK(cudaMemcpy(ids->data(), o.matDev.get(), ids->size(), cudaMemcpyDeviceToHost));
+    o.binMaterial = ids;
+  }
   const long long n = o.tallySize;
   std::vector<double> d(n), d2(n), st;
   CK(cudaMemcpy(d.data(), o.d_dose, n * sizeof(double), cudaMemcpyDeviceToHost));
