@@ -356,6 +356,18 @@ int dpmx_tables_material_name(const dpmx_tables* t, int imat, char* name, int ca
   return DPMX_OK;
 }
 
+// the material ids of a phantom: a block of the scratch pool (no cudaMalloc or
+// device-wide cudaFree per phantom), shared by the phantom and the results
+// that write its dose; back to the pool when the last of them lets go (every
+// device use of it has completed by then: runs and dose writers synchronise)
+static int NewDeviceIds(dpmx_phantom* p, size_t bytes) {
+  void* q = nullptr;
+  CK(ScratchGet(bytes, &q));
+  p->d_mat = static_cast<uint8_t*>(q);
+  p->matOwner.reset(p->d_mat, [](uint8_t* m) { ScratchPut(m); });
+  return DPMX_OK;
+}
+
 int dpmx_phantom_slab(const dpmx_tables* t, int geom_index, double lbox, dpmx_phantom** out) {
   if (!t || !out || !(lbox > 0.0)) return Fail(DPMX_ERR_ARG, "bad slab phantom arguments");
   if (geom_index < 0) return Fail(DPMX_ERR_ARG, "geometry index must be >= 0");
@@ -377,8 +389,7 @@ int dpmx_phantom_slab(const dpmx_tables* t, int geom_index, double lbox, dpmx_ph
   p->lbox = lbox;
   std::vector<uint8_t> m(nz);
   for (int iz = 0; iz < nz; ++iz) m[iz] = uint8_t(SlabMaterialAt(geom_index, invL, iz));
-  CK(cudaMalloc(&p->d_mat, nz));
-  p->matOwner.reset(p->d_mat, [](uint8_t* q) { cudaFree(q); });
+  if (int rc = NewDeviceIds(p.get(), nz)) return rc;
   CK(cudaMemcpy(p->d_mat, m.data(), nz, cudaMemcpyHostToDevice));
   GridGeom& g = p->grid;
   g.nx = nx; g.ny = nx; g.nz = nz;
@@ -410,8 +421,7 @@ int dpmx_phantom_voxels(const dpmx_tables* t, int nx, int ny, int nz, double vx,
   // the material ids, and after them (16-byte aligned) the slot where the
   // device writes the largest id other than vacuum: checked on the GPU
   const size_t nal = (n + 15) & ~size_t(15);
-  CK(cudaMalloc(&p->d_mat, nal + 16));
-  p->matOwner.reset(p->d_mat, [](uint8_t* q) { cudaFree(q); });
+  if (int rc = NewDeviceIds(p.get(), nal + 16)) return rc;
   CK(cudaMemcpy(p->d_mat, mat, n, cudaMemcpyHostToDevice));
   unsigned* dworst = reinterpret_cast<unsigned*>(p->d_mat + nal);
   CK(cudaMemset(dworst, 0, sizeof(unsigned)));
@@ -459,7 +469,11 @@ int dpmx_phantom_voxels_density(const dpmx_tables* t, int nx, int ny, int nz, do
     (*rho)[i] = r;
     ws = std::max(ws, double(r) / t->h.density[mat[i]]);
   }
-  CK(cudaMalloc(&p->d_rho, n * sizeof(float)));
+  {
+    void* q = nullptr;
+    CK(ScratchGet(n * sizeof(float), &q));
+    p->d_rho = static_cast<float*>(q);
+  }
   CK(cudaMemcpy(p->d_rho, rho->data(), n * sizeof(float), cudaMemcpyHostToDevice));
   p->grid.rho = p->d_rho;
   p->grid.wscale = ws;
@@ -471,7 +485,7 @@ int dpmx_phantom_voxels_density(const dpmx_tables* t, int nx, int ny, int nz, do
 void dpmx_phantom_free(dpmx_phantom* p) {
   if (!p) return;
   p->matOwner.reset();   // the device ids go when no result holds them either
-  cudaFree(p->d_rho);
+  ScratchPut(p->d_rho);
   delete p;
 }
 

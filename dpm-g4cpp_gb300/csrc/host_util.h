@@ -42,6 +42,11 @@ struct JobOut;
 // caller's own use of dpmx_result_tally_device pointers must be complete
 // before the result is freed.
 void ReleaseJobOut(JobOut& o);
+// a device block of the run scratch pool (no cudaMalloc once the pool holds
+// one that fits, and no device-wide synchronisation when it goes back): for
+// buffers whose last device use has completed when ScratchPut is called
+cudaError_t ScratchGet(size_t bytes, void** out);
+void ScratchPut(void* p);
 
 struct JobOut {
   long long tallySize = 0;

@@ -738,6 +738,10 @@ void ReleaseJobOut(JobOut& o) {
     if (p) ScratchPool::Instance().Put(p);
   o.d_dose = o.d_dose2 = o.d_steps = o.d_btally = nullptr;
 }
+cudaError_t ScratchGet(size_t bytes, void** out) { return ScratchPool::Instance().Get(bytes, out); }
+void ScratchPut(void* p) {
+  if (p) ScratchPool::Instance().Put(p);
+}
 }  // namespace dpmx
 
 // ===========================================================================
