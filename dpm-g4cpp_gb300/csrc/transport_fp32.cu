@@ -1004,9 +1004,10 @@ __global__ void __launch_bounds__(256) ElectronPhase(PhaseArgs a) {
 // cell, so a cell never lags its newest reservation by more laps than the
 // block has warps (at most 32), and 6 bits tell the laps apart.
 // ---------------------------------------------------------------------------
-constexpr int kSlots = 416;   // 3 blocks leave the SM 164 KB of shared memory and the rest to L1
+constexpr int kSlots = 448;   // 3 blocks (~157 KB) fit the 164 KB shared-memory carve-out; the rest is L1
 constexpr int kBlockMinBlocks = 3;      // resident blocks per SM the kernel is compiled for
 constexpr int kBlockThreads = 320;      // threads per block (a multiple of 32): 64 registers, 30 warps per SM
+constexpr int kSecondStepLanes = 20;    // lanes that must go on for a second sub-step in the same turn
 constexpr bool kTablesInSmem = false;  // electron tables staged per block, else read through L1
 constexpr uint32_t kFHinge = 4u, kFPositron = 16u;
 constexpr int8_t kMatUnknown = -2;   // the slot's voxel changed since its material was read
@@ -1631,10 +1632,14 @@ __global__ void __launch_bounds__(kBlockThreads, kBlockMinBlocks) ElectronPhaseB
       default:
         break;
     }
-    // a slot that keeps stepping takes up to K sub-steps before it goes back
-    // to a ring (one call site; lanes whose slot had an event wait)
+    // a slot that keeps stepping takes a second sub-step before it goes back
+    // to a ring when at least kSecondStepLanes lanes of the warp do (one call
+    // site; lanes whose slot had an event wait). With fewer, they go back to
+    // the step ring and join a fuller warp.
     int code = live ? 0 : 5;
-    for (int rep = 0; rep < 2 && __any_sync(kFull, code == 0); ++rep)
+    for (int rep = 0; rep < 2 && (rep == 0 ? __any_sync(kFull, code == 0)
+                                           : __popc(__ballot_sync(kFull, code == 0)) >= kSecondStepLanes);
+         ++rep)
       if (code == 0) code = StepSlot<AGG>(a, et, jobs, S, k, esc, nsteps, dacc);
     // the ring of the slot's next action; a finished slot goes back to the
     // idle ring while there is work left, else it retires (q == kRings)
