@@ -57,7 +57,8 @@ class _Opts(C.Structure):
     _fields_ = [("precision", C.c_int), ("batches", C.c_int), ("block_size", C.c_int), ("blocks_per_sm", C.c_int),
                 ("chunk_histories", C.c_longlong), ("tally_aggregate", C.c_int), ("use_graph", C.c_int),
                 ("tag_beamlets", C.c_int), ("autotune", C.c_int), ("profile_phases", C.c_int),
-                ("electron_kernel", C.c_int), ("photon_kernel", C.c_int), ("stream", C.c_void_p)]
+                ("electron_kernel", C.c_int), ("photon_kernel", C.c_int), ("stream", C.c_void_p),
+                ("electron_slots", C.c_int)]
 
 
 class _Stats(C.Structure):
@@ -381,7 +382,7 @@ class Result:
         a = (C.c_longlong * 4)()
         _check(library().dpmx_result_config(self._h, a))
         return dict(block_size=a[0], blocks_per_sm=a[1], chunk_histories=a[2], tally_aggregate=a[3] & 1,
-                    electron_kernel=(a[3] >> 1) & 1, photon_kernel=(a[3] >> 2) & 1)
+                    electron_kernel=(a[3] >> 1) & 1, photon_kernel=(a[3] >> 2) & 1, electron_slots=a[3] >> 3)
 
     @property
     def profile(self):
@@ -470,7 +471,7 @@ def scratch_release():
 
 def run(tables, jobs, precision=FP32_EVENT, batches=10, block_size=0, blocks_per_sm=0, chunk_histories=0,
         tally_aggregate=-1, use_graph=True, tag_beamlets=False, autotune=False, profile_phases=False,
-        electron_kernel=-1, photon_kernel=-1, stream=None):
+        electron_kernel=-1, photon_kernel=-1, stream=None, electron_slots=0):
     """Runs the jobs (one run, one stream) and returns a Result."""
     L = library()
     arr = (_Job * len(jobs))()
@@ -492,6 +493,7 @@ def run(tables, jobs, precision=FP32_EVENT, batches=10, block_size=0, blocks_per
     o.electron_kernel = electron_kernel
     o.photon_kernel = photon_kernel
     o.stream = stream
+    o.electron_slots = electron_slots
     h = C.c_void_p()
     rc = L.dpmx_run(tables.handle, arr, len(jobs), C.byref(o), C.byref(h))
     if rc != OK:

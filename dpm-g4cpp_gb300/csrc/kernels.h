@@ -158,11 +158,14 @@ cudaError_t LaunchTableEval32(const DevTables<float>& T, int q, int imat, const 
 cudaError_t LaunchRingSelfTest(int blocks, int nslots, int rounds, uint32_t seed, long long probeCycles,
                                unsigned long long* out, cudaStream_t st);
 int ElectronPhaseSmemBytes(const DevTables<float>& T);
-// block-batched electron phase (256 threads per block, shared-memory slots)
+// block-batched electron phase (320 threads per block, shared-memory slots)
 int BlockPhaseSmemBytes(const DevTables<float>& T);
 int BlockPhaseBlocksPerSM();
+// the slots per block a run gets for a requested count (0: the default; the
+// instantiated sizes are 448 and 384)
+int BlockPhaseSlots(int requested);
 cudaError_t PrepareBlockPhase(const DevTables<float>& T);
-cudaError_t LaunchElectronPhaseBlock(const PhaseArgs& a, int blocks, cudaStream_t st);
+cudaError_t LaunchElectronPhaseBlock(const PhaseArgs& a, int blocks, int slots, cudaStream_t st);
 
 // ---- influence matrix (influence.cu) ----
 cudaError_t LaunchCountNnz(const double* dense, long long nvox, int nb, double thr, long long* rowCount,

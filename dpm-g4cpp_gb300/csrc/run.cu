@@ -48,6 +48,7 @@ struct Cfg {
   int aggregate = 0;
   int eblock = 1;          // electron phase: 0 lane-refill kernel, 1 block-batched kernel
   int pblock = 1;          // photon phase: 0 one photon per lane, 1 block-batched kernel
+  int eslots = 0;          // electron slots per block of the block-batched kernel (0: default)
 };
 
 // Device scratch kept across runs. A run of the FP32 form needs GBs of queues,
@@ -373,7 +374,7 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
             CK(cudaEventCreate(&evE.back()));
             CK(cudaEventRecord(evE[evE.size() - 2], s));
           }
-          if (cfg.eblock) CK(LaunchElectronPhaseBlock(a, eblocks, s));
+          if (cfg.eblock) CK(LaunchElectronPhaseBlock(a, eblocks, cfg.eslots, s));
           else CK(LaunchElectronPhase(a, blocks, cfg.threads, s));
           if (profile) CK(cudaEventRecord(evE.back(), s));
           ++nl;
@@ -687,6 +688,8 @@ Cfg DefaultCfg(const dpmx_run_options* o, long long totalHist) {
   if (o && o->tally_aggregate >= 0) c.aggregate = o->tally_aggregate;
   if (o && o->electron_kernel >= 0) c.eblock = o->electron_kernel;
   if (o && o->photon_kernel >= 0) c.pblock = o->photon_kernel;
+  if (o && o->electron_slots > 0) c.eslots = o->electron_slots;
+  c.eslots = BlockPhaseSlots(c.eslots);
   return c;
 }
 
@@ -697,14 +700,17 @@ int Autotune(const dpmx_tables* t, const dpmx_job* jobs, int njobs, const Cfg ba
   const long long sample = std::min<long long>(total, 1 << 18);
   std::vector<dpmx_job> sj(jobs, jobs + njobs);
   for (auto& j : sj) j.histories = std::max<long long>(1, (long long)(double(j.histories) * sample / std::max(1LL, total)));
-  // threads and blocks per SM of the lane kernels, tally aggregation and the
-  // electron kernel; the photon kernel stays the run's (the two photon
-  // kernels round some FP32 results differently)
-  struct Cand { int threads, bps, agg, eblock, pblock; };
+  // threads and blocks per SM of the lane kernels, tally aggregation, the
+  // electron kernel and the block kernel's slots per block (its queue
+  // depth); the photon kernel stays the run's (the two photon kernels round
+  // some FP32 results differently)
+  struct Cand { int threads, bps, agg, eblock, pblock, eslots; };
   // (threads and blocks per SM shape the lane kernels, compiled for at most
-  // 256 threads per block; the block-batched kernels have fixed shapes)
-  const Cand cands[] = {{256, 3, 0, 0, -1}, {256, 3, 1, 0, -1}, {256, 2, 0, 0, -1}, {128, 6, 0, 0, -1},
-                        {256, 3, 0, 1, -1}, {256, 3, 1, 1, -1}, {256, 2, 0, 1, -1}};
+  // 256 threads per block; the block-batched kernels have fixed block shapes)
+  const int sDef = BlockPhaseSlots(0), sSmall = 384;
+  const Cand cands[] = {{256, 3, 0, 0, -1, sDef},   {256, 3, 1, 0, -1, sDef},   {256, 2, 0, 0, -1, sDef},
+                        {128, 6, 0, 0, -1, sDef},   {256, 3, 0, 1, -1, sDef},   {256, 3, 1, 1, -1, sDef},
+                        {256, 3, 0, 1, -1, sSmall}, {256, 3, 1, 1, -1, sSmall}};
   double bestMs = 1e30;
   *best = base;
   for (const Cand& c : cands) {
@@ -713,6 +719,7 @@ int Autotune(const dpmx_tables* t, const dpmx_job* jobs, int njobs, const Cfg ba
     cfg.blocksPerSM = c.bps;
     cfg.aggregate = c.agg;
     cfg.eblock = c.eblock;
+    cfg.eslots = BlockPhaseSlots(c.eslots);
     if (c.pblock >= 0) cfg.pblock = c.pblock;
     cfg.chunk = sample;
     std::vector<JobOut> outs;
@@ -778,7 +785,7 @@ int dpmx_run(const dpmx_tables* t, const dpmx_job* jobs, int njobs, const dpmx_r
         rc = RunFp32(t, jobs, njobs, o.batches, cfg, tag, o.use_graph != 0 && !o.profile_phases, st, r->jobs, &r->ms,
                      &r->launches, o.profile_phases ? r->prof : nullptr);
       r->cfg[0] = cfg.threads; r->cfg[1] = cfg.blocksPerSM; r->cfg[2] = cfg.chunk;
-      r->cfg[3] = cfg.aggregate | (cfg.eblock << 1) | (cfg.pblock << 2);
+      r->cfg[3] = cfg.aggregate | (cfg.eblock << 1) | (cfg.pblock << 2) | ((long long)cfg.eslots << 3);
     }
   }
   if (ownStream) cudaStreamDestroy(st);
@@ -791,18 +798,18 @@ int dpmx_result_tally(const dpmx_result* r, int job, double* dose, double* dose2
   if (!r || job < 0 || job >= int(r->jobs.size())) return Fail(DPMX_ERR_ARG, "bad job index");
   const JobOut& o = r->jobs[job];
   const size_t n = size_t(o.tallySize) * sizeof(double);
-  // dose and dose^2 on two streams, so that two copy engines move them at once
-  StreamGuard s0, s1;
+  // on a stream of this call (no wait on other streams); into pinned memory
+  // the copies run at the host link's rate (GB300: ~190 GB/s device to host,
+  // the same for one or two streams and for a kernel storing to mapped memory)
+  StreamGuard s0;
   CK(s0.Create());
-  CK(s1.Create());
   if (dose) CK(cudaMemcpyAsync(dose, o.d_dose, n, cudaMemcpyDeviceToHost, s0.st));
-  if (dose2) CK(cudaMemcpyAsync(dose2, o.d_dose2, n, cudaMemcpyDeviceToHost, s1.st));
+  if (dose2) CK(cudaMemcpyAsync(dose2, o.d_dose2, n, cudaMemcpyDeviceToHost, s0.st));
   if (steps) {
     if (o.d_steps) CK(cudaMemcpyAsync(steps, o.d_steps, n, cudaMemcpyDeviceToHost, s0.st));
     else std::memset(steps, 0, n);
   }
   CK(cudaStreamSynchronize(s0.st));
-  CK(cudaStreamSynchronize(s1.st));
   return DPMX_OK;
 }
 

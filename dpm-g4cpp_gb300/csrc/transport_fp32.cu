@@ -42,7 +42,6 @@ namespace {
 
 constexpr float kEMC2f = 0.510991f;
 constexpr float kPIf = 3.1415926535897932f;
-constexpr float kTolF = 1.0e-4f;
 constexpr float kHalfTolF = 0.5e-4f;
 constexpr unsigned kFull = 0xffffffffu;
 constexpr unsigned kMaxPhotonSteps = 1u << 22;     // per particle: a lane never loops without bound
@@ -1004,7 +1003,12 @@ __global__ void __launch_bounds__(256) ElectronPhase(PhaseArgs a) {
 // cell, so a cell never lags its newest reservation by more laps than the
 // block has warps (at most 32), and 6 bits tell the laps apart.
 // ---------------------------------------------------------------------------
-constexpr int kSlots = 448;   // 3 blocks (~157 KB) fit the 164 KB shared-memory carve-out; the rest is L1
+// Slots per block: a compile-time size of the shared-memory state, instantiated
+// for kSlots (the default: 3 blocks, ~157 KB, fit the 164 KB shared-memory
+// carve-out and leave the rest to L1) and kSlotsSmall (more L1), and chosen per
+// run (dpmx_run_options::electron_slots, tried by the autotuner)
+constexpr int kSlots = 448;
+constexpr int kSlotsSmall = 384;
 constexpr int kBlockMinBlocks = 3;      // resident blocks per SM the kernel is compiled for
 constexpr int kBlockThreads = 320;      // threads per block (a multiple of 32): 64 registers, 30 warps per SM
 constexpr int kSecondStepLanes = 20;    // lanes that must go on for a second sub-step in the same turn
@@ -1012,17 +1016,19 @@ constexpr bool kTablesInSmem = false;  // electron tables staged per block, else
 constexpr uint32_t kFHinge = 4u, kFPositron = 16u;
 constexpr int8_t kMatUnknown = -2;   // the slot's voxel changed since its material was read
 
-// shared-memory state of the resident electrons, in 16-byte records that a
+// shared-memory state of the NS resident electrons, in 16-byte records that a
 // lane reads or writes with one 128-bit access
-struct SlotArrays {
-  float4 pos[kSlots];   // offset in the voxel lx, ly, lz; kinetic energy
-  float4 dir[kSlots];   // direction dx, dy, dz; voxel (PackVox, as float bits)
-  float4 mfp[kSlots];   // nTr1, nMol, invMol, nBrem
-  uint4 id[kSlots];     // flags (hinge, positron; sub-job << 8), history, energy-check slot, sub-steps
-  uint4 rs[kSlots];     // random stream uid lo, uid hi, counter; ekin0 (float bits)
-  float nTr10[kSlots];
-  double acc[kSlots];
-  int8_t mat[kSlots];   // material of the slot's current voxel (-1: vacuum)
+template <int NS>
+struct SlotArraysT {
+  static constexpr int kCount = NS;
+  float4 pos[NS];   // offset in the voxel lx, ly, lz; kinetic energy
+  float4 dir[NS];   // direction dx, dy, dz; voxel (PackVox, as float bits)
+  float4 mfp[NS];   // nTr1, nMol, invMol, nBrem
+  uint4 id[NS];     // flags (hinge, positron; sub-job << 8), history, energy-check slot, sub-steps
+  uint4 rs[NS];     // random stream uid lo, uid hi, counter; ekin0 (float bits)
+  float nTr10[NS];
+  double acc[NS];
+  int8_t mat[NS];   // material of the slot's current voxel (-1: vacuum)
 };
 constexpr long long kWaitCycles = 4LL << 30;   // bound of one wait (~2 s): then the warp gives up
 constexpr int kRingBits = 9;
@@ -1180,20 +1186,22 @@ __device__ __forceinline__ void RingPut(Rings<NR>& R, int lane, int q, int k, bo
 
 // electron rings (of equally full rings the first is taken)
 enum : int { kRBrem, kRMoller, kRHinge, kRMscEnd, kRIdle, kRStep, kRings };
-static_assert(kSlots <= kRingSize, "a ring holds every slot");
+static_assert(kSlots <= kRingSize && kSlotsSmall <= kRingSize, "a ring holds every slot");
 // ring of a sub-step's result code (0 step, 1 brem, 2 Moller, 3 hinge, 4 MSC
 // step end, 5 finished), four bits per code
 constexpr uint32_t kRingOfCode = 0x432105u;
 using SlotRings = Rings<kRings>;
 
+template <int NS>
 __host__ __device__ constexpr size_t BlockPhaseStaticBytes() {
-  return (sizeof(SlotArrays) + sizeof(SlotRings) + 15) & ~size_t(15);   // staged tables start 16-byte aligned
+  return (sizeof(SlotArraysT<NS>) + sizeof(SlotRings) + 15) & ~size_t(15);   // staged tables start 16-byte aligned
 }
 
 // dynamic shared memory of the block kernel: slots, rings, the electron tables
 // when staged, then the depth tally of `depthBins` bins
+template <int NS>
 __host__ __device__ inline size_t BlockPhaseSmemBytesFor(const DevTables<float>& T, int depthBins) {
-  const size_t b = BlockPhaseStaticBytes() + (kTablesInSmem ? size_t(T.elecCount) * sizeof(float) : 0);
+  const size_t b = BlockPhaseStaticBytes<NS>() + (kTablesInSmem ? size_t(T.elecCount) * sizeof(float) : 0);
   return ((b + 15) & ~size_t(15)) + DepthAccBytes(depthBins);
 }
 
@@ -1201,7 +1209,8 @@ __device__ __forceinline__ void UnpackVox(uint32_t v, PState& p) {
   p.ix = int(v & 0x7ffu); p.iy = int((v >> 11) & 0x7ffu); p.iz = int(v >> 22);
 }
 
-__device__ __forceinline__ void LoadSlot(const SlotArrays& S, int k, PState& p, EState& s, uint32_t& fl) {
+template <class SA>
+__device__ __forceinline__ void LoadSlot(const SA& S, int k, PState& p, EState& s, uint32_t& fl) {
   const float4 a = S.pos[k], b = S.dir[k], c = S.mfp[k];
   const uint4 d = S.id[k], r = S.rs[k];
   p.lx = a.x; p.ly = a.y; p.lz = a.z; p.e = a.w;
@@ -1217,7 +1226,8 @@ __device__ __forceinline__ void LoadSlot(const SlotArrays& S, int k, PState& p, 
 }
 
 // a new particle in slot k, its random stream at counter ctr
-__device__ __forceinline__ void StoreSlot(SlotArrays& S, int k, const PState& p, const EState& s, uint32_t ctr) {
+template <class SA>
+__device__ __forceinline__ void StoreSlot(SA& S, int k, const PState& p, const EState& s, uint32_t ctr) {
   S.pos[k] = make_float4(p.lx, p.ly, p.lz, p.e);
   S.dir[k] = make_float4(p.dx, p.dy, p.dz, __uint_as_float(PackVox(p.ix, p.iy, p.iz)));
   S.mfp[k] = make_float4(s.nTr1, s.nMol, s.invMol, s.nBrem);
@@ -1230,7 +1240,8 @@ __device__ __forceinline__ void StoreSlot(SlotArrays& S, int k, const PState& p,
 // the part of slot k a plain sub-step reads (the random stream, the MSC hinge
 // state and nTr10 stay as they are; pst: sub-steps taken), and the part it
 // writes back
-__device__ __forceinline__ void LoadStepState(const SlotArrays& S, int k, PState& p, EState& s, uint32_t& fl,
+template <class SA>
+__device__ __forceinline__ void LoadStepState(const SA& S, int k, PState& p, EState& s, uint32_t& fl,
                                               uint32_t& pst) {
   const float4 a = S.pos[k], b = S.dir[k], c = S.mfp[k];
   const uint4 d = S.id[k];
@@ -1243,14 +1254,16 @@ __device__ __forceinline__ void LoadStepState(const SlotArrays& S, int k, PState
   s.hinge = (fl & kFHinge) != 0;
 }
 
-__device__ __forceinline__ void StoreStepState(SlotArrays& S, int k, const PState& p, const EState& s) {
+template <class SA>
+__device__ __forceinline__ void StoreStepState(SA& S, int k, const PState& p, const EState& s) {
   S.pos[k] = make_float4(p.lx, p.ly, p.lz, p.e);
   S.dir[k].w = __uint_as_float(PackVox(p.ix, p.iy, p.iz));
   S.mfp[k] = make_float4(s.nTr1, s.nMol, s.invMol, s.nBrem);
 }
 
 // random stream of slot k (a fresh Philox block per use; the counter advances)
-__device__ __forceinline__ void SlotRng(const SlotArrays& S, int k, const JobF& J, uint32_t hist, PRng& r) {
+template <class SA>
+__device__ __forceinline__ void SlotRng(const SA& S, int k, const JobF& J, uint32_t hist, PRng& r) {
   const uint4 q = S.rs[k];
   r.Init(J.k0, J.k1, hist, q.x, q.y);
   r.ctr = q.z;
@@ -1281,8 +1294,8 @@ __device__ __forceinline__ void AnnihilateF(const PhaseArgs& a, const PState& p,
 // a voxel face only moves onto it, and the next one settles. One deposit at
 // most is scored, and one escape counted, per sub-step, at one place in the
 // code each (fewer inlined copies: the kernel is instruction-fetch bound).
-template <int AGG>
-__device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, const JobF* jobs, SlotArrays& S,
+template <int AGG, class SA>
+__device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, const JobF* jobs, SA& S,
                                         int k, EscTally& esc, unsigned long long& nsteps, const DepthAcc& dacc) {
   const DevTables<float>& T = a.T;
   PState p;
@@ -1417,7 +1430,8 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
 }
 
 // GS angular deflection at the MSC hinge (SimDPMLike.cc:216-226, :731-750)
-__device__ __forceinline__ void EventHinge(const PhaseArgs& a, const JobF* jobs, SlotArrays& S, int k) {
+template <class SA>
+__device__ __forceinline__ void EventHinge(const PhaseArgs& a, const JobF* jobs, SA& S, int k) {
   PState p;
   EState s;
   uint32_t fl;
@@ -1440,7 +1454,8 @@ __device__ __forceinline__ void EventHinge(const PhaseArgs& a, const JobF* jobs,
 }
 
 // end of an MSC step: new scattering strength and hinge (SimDPMLike.cc:227-237)
-__device__ __forceinline__ void EventMscEnd(const PhaseArgs& a, const ETables& et, const JobF* jobs, SlotArrays& S,
+template <class SA>
+__device__ __forceinline__ void EventMscEnd(const PhaseArgs& a, const ETables& et, const JobF* jobs, SA& S,
                                             int k) {
   const uint4 d = S.id[k], q = S.rs[k];
   const uint32_t fl = d.x;
@@ -1459,8 +1474,8 @@ __device__ __forceinline__ void EventMscEnd(const PhaseArgs& a, const ETables& e
 
 // bremsstrahlung (SimDPMLike.cc:172-194, :661-695); false when the electron
 // fell below the tracking cut and finished
-template <int AGG>
-__device__ __forceinline__ bool EventBrem(const PhaseArgs& a, const JobF* jobs, SlotArrays& S, int k,
+template <int AGG, class SA>
+__device__ __forceinline__ bool EventBrem(const PhaseArgs& a, const JobF* jobs, SA& S, int k,
                                          const DepthAcc& dacc) {
   PState p;
   EState s;
@@ -1505,7 +1520,8 @@ __device__ __forceinline__ bool EventBrem(const PhaseArgs& a, const JobF* jobs, 
 }
 
 // Moller delta electron (SimDPMLike.cc:204-214, :699-728)
-__device__ __forceinline__ void EventMoller(const PhaseArgs& a, const ETables& et, const JobF* jobs, SlotArrays& S,
+template <class SA>
+__device__ __forceinline__ void EventMoller(const PhaseArgs& a, const ETables& et, const JobF* jobs, SA& S,
                                             int k) {
   PState p;
   EState s;
@@ -1541,8 +1557,9 @@ __device__ __forceinline__ void EventMoller(const PhaseArgs& a, const ETables& e
 
 // first sub-step state of a claimed work item (a primary or a queued
 // electron) in slot k; false when it starts outside the phantom
+template <class SA>
 __device__ __forceinline__ bool RefillSlot(const PhaseArgs& a, const ETables& et, const JobF* jobs,
-                                           const unsigned long long* spre, SlotArrays& S, int k,
+                                           const unsigned long long* spre, SA& S, int k,
                                            unsigned long long item, EscTally& esc) {
   PState p;
   PRng rng;
@@ -1570,19 +1587,20 @@ __device__ __forceinline__ bool RefillSlot(const PhaseArgs& a, const ETables& et
   return true;
 }
 
-template <int AGG>
+template <int AGG, int NS>
 __global__ void __launch_bounds__(kBlockThreads, kBlockMinBlocks) ElectronPhaseB(PhaseArgs a) {
+  using SlotArrays = SlotArraysT<NS>;
   extern __shared__ __align__(16) unsigned char dyn[];
   SlotArrays& S = *reinterpret_cast<SlotArrays*>(dyn);
   SlotRings& R = *reinterpret_cast<SlotRings*>(dyn + sizeof(SlotArrays));
-  float* sdata = reinterpret_cast<float*>(dyn + BlockPhaseStaticBytes());
+  float* sdata = reinterpret_cast<float*>(dyn + BlockPhaseStaticBytes<NS>());
   __shared__ ETables et;
   __shared__ JobF sjobs[16];
   __shared__ unsigned long long spre[kStripes + 1];
   const bool fewJobs = a.njobs <= 16;
   if (fewJobs)
     for (int j = threadIdx.x; j < a.njobs; j += blockDim.x) sjobs[j] = a.jobs[j];
-  const DepthAcc dacc = DepthAccInit(a, dyn + BlockPhaseSmemBytesFor(a.T, 0));
+  const DepthAcc dacc = DepthAccInit(a, dyn + BlockPhaseSmemBytesFor<NS>(a.T, 0));
   const unsigned long long nQ = StripePrefix(a.inCount, spre);
   const JobF* jobs = fewJobs ? sjobs : a.jobs;
   const unsigned long long total = (unsigned long long)a.nPrimaries + nQ;
@@ -1590,8 +1608,8 @@ __global__ void __launch_bounds__(kBlockThreads, kBlockMinBlocks) ElectronPhaseB
   if (kTablesInSmem) StageElectronTables(a.T, sdata, &et);
   else if (threadIdx.x == 0) BindElectronTables(a.T, &et);   // visible after the barrier below
   const int tid = threadIdx.x, lane = tid & 31;
-  RingsInit(R, kRIdle, kSlots);
-  for (int k = tid; k < kSlots; k += blockDim.x) S.id[k] = make_uint4(0u, 0u, 0u, 0u);
+  RingsInit(R, kRIdle, NS);
+  for (int k = tid; k < NS; k += blockDim.x) S.id[k] = make_uint4(0u, 0u, 0u, 0u);
   __syncthreads();
   volatile int* vexh = &R.exhausted;
   EscTally esc;
@@ -2178,21 +2196,35 @@ cudaError_t LaunchPhotonPhase(const PhaseArgs& a, int blocks, int threads, cudaS
   return cudaGetLastError();
 }
 
-int BlockPhaseSmemBytes(const DevTables<float>& T) { return int(BlockPhaseSmemBytesFor(T, kDepthBins)); }
+int BlockPhaseSmemBytes(const DevTables<float>& T) { return int(BlockPhaseSmemBytesFor<kSlots>(T, kDepthBins)); }
 
 int BlockPhaseBlocksPerSM() { return kBlockMinBlocks; }
 
-cudaError_t PrepareBlockPhase(const DevTables<float>& T) {
-  const int smem = BlockPhaseSmemBytes(T);
-  cudaError_t e = cudaFuncSetAttribute(ElectronPhaseB<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+int BlockPhaseSlots(int requested) { return requested == kSlotsSmall ? kSlotsSmall : kSlots; }
+
+template <int NS>
+static cudaError_t PrepareBlockPhaseFor(const DevTables<float>& T) {
+  const int smem = int(BlockPhaseSmemBytesFor<NS>(T, kDepthBins));
+  cudaError_t e = cudaFuncSetAttribute(ElectronPhaseB<0, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(ElectronPhaseB<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  return cudaFuncSetAttribute(ElectronPhaseB<1, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
 }
 
-cudaError_t LaunchElectronPhaseBlock(const PhaseArgs& a, int blocks, cudaStream_t st) {
-  const size_t smem = BlockPhaseSmemBytesFor(a.T, a.depthBins);
-  if (a.aggregate) ElectronPhaseB<1><<<blocks, kBlockThreads, smem, st>>>(a);
-  else ElectronPhaseB<0><<<blocks, kBlockThreads, smem, st>>>(a);
+cudaError_t PrepareBlockPhase(const DevTables<float>& T) {
+  const cudaError_t e = PrepareBlockPhaseFor<kSlots>(T);
+  return e != cudaSuccess ? e : PrepareBlockPhaseFor<kSlotsSmall>(T);
+}
+
+template <int NS>
+static void LaunchElectronPhaseBlockFor(const PhaseArgs& a, int blocks, cudaStream_t st) {
+  const size_t smem = BlockPhaseSmemBytesFor<NS>(a.T, a.depthBins);
+  if (a.aggregate) ElectronPhaseB<1, NS><<<blocks, kBlockThreads, smem, st>>>(a);
+  else ElectronPhaseB<0, NS><<<blocks, kBlockThreads, smem, st>>>(a);
+}
+
+cudaError_t LaunchElectronPhaseBlock(const PhaseArgs& a, int blocks, int slots, cudaStream_t st) {
+  if (BlockPhaseSlots(slots) == kSlotsSmall) LaunchElectronPhaseBlockFor<kSlotsSmall>(a, blocks, st);
+  else LaunchElectronPhaseBlockFor<kSlots>(a, blocks, st);
   return cudaGetLastError();
 }
 

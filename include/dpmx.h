@@ -117,15 +117,19 @@ typedef struct {
   int tally_aggregate;       /* FP32: -1 default, 0 plain atomics, 1 warp-aggregated */
   int use_graph;             /* FP32: capture each batch in a CUDA graph (default 1) */
   int tag_beamlets;          /* FP32: also tally dose per beamlet (influence matrix) */
-  int autotune;              /* 1: tune block size / chunk / aggregation on a sample */
+  int autotune;              /* 1: time the candidate kernel shapes (electron kernel, block
+                                size, tally aggregation, electron slots per block) on a
+                                sample of the jobs and run the fastest */
   int profile_phases;        /* FP32: time every phase launch (no graph); see dpmx_result_profile */
   int electron_kernel;       /* FP32 electron phase: -1 default, 0 one electron per lane with
-                                refill, 1 block-batched (shared-memory slots, interactions
-                                processed over compacted per-type lists) */
+                                refill, 1 block-batched (shared-memory slots on rings by their
+                                next interaction, one interaction kind per warp) */
   int photon_kernel;         /* FP32 photon phase: -1 default, 0 one photon per lane, 1
-                                block-batched (Compton and pair over compacted lists); both
-                                draw the same random numbers per photon */
+                                block-batched (shared-memory slots on rings by their next
+                                interaction); both draw the same random numbers per photon */
   void* stream;              /* cudaStream_t to run on, NULL = library stream */
+  int electron_slots;        /* FP32 block-batched electron phase: electrons resident per block
+                                (its ring depth): 0 default (448), or 384 */
 } dpmx_run_options;
 
 void dpmx_run_options_default(dpmx_run_options* o);
@@ -154,7 +158,7 @@ int dpmx_result_stats(const dpmx_result* r, int job, dpmx_job_stats* s);
 double dpmx_result_elapsed_ms(const dpmx_result* r);
 long long dpmx_result_launches(const dpmx_result* r);
 /* chosen launch configuration: [block_size, blocks_per_sm, chunk_histories,
- * tally_aggregate + 2 * electron_kernel + 4 * photon_kernel] */
+ * tally_aggregate + 2 * electron_kernel + 4 * photon_kernel + 8 * electron_slots] */
 int dpmx_result_config(const dpmx_result* r, long long* cfg4);
 /* phase profile of a run with profile_phases = 1 (zeros otherwise), 10 values:
  * electron-phase ms, photon-phase ms, electron-phase launches, photon-phase

@@ -57,8 +57,11 @@ def test_schedule_invariance(tables_wlb, dpm):
     jobs, keep = small_jobs(dpm, tables_wlb, n=3)
     base = tallies(dpm.run(tables_wlb, jobs, batches=2), 3)
     for kw in (dict(use_graph=False), dict(chunk_histories=3000), dict(block_size=128, blocks_per_sm=4),
-               dict(tally_aggregate=1)):
-        assert_same(tallies(dpm.run(tables_wlb, jobs, batches=2, **kw), 3), base)
+               dict(tally_aggregate=1), dict(electron_slots=384)):
+        r = dpm.run(tables_wlb, jobs, batches=2, **kw)
+        if "electron_slots" in kw:
+            assert r.config["electron_slots"] == 384
+        assert_same(tallies(r, 3), base)
 
 
 def test_autotuned_run_equals_its_configuration(tables_wlb, dpm):
@@ -69,7 +72,9 @@ def test_autotuned_run_equals_its_configuration(tables_wlb, dpm):
     c = tuned.config
     again = dpm.run(tables_wlb, jobs, batches=2, block_size=c["block_size"], blocks_per_sm=c["blocks_per_sm"],
                     tally_aggregate=c["tally_aggregate"], electron_kernel=c["electron_kernel"],
-                    photon_kernel=c["photon_kernel"], chunk_histories=c["chunk_histories"])
+                    photon_kernel=c["photon_kernel"], chunk_histories=c["chunk_histories"],
+                    electron_slots=c["electron_slots"])
+    assert c["electron_slots"] in (384, 448)
     assert_same(tallies(tuned, 3), tallies(again, 3))
     for j in range(3):
         assert tuned.stats(j).lost == 0 and tuned.stats(j).residual_violations == 0
