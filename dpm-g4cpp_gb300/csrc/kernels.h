@@ -125,6 +125,9 @@ struct PhaseArgs {
   int aggregate;               // warp-aggregated tally atomics
   int depthBins;               // > 0: depth tallies summed per block in shared memory first
   int depthStride;             //      (bins per job; job j at j * depthStride)
+  int plainTally;              // 1: every job scores a 3-D voxel tally only (depthBins 0, no
+                               //    tallyDepth, step counts or beamlet tally): the block kernels
+                               //    built for that form run
 };
 
 // shared-memory depth tally of a block (slab jobs): bins of all jobs of a run

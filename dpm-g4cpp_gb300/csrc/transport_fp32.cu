@@ -255,6 +255,21 @@ struct DepthAcc {
   int sliceStride = 0;   // bins between the batch slices of a job
 };
 
+// adds de to bin idx of batch slice `slice` of the job's tally. Bins and
+// slices of a run stay below 2^32 doubles (checked when the run is planned):
+// 32-bit index arithmetic, one widening for the address
+__device__ __forceinline__ void ScoreBin(const JobF& J, uint32_t slice, uint32_t idx, double de, int agg) {
+  double* ptr = J.tally + (slice * uint32_t(J.sstride) + idx * uint32_t(J.tstride));
+  if (agg) {
+    cg::coalesced_group g = cg::coalesced_threads();
+    cg::coalesced_group peers = cg::labeled_partition(g, (unsigned long long)ptr);
+    const double sum = cg::reduce(peers, de, cg::plus<double>());
+    if (peers.thread_rank() == 0) atomicAdd(ptr, sum);
+  } else {
+    atomicAdd(ptr, de);
+  }
+}
+
 // deposit e of a particle (meta: its type and sub-job) in voxel (ix, iy, iz)
 __device__ __forceinline__ void Score(const JobF& J, uint32_t meta, int ix, int iy, int iz, uint32_t hist, float e,
                                       int agg, const DepthAcc& d = DepthAcc()) {
@@ -266,22 +281,29 @@ __device__ __forceinline__ void Score(const JobF& J, uint32_t meta, int ix, int 
     atomicAdd(d.n + b, 1u);
     return;
   }
-  // bins and slices of a run stay below 2^32 doubles (checked when the run is
-  // planned): 32-bit index arithmetic, one widening for the address
   const uint32_t idx = J.tallyDepth ? uint32_t(iz) : (uint32_t(iz) * uint32_t(J.ny) + uint32_t(iy)) * uint32_t(J.nx) + uint32_t(ix);
-  double* ptr = J.tally + (slice * uint32_t(J.sstride) + idx * uint32_t(J.tstride));
-  if (agg) {
-    cg::coalesced_group g = cg::coalesced_threads();
-    cg::coalesced_group peers = cg::labeled_partition(g, (unsigned long long)ptr);
-    const double sum = cg::reduce(peers, de, cg::plus<double>());
-    if (peers.thread_rank() == 0) atomicAdd(ptr, sum);
-  } else {
-    atomicAdd(ptr, de);
-  }
+  ScoreBin(J, slice, idx, de, agg);
   if (J.steps) atomicAdd(J.steps + iz, 1.0);
   if (J.btally) {
     const long long nvox = (long long)J.nx * J.ny * J.nz;
     atomicAdd(J.btally + (long long)(hist % uint32_t(J.nbeamlets)) * nvox + (long long)idx, de);
+  }
+}
+
+// tally forms of the block kernels, as template flags: warp-aggregated
+// atomics, and the plain 3-D tally. A run whose jobs all score voxel dose only
+// (no slab depth tally, no step counts, no beamlet tally) gets kernels
+// without the other forms' code at every deposit site (smaller kernels: the
+// phases are instruction-fetch bound)
+constexpr int kTallyAgg = 1, kTallyPlain = 2;
+template <int TF>
+__device__ __forceinline__ void ScoreT(const JobF& J, uint32_t meta, int ix, int iy, int iz, uint32_t hist, float e,
+                                       const DepthAcc& d) {
+  if constexpr ((TF & kTallyPlain) != 0) {
+    const uint32_t idx = (uint32_t(iz) * uint32_t(J.ny) + uint32_t(iy)) * uint32_t(J.nx) + uint32_t(ix);
+    ScoreBin(J, SliceOfSub(meta >> 2), idx, double(e), TF & kTallyAgg);
+  } else {
+    Score(J, meta, ix, iy, iz, hist, e, TF & kTallyAgg, d);
   }
 }
 
@@ -1294,7 +1316,7 @@ __device__ __forceinline__ void AnnihilateF(const PhaseArgs& a, const PState& p,
 // a voxel face only moves onto it, and the next one settles. One deposit at
 // most is scored, and one escape counted, per sub-step, at one place in the
 // code each (fewer inlined copies: the kernel is instruction-fetch bound).
-template <int AGG, class SA>
+template <int TF, class SA>
 __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, const JobF* jobs, SA& S,
                                         int k, EscTally& esc, unsigned long long& nsteps, const DepthAcc& dacc) {
   const DevTables<float>& T = a.T;
@@ -1398,7 +1420,7 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
     }
   }
   if (score) {
-    Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, scored, AGG, dacc);
+    ScoreT<TF>(J, p.meta, p.ix, p.iy, p.iz, p.hist, scored, dacc);
     acc += scored;
   }
   if (moves) {
@@ -1474,7 +1496,7 @@ __device__ __forceinline__ void EventMscEnd(const PhaseArgs& a, const ETables& e
 
 // bremsstrahlung (SimDPMLike.cc:172-194, :661-695); false when the electron
 // fell below the tracking cut and finished
-template <int AGG, class SA>
+template <int TF, class SA>
 __device__ __forceinline__ bool EventBrem(const PhaseArgs& a, const JobF* jobs, SA& S, int k,
                                          const DepthAcc& dacc) {
   PState p;
@@ -1505,7 +1527,7 @@ __device__ __forceinline__ bool EventBrem(const PhaseArgs& a, const JobF* jobs, 
     p.e -= eg;
   }
   if (p.e < T.ecut) {
-    Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, p.e, AGG, dacc);
+    ScoreT<TF>(J, p.meta, p.ix, p.iy, p.iz, p.hist, p.e, dacc);
     acc += p.e;
     if ((fl & kFPositron) != 0) AnnihilateF(a, p, rng, acc);
     atomicAdd(a.histE + p.slot, acc);
@@ -1587,7 +1609,8 @@ __device__ __forceinline__ bool RefillSlot(const PhaseArgs& a, const ETables& et
   return true;
 }
 
-template <int AGG, int NS>
+// TF: tally flags (kTallyAgg, kTallyPlain); NS: slots per block
+template <int TF, int NS>
 __global__ void __launch_bounds__(kBlockThreads, kBlockMinBlocks) ElectronPhaseB(PhaseArgs a) {
   using SlotArrays = SlotArraysT<NS>;
   extern __shared__ __align__(16) unsigned char dyn[];
@@ -1629,7 +1652,7 @@ __global__ void __launch_bounds__(kBlockThreads, kBlockMinBlocks) ElectronPhaseB
         if (have) EventMscEnd(a, et, jobs, S, k);
         break;
       case kRBrem:
-        if (have) live = EventBrem<AGG>(a, jobs, S, k, dacc);
+        if (have) live = EventBrem<TF>(a, jobs, S, k, dacc);
         break;
       case kRMoller:
         if (have) EventMoller(a, et, jobs, S, k);
@@ -1658,7 +1681,7 @@ __global__ void __launch_bounds__(kBlockThreads, kBlockMinBlocks) ElectronPhaseB
     for (int rep = 0; rep < 2 && (rep == 0 ? __any_sync(kFull, code == 0)
                                            : __popc(__ballot_sync(kFull, code == 0)) >= kSecondStepLanes);
          ++rep)
-      if (code == 0) code = StepSlot<AGG>(a, et, jobs, S, k, esc, nsteps, dacc);
+      if (code == 0) code = StepSlot<TF>(a, et, jobs, S, k, esc, nsteps, dacc);
     // the ring of the slot's next action; a finished slot goes back to the
     // idle ring while there is work left, else it retires (q == kRings)
     int q = -1;
@@ -1732,7 +1755,7 @@ __device__ __forceinline__ void StorePhoton(PSlotArrays& S, int k, const PState&
 // Woodcock steps of slot k (SimDPMLike.cc:471-508), up to kPhotonStepsPerTake
 // while they are delta steps: 0 delta step, 1 Compton, 2 pair, 3 finished
 // (escaped, absorbed, or over the step cap)
-template <int AGG>
+template <int TF>
 __device__ __forceinline__ int PhotonStepSlot(const PhaseArgs& a, const PTables& pt, const JobF* jobs, PSlotArrays& S,
                                               int k, EscTally& esc, unsigned long long& nph, const DepthAcc& dacc) {
   const DevTables<float>& T = a.T;
@@ -1775,7 +1798,7 @@ __device__ __forceinline__ int PhotonStepSlot(const PhaseArgs& a, const PTables&
               code = 2;
             } else {
               // photoelectric absorption (also below the pair threshold)
-              Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, p.e, AGG, dacc);
+              ScoreT<TF>(J, p.meta, p.ix, p.iy, p.iz, p.hist, p.e, dacc);
               acc += p.e;
               code = 3;
             }
@@ -1796,7 +1819,7 @@ __device__ __forceinline__ int PhotonStepSlot(const PhaseArgs& a, const PTables&
 
 // Compton scattering at the slot's position (SimDPMLike.cc:512-570); false
 // when the scattered photon falls below the cut and is absorbed
-template <int AGG>
+template <int TF>
 __device__ __forceinline__ bool PhotonComptonSlot(const PhaseArgs& a, const JobF* jobs, PSlotArrays& S, int k,
                                                   const DepthAcc& dacc) {
   const DevTables<float>& T = a.T;
@@ -1815,7 +1838,7 @@ __device__ __forceinline__ bool PhotonComptonSlot(const PhaseArgs& a, const JobF
   float sn, cs;
   __sincosf(phPhi, &sn, &cs);
   if (elE < T.ecut) {
-    Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, elE, AGG, dacc);
+    ScoreT<TF>(J, p.meta, p.ix, p.iy, p.iz, p.hist, elE, dacc);
     acc += elE;
   } else {
     const float e0 = kappa;
@@ -1831,7 +1854,7 @@ __device__ __forceinline__ bool PhotonComptonSlot(const PhaseArgs& a, const JobF
   }
   p.e = phE;
   if (p.e < T.gcut) {
-    Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, p.e, AGG, dacc);
+    ScoreT<TF>(J, p.meta, p.ix, p.iy, p.iz, p.hist, p.e, dacc);
     acc += p.e;
     atomicAdd(a.histE + p.slot, acc);
     return false;
@@ -1846,7 +1869,7 @@ __device__ __forceinline__ bool PhotonComptonSlot(const PhaseArgs& a, const JobF
 }
 
 // pair production at the slot's position (SimDPMLike.cc:573-627); the photon ends
-template <int AGG>
+template <int TF>
 __device__ __forceinline__ void PhotonPairSlot(const PhaseArgs& a, const JobF* jobs, PSlotArrays& S, int k,
                                                const DepthAcc& dacc) {
   const DevTables<float>& T = a.T;
@@ -1859,7 +1882,7 @@ __device__ __forceinline__ void PhotonPairSlot(const PhaseArgs& a, const JobF* j
   const float e1 = rng.U() * sum;
   const float e2 = sum - e1;
   if (e2 < T.ecut) {
-    Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, e2, AGG, dacc);
+    ScoreT<TF>(J, p.meta, p.ix, p.iy, p.iz, p.hist, e2, dacc);
     acc += e2;
   } else {
     PState c = p;
@@ -1868,7 +1891,7 @@ __device__ __forceinline__ void PhotonPairSlot(const PhaseArgs& a, const JobF* j
     if (!Append(a.outE, a.outECount, a.overflow, c)) acc += e2;
   }
   if (e1 < T.ecut) {
-    Score(J, p.meta, p.ix, p.iy, p.iz, p.hist, e1, AGG, dacc);
+    ScoreT<TF>(J, p.meta, p.ix, p.iy, p.iz, p.hist, e1, dacc);
     acc += e1;
     AnnihilateF(a, p, rng, acc);   // at rest (SimDPMLike.cc:753-791)
   } else {
@@ -1905,7 +1928,8 @@ __device__ __forceinline__ bool PhotonRefillSlot(const PhaseArgs& a, const JobF*
   return true;
 }
 
-template <int AGG>
+// TF: tally flags (kTallyAgg, kTallyPlain)
+template <int TF>
 __global__ void __launch_bounds__(kPBlockThreads, kPBlockMinBlocks) PhotonPhaseB(PhaseArgs a) {
   extern __shared__ __align__(16) unsigned char dyn[];
   PSlotArrays& S = *reinterpret_cast<PSlotArrays*>(dyn);
@@ -1936,9 +1960,9 @@ __global__ void __launch_bounds__(kPBlockThreads, kPBlockMinBlocks) PhotonPhaseB
     const bool have = lane < n;
     bool live = have;
     if (ring == kPRComp) {
-      if (have) live = PhotonComptonSlot<AGG>(a, jobs, S, k, dacc);
+      if (have) live = PhotonComptonSlot<TF>(a, jobs, S, k, dacc);
     } else if (ring == kPRPair) {
-      if (have) PhotonPairSlot<AGG>(a, jobs, S, k, dacc);
+      if (have) PhotonPairSlot<TF>(a, jobs, S, k, dacc);
       live = false;
     } else if (ring == kPRIdle) {
       live = false;
@@ -1952,7 +1976,7 @@ __global__ void __launch_bounds__(kPBlockThreads, kPBlockMinBlocks) PhotonPhaseB
         if (item < total) live = PhotonRefillSlot(a, jobs, spre, S, k, item, esc);
       }
     }
-    const int code = live ? PhotonStepSlot<AGG>(a, pt, jobs, S, k, esc, nph, dacc) : 3;
+    const int code = live ? PhotonStepSlot<TF>(a, pt, jobs, S, k, esc, nph, dacc) : 3;
     int q = -1;
     if (have) {
       q = int((kPRingOfCode >> (4 * code)) & 15u);
@@ -2179,6 +2203,8 @@ cudaError_t PreparePhotonPhase(const DevTables<float>& T) {
   const int sb = int(PhotonBlockSmemBytes(kDepthBins));
   if (e == cudaSuccess) e = cudaFuncSetAttribute(PhotonPhaseB<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(PhotonPhaseB<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(PhotonPhaseB<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(PhotonPhaseB<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
   return e;
 }
 
@@ -2186,8 +2212,12 @@ int PhotonBlockBlocksPerSM() { return kPBlockMinBlocks; }
 
 cudaError_t LaunchPhotonPhaseBlock(const PhaseArgs& a, int blocks, cudaStream_t st) {
   const size_t smem = PhotonBlockSmemBytes(a.depthBins);
-  if (a.aggregate) PhotonPhaseB<1><<<blocks, kPBlockThreads, smem, st>>>(a);
-  else PhotonPhaseB<0><<<blocks, kPBlockThreads, smem, st>>>(a);
+  switch ((a.aggregate ? kTallyAgg : 0) | (a.plainTally ? kTallyPlain : 0)) {
+    case 0: PhotonPhaseB<0><<<blocks, kPBlockThreads, smem, st>>>(a); break;
+    case 1: PhotonPhaseB<1><<<blocks, kPBlockThreads, smem, st>>>(a); break;
+    case 2: PhotonPhaseB<2><<<blocks, kPBlockThreads, smem, st>>>(a); break;
+    default: PhotonPhaseB<3><<<blocks, kPBlockThreads, smem, st>>>(a); break;
+  }
   return cudaGetLastError();
 }
 
@@ -2206,8 +2236,10 @@ template <int NS>
 static cudaError_t PrepareBlockPhaseFor(const DevTables<float>& T) {
   const int smem = int(BlockPhaseSmemBytesFor<NS>(T, kDepthBins));
   cudaError_t e = cudaFuncSetAttribute(ElectronPhaseB<0, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(ElectronPhaseB<1, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(ElectronPhaseB<1, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(ElectronPhaseB<2, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(ElectronPhaseB<3, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  return e;
 }
 
 cudaError_t PrepareBlockPhase(const DevTables<float>& T) {
@@ -2218,8 +2250,12 @@ cudaError_t PrepareBlockPhase(const DevTables<float>& T) {
 template <int NS>
 static void LaunchElectronPhaseBlockFor(const PhaseArgs& a, int blocks, cudaStream_t st) {
   const size_t smem = BlockPhaseSmemBytesFor<NS>(a.T, a.depthBins);
-  if (a.aggregate) ElectronPhaseB<1, NS><<<blocks, kBlockThreads, smem, st>>>(a);
-  else ElectronPhaseB<0, NS><<<blocks, kBlockThreads, smem, st>>>(a);
+  switch ((a.aggregate ? kTallyAgg : 0) | (a.plainTally ? kTallyPlain : 0)) {
+    case 0: ElectronPhaseB<0, NS><<<blocks, kBlockThreads, smem, st>>>(a); break;
+    case 1: ElectronPhaseB<1, NS><<<blocks, kBlockThreads, smem, st>>>(a); break;
+    case 2: ElectronPhaseB<2, NS><<<blocks, kBlockThreads, smem, st>>>(a); break;
+    default: ElectronPhaseB<3, NS><<<blocks, kBlockThreads, smem, st>>>(a); break;
+  }
 }
 
 cudaError_t LaunchElectronPhaseBlock(const PhaseArgs& a, int blocks, int slots, cudaStream_t st) {
