@@ -128,6 +128,8 @@ struct PhaseArgs {
   int plainTally;              // 1: every job scores a 3-D voxel tally only (depthBins 0, no
                                //    tallyDepth, step counts or beamlet tally): the block kernels
                                //    built for that form run
+  int plainGeom;               // 1: every job is a voxel phantom of material ids with nominal
+                               //    densities (no slab preset, no per-voxel density array)
 };
 
 // shared-memory depth tally of a block (slab jobs): bins of all jobs of a run

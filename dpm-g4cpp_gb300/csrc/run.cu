@@ -280,8 +280,11 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
   // jobs that all score a 3-D voxel tally only run the block kernels built
   // for that tally form
   bool plainTally = depthBins == 0;
-  for (int j = 0; j < njobs; ++j)
+  bool plainGeom = true;
+  for (int j = 0; j < njobs; ++j) {
     plainTally = plainTally && hj[j].tallyDepth == 0 && hj[j].steps == nullptr && hj[j].btally == nullptr;
+    plainGeom = plainGeom && hj[j].matByDepth == 0 && hj[j].rho == nullptr;
+  }
   JobF* dj;
   if (int rc = buf.Get(&dj, njobs)) return rc;
   CK(cudaMemcpyAsync(dj, hj.data(), njobs * sizeof(JobF), cudaMemcpyHostToDevice, st));
@@ -352,6 +355,7 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
           a.depthBins = depthBins;
           a.depthStride = maxNz;
           a.plainTally = plainTally ? 1 : 0;
+          a.plainGeom = plainGeom ? 1 : 0;
           // photons of generation g; their electrons join generation g
           a.segs = sP; a.nsegs = int(c.segP.size()); a.nPrimaries = (g == 0) ? c.nP : 0;
           a.in = qp[g & 1]; a.inCount = cntP + g * kStripes;

@@ -296,6 +296,10 @@ __device__ __forceinline__ void Score(const JobF& J, uint32_t meta, int ix, int 
 // without the other forms' code at every deposit site (smaller kernels: the
 // phases are instruction-fetch bound)
 constexpr int kTallyAgg = 1, kTallyPlain = 2;
+// geometry form flag (set only together with kTallyPlain): every job is a
+// voxel phantom of material ids with the materials' nominal densities (no
+// slab preset indexed by depth, no per-voxel density array)
+constexpr int kGeomPlain = 4;
 template <int TF>
 __device__ __forceinline__ void ScoreT(const JobF& J, uint32_t meta, int ix, int iy, int iz, uint32_t hist, float e,
                                        const DepthAcc& d) {
@@ -352,6 +356,23 @@ __device__ __forceinline__ int MaterialAt(const JobF& J, int ix, int iy, int iz)
   const uint8_t m = J.matByDepth ? __ldg(J.mat + iz)
                                  : __ldg(J.mat + (uint32_t(iz) * uint32_t(J.ny) + uint32_t(iy)) * uint32_t(J.nx) + uint32_t(ix));
   return m == kVacuum ? -1 : int(m);
+}
+
+// MaterialAt and VoxelRho for the kernels' geometry form (TF & kGeomPlain:
+// the 3-D id array and the material's nominal density only)
+template <int TF>
+__device__ __forceinline__ int MaterialAtT(const JobF& J, int ix, int iy, int iz) {
+  if constexpr ((TF & kGeomPlain) != 0) {
+    const uint8_t m = __ldg(J.mat + (uint32_t(iz) * uint32_t(J.ny) + uint32_t(iy)) * uint32_t(J.nx) + uint32_t(ix));
+    return m == kVacuum ? -1 : int(m);
+  } else {
+    return MaterialAt(J, ix, iy, iz);
+  }
+}
+template <int TF>
+__device__ __forceinline__ float VoxelRhoT(const JobF& J, const DevTables<float>& T, int ix, int iy, int iz, int im) {
+  if constexpr ((TF & kGeomPlain) != 0) return T.density[im];
+  else return VoxelRho(J, T, ix, iy, iz, im);
 }
 
 // Distance to the voxel walls along d. A face closer than half the tolerance
@@ -1335,7 +1356,7 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
     if (Settle(J, p, s.sGeom, s.axis)) {
       im = S.mat[k];
       if (im == kMatUnknown || p.ix != ox || p.iy != oy || p.iz != oz) {
-        im = MaterialAt(J, p.ix, p.iy, p.iz);
+        im = MaterialAtT<TF>(J, p.ix, p.iy, p.iz);
         S.mat[k] = int8_t(im);
       }
     }
@@ -1356,7 +1377,7 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
   } else {
     ++nsteps;
     const float ecut = T.ecut;
-    const float rho = VoxelRho(J, T, p.ix, p.iy, p.iz, im);
+    const float rho = VoxelRhoT<TF>(J, T, p.ix, p.iy, p.iz, im);
     step = s.sGeom;
     // dE/dx and 1/lambda_1 at E and at the mid-step energy, each pair from
     // one record; a step that no event shortens ends with the same mid-step
@@ -1400,7 +1421,7 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
         bool inside;
         if (what == 0) inside = MoveToFace(J, p, step, s.axis);
         else { p.lx += step * p.dx; p.ly += step * p.dy; p.lz += step * p.dz; inside = true; }
-        const int im2 = inside ? MaterialAt(J, p.ix, p.iy, p.iz) : -1;
+        const int im2 = inside ? MaterialAtT<TF>(J, p.ix, p.iy, p.iz) : -1;
         if (im2 < 0) {
           out = scored + 2.0f * kEMC2f;
           escapes = true;
@@ -1579,7 +1600,7 @@ __device__ __forceinline__ void EventMoller(const PhaseArgs& a, const ETables& e
 
 // first sub-step state of a claimed work item (a primary or a queued
 // electron) in slot k; false when it starts outside the phantom
-template <class SA>
+template <int TF, class SA>
 __device__ __forceinline__ bool RefillSlot(const PhaseArgs& a, const ETables& et, const JobF* jobs,
                                            const unsigned long long* spre, SA& S, int k,
                                            unsigned long long item, EscTally& esc) {
@@ -1594,7 +1615,7 @@ __device__ __forceinline__ bool RefillSlot(const PhaseArgs& a, const ETables& et
   }
   const int job = JobOfSub(p.meta >> 2);
   const JobF& J = jobs[job];
-  const int im0 = InBox(J, p.ix, p.iy, p.iz) ? MaterialAt(J, p.ix, p.iy, p.iz) : -1;
+  const int im0 = InBox(J, p.ix, p.iy, p.iz) ? MaterialAtT<TF>(J, p.ix, p.iy, p.iz) : -1;
   if (im0 < 0) {
     const double out = p.e + ((p.meta & 3u) == 2u ? 2.0 * kEMC2f : 0.0);
     esc.Add(jobs, job, out);
@@ -1609,7 +1630,7 @@ __device__ __forceinline__ bool RefillSlot(const PhaseArgs& a, const ETables& et
   return true;
 }
 
-// TF: tally flags (kTallyAgg, kTallyPlain); NS: slots per block
+// TF: form flags (kTallyAgg, kTallyPlain, kGeomPlain); NS: slots per block
 template <int TF, int NS>
 __global__ void __launch_bounds__(kBlockThreads, kBlockMinBlocks) ElectronPhaseB(PhaseArgs a) {
   using SlotArrays = SlotArraysT<NS>;
@@ -1667,7 +1688,7 @@ __global__ void __launch_bounds__(kBlockThreads, kBlockMinBlocks) ElectronPhaseB
           base = g.shfl(base, 0);
           const unsigned long long item = base + g.thread_rank();
           if (base + g.size() >= total) *vexh = 1;
-          if (item < total) live = RefillSlot(a, et, jobs, spre, S, k, item, esc);
+          if (item < total) live = RefillSlot<TF>(a, et, jobs, spre, S, k, item, esc);
         }
         break;
       default:
@@ -1779,13 +1800,13 @@ __device__ __forceinline__ int PhotonStepSlot(const PhaseArgs& a, const PTables&
       ++nph;
       const float step = -lmax * __logf(rng.U());
       int im = -1;
-      if (Fly(J, p, step)) im = MaterialAt(J, p.ix, p.iy, p.iz);
+      if (Fly(J, p, step)) im = MaterialAtT<TF>(J, p.ix, p.iy, p.iz);
       if (im < 0) {
         acc += p.e;
         esc.Add(jobs, job, double(p.e));
         code = 3;
       } else {
-        const float rho = VoxelRho(J, T, p.ix, p.iy, p.iz, im);
+        const float rho = VoxelRhoT<TF>(J, T, p.ix, p.iy, p.iz, im);
         const float r1 = rng.U();
         float prob = 1.0f - LinearGet(pt.tot[im], p.e) * rho * lmax;
         if (r1 >= prob) {
@@ -1904,6 +1925,7 @@ __device__ __forceinline__ void PhotonPairSlot(const PhaseArgs& a, const JobF* j
 }
 
 // a new photon (primary or queued) in slot k; false when it starts outside
+template <int TF>
 __device__ __forceinline__ bool PhotonRefillSlot(const PhaseArgs& a, const JobF* jobs,
                                                  const unsigned long long* spre, PSlotArrays& S, int k,
                                                  unsigned long long item, EscTally& esc) {
@@ -1917,7 +1939,7 @@ __device__ __forceinline__ bool PhotonRefillSlot(const PhaseArgs& a, const JobF*
     rng.Init(J.k0, J.k1, p.hist, p.ulo, p.uhi);
   }
   const JobF& J = jobs[JobOfSub(p.meta >> 2)];
-  if (!InBox(J, p.ix, p.iy, p.iz) || MaterialAt(J, p.ix, p.iy, p.iz) < 0) {
+  if (!InBox(J, p.ix, p.iy, p.iz) || MaterialAtT<TF>(J, p.ix, p.iy, p.iz) < 0) {
     esc.Add(jobs, JobOfSub(p.meta >> 2), double(p.e));
     atomicAdd(a.histE + p.slot, double(p.e));
     return false;
@@ -1928,7 +1950,7 @@ __device__ __forceinline__ bool PhotonRefillSlot(const PhaseArgs& a, const JobF*
   return true;
 }
 
-// TF: tally flags (kTallyAgg, kTallyPlain)
+// TF: form flags (kTallyAgg, kTallyPlain, kGeomPlain)
 template <int TF>
 __global__ void __launch_bounds__(kPBlockThreads, kPBlockMinBlocks) PhotonPhaseB(PhaseArgs a) {
   extern __shared__ __align__(16) unsigned char dyn[];
@@ -1973,7 +1995,7 @@ __global__ void __launch_bounds__(kPBlockThreads, kPBlockMinBlocks) PhotonPhaseB
         base = g.shfl(base, 0);
         const unsigned long long item = base + g.thread_rank();
         if (base + g.size() >= total) *vexh = 1;
-        if (item < total) live = PhotonRefillSlot(a, jobs, spre, S, k, item, esc);
+        if (item < total) live = PhotonRefillSlot<TF>(a, jobs, spre, S, k, item, esc);
       }
     }
     const int code = live ? PhotonStepSlot<TF>(a, pt, jobs, S, k, esc, nph, dacc) : 3;
@@ -2192,6 +2214,16 @@ __global__ void __launch_bounds__(256) RingSelfTestKernel(int nslots, int rounds
 
 int ElectronPhaseSmemBytes(const DevTables<float>& T) { return int(T.elecCount * sizeof(float)); }
 
+// template flags of the block kernels a run's phase arguments select: 0 or
+// kTallyAgg (the general forms), kTallyPlain, kTallyPlain | kGeomPlain (warp
+// aggregation, measured slower on every workload, is built for the general
+// form only)
+static int KernelForm(const PhaseArgs& a) {
+  if (a.aggregate) return kTallyAgg;
+  if (!a.plainTally) return 0;
+  return a.plainGeom ? (kTallyPlain | kGeomPlain) : kTallyPlain;
+}
+
 // dynamic shared memory of the block-batched photon phase
 __host__ __device__ inline size_t PhotonBlockSmemBytes(int depthBins) {
   return ((PhotonBlockStaticBytes() + 15) & ~size_t(15)) + DepthAccBytes(depthBins);
@@ -2204,7 +2236,7 @@ cudaError_t PreparePhotonPhase(const DevTables<float>& T) {
   if (e == cudaSuccess) e = cudaFuncSetAttribute(PhotonPhaseB<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(PhotonPhaseB<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(PhotonPhaseB<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(PhotonPhaseB<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(PhotonPhaseB<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
   return e;
 }
 
@@ -2212,11 +2244,11 @@ int PhotonBlockBlocksPerSM() { return kPBlockMinBlocks; }
 
 cudaError_t LaunchPhotonPhaseBlock(const PhaseArgs& a, int blocks, cudaStream_t st) {
   const size_t smem = PhotonBlockSmemBytes(a.depthBins);
-  switch ((a.aggregate ? kTallyAgg : 0) | (a.plainTally ? kTallyPlain : 0)) {
+  switch (KernelForm(a)) {
     case 0: PhotonPhaseB<0><<<blocks, kPBlockThreads, smem, st>>>(a); break;
     case 1: PhotonPhaseB<1><<<blocks, kPBlockThreads, smem, st>>>(a); break;
     case 2: PhotonPhaseB<2><<<blocks, kPBlockThreads, smem, st>>>(a); break;
-    default: PhotonPhaseB<3><<<blocks, kPBlockThreads, smem, st>>>(a); break;
+    default: PhotonPhaseB<6><<<blocks, kPBlockThreads, smem, st>>>(a); break;
   }
   return cudaGetLastError();
 }
@@ -2238,7 +2270,7 @@ static cudaError_t PrepareBlockPhaseFor(const DevTables<float>& T) {
   cudaError_t e = cudaFuncSetAttribute(ElectronPhaseB<0, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(ElectronPhaseB<1, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(ElectronPhaseB<2, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(ElectronPhaseB<3, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(ElectronPhaseB<6, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   return e;
 }
 
@@ -2250,11 +2282,11 @@ cudaError_t PrepareBlockPhase(const DevTables<float>& T) {
 template <int NS>
 static void LaunchElectronPhaseBlockFor(const PhaseArgs& a, int blocks, cudaStream_t st) {
   const size_t smem = BlockPhaseSmemBytesFor<NS>(a.T, a.depthBins);
-  switch ((a.aggregate ? kTallyAgg : 0) | (a.plainTally ? kTallyPlain : 0)) {
+  switch (KernelForm(a)) {
     case 0: ElectronPhaseB<0, NS><<<blocks, kBlockThreads, smem, st>>>(a); break;
     case 1: ElectronPhaseB<1, NS><<<blocks, kBlockThreads, smem, st>>>(a); break;
     case 2: ElectronPhaseB<2, NS><<<blocks, kBlockThreads, smem, st>>>(a); break;
-    default: ElectronPhaseB<3, NS><<<blocks, kBlockThreads, smem, st>>>(a); break;
+    default: ElectronPhaseB<6, NS><<<blocks, kBlockThreads, smem, st>>>(a); break;
   }
 }
 
