@@ -130,6 +130,8 @@ struct PhaseArgs {
                                //    built for that form run
   int plainGeom;               // 1: every job is a voxel phantom of material ids with nominal
                                //    densities (no slab preset, no per-voxel density array)
+  JobF job0;                   // the first job's record (a single-job run reads it from the
+                               //    kernel parameters)
 };
 
 // shared-memory depth tally of a block (slab jobs): bins of all jobs of a run

@@ -356,6 +356,7 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
           a.depthStride = maxNz;
           a.plainTally = plainTally ? 1 : 0;
           a.plainGeom = plainGeom ? 1 : 0;
+          if (njobs > 0) a.job0 = hj[0];
           // photons of generation g; their electrons join generation g
           a.segs = sP; a.nsegs = int(c.segP.size()); a.nPrimaries = (g == 0) ? c.nP : 0;
           a.in = qp[g & 1]; a.inCount = cntP + g * kStripes;

@@ -300,6 +300,15 @@ constexpr int kTallyAgg = 1, kTallyPlain = 2;
 // voxel phantom of material ids with the materials' nominal densities (no
 // slab preset indexed by depth, no per-voxel density array)
 constexpr int kGeomPlain = 4;
+// single-job form flag (electron block kernel): the run has one job, whose
+// record the kernel reads from its parameter block (constant-bank operands)
+// instead of loading it from shared memory at every use
+constexpr int kSingleJob = 8;
+template <int TF>
+__device__ __forceinline__ const JobF& JobRec(const PhaseArgs& a, const JobF* jobs, int job) {
+  if constexpr ((TF & kSingleJob) != 0) return a.job0;
+  else return jobs[job];
+}
 template <int TF>
 __device__ __forceinline__ void ScoreT(const JobF& J, uint32_t meta, int ix, int iy, int iz, uint32_t hist, float e,
                                        const DepthAcc& d) {
@@ -1346,7 +1355,7 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
   uint32_t fl, pst;
   LoadStepState(S, k, p, s, fl, pst);
   const int job = JobOfSub(fl >> 8);
-  const JobF& J = jobs[job];
+  const JobF& J = JobRec<TF>(a, jobs, job);
   const bool positron = (fl & kFPositron) != 0;
   double acc = S.acc[k];
   int code = 0;
@@ -1473,14 +1482,14 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
 }
 
 // GS angular deflection at the MSC hinge (SimDPMLike.cc:216-226, :731-750)
-template <class SA>
+template <int TF, class SA>
 __device__ __forceinline__ void EventHinge(const PhaseArgs& a, const JobF* jobs, SA& S, int k) {
   PState p;
   EState s;
   uint32_t fl;
   LoadSlot(S, k, p, s, fl);
   PRng rng;
-  SlotRng(S, k, jobs[JobOfSub(fl >> 8)], p.hist, rng);
+  SlotRng(S, k, JobRec<TF>(a, jobs, JobOfSub(fl >> 8)), p.hist, rng);
   const float r2 = rng.U(), r1 = rng.U();
   float cost, sint;
   SampleGSAngle(a.T.gs, s.ekin0, r1, r2, cost, sint);
@@ -1497,12 +1506,12 @@ __device__ __forceinline__ void EventHinge(const PhaseArgs& a, const JobF* jobs,
 }
 
 // end of an MSC step: new scattering strength and hinge (SimDPMLike.cc:227-237)
-template <class SA>
+template <int TF, class SA>
 __device__ __forceinline__ void EventMscEnd(const PhaseArgs& a, const ETables& et, const JobF* jobs, SA& S,
                                             int k) {
   const uint4 d = S.id[k], q = S.rs[k];
   const uint32_t fl = d.x;
-  const JobF& J = jobs[JobOfSub(fl >> 8)];
+  const JobF& J = JobRec<TF>(a, jobs, JobOfSub(fl >> 8));
   PRng rng;
   rng.Init(J.k0, J.k1, d.y, q.x, q.y);
   rng.ctr = q.z;
@@ -1524,7 +1533,7 @@ __device__ __forceinline__ bool EventBrem(const PhaseArgs& a, const JobF* jobs, 
   EState s;
   uint32_t fl;
   LoadSlot(S, k, p, s, fl);
-  const JobF& J = jobs[JobOfSub(fl >> 8)];
+  const JobF& J = JobRec<TF>(a, jobs, JobOfSub(fl >> 8));
   const DevTables<float>& T = a.T;
   PRng rng;
   SlotRng(S, k, J, p.hist, rng);
@@ -1563,14 +1572,14 @@ __device__ __forceinline__ bool EventBrem(const PhaseArgs& a, const JobF* jobs, 
 }
 
 // Moller delta electron (SimDPMLike.cc:204-214, :699-728)
-template <class SA>
+template <int TF, class SA>
 __device__ __forceinline__ void EventMoller(const PhaseArgs& a, const ETables& et, const JobF* jobs, SA& S,
                                             int k) {
   PState p;
   EState s;
   uint32_t fl;
   LoadSlot(S, k, p, s, fl);
-  const JobF& J = jobs[JobOfSub(fl >> 8)];
+  const JobF& J = JobRec<TF>(a, jobs, JobOfSub(fl >> 8));
   PRng rng;
   SlotRng(S, k, J, p.hist, rng);
   double acc = S.acc[k];
@@ -1610,11 +1619,11 @@ __device__ __forceinline__ bool RefillSlot(const PhaseArgs& a, const ETables& et
     MakePrimary(a, a.segs, (long long)item, p, rng);
   } else {
     LoadParticle(a.in, StripedIndex(a.in, spre, item - a.nPrimaries), p);
-    const JobF& J = jobs[JobOfSub(p.meta >> 2)];
+    const JobF& J = JobRec<TF>(a, jobs, JobOfSub(p.meta >> 2));
     rng.Init(J.k0, J.k1, p.hist, p.ulo, p.uhi);
   }
   const int job = JobOfSub(p.meta >> 2);
-  const JobF& J = jobs[job];
+  const JobF& J = JobRec<TF>(a, jobs, job);
   const int im0 = InBox(J, p.ix, p.iy, p.iz) ? MaterialAtT<TF>(J, p.ix, p.iy, p.iz) : -1;
   if (im0 < 0) {
     const double out = p.e + ((p.meta & 3u) == 2u ? 2.0 * kEMC2f : 0.0);
@@ -1630,7 +1639,7 @@ __device__ __forceinline__ bool RefillSlot(const PhaseArgs& a, const ETables& et
   return true;
 }
 
-// TF: form flags (kTallyAgg, kTallyPlain, kGeomPlain); NS: slots per block
+// TF: form flags (kTallyAgg, kTallyPlain, kGeomPlain, kSingleJob); NS: slots per block
 template <int TF, int NS>
 __global__ void __launch_bounds__(kBlockThreads, kBlockMinBlocks) ElectronPhaseB(PhaseArgs a) {
   using SlotArrays = SlotArraysT<NS>;
@@ -1667,16 +1676,16 @@ __global__ void __launch_bounds__(kBlockThreads, kBlockMinBlocks) ElectronPhaseB
     bool live = have;
     switch (ring) {   // the same on every lane
       case kRHinge:
-        if (have) EventHinge(a, jobs, S, k);
+        if (have) EventHinge<TF>(a, jobs, S, k);
         break;
       case kRMscEnd:
-        if (have) EventMscEnd(a, et, jobs, S, k);
+        if (have) EventMscEnd<TF>(a, et, jobs, S, k);
         break;
       case kRBrem:
         if (have) live = EventBrem<TF>(a, jobs, S, k, dacc);
         break;
       case kRMoller:
-        if (have) EventMoller(a, et, jobs, S, k);
+        if (have) EventMoller<TF>(a, et, jobs, S, k);
         break;
       case kRIdle:
         live = false;
@@ -2271,6 +2280,11 @@ static cudaError_t PrepareBlockPhaseFor(const DevTables<float>& T) {
   if (e == cudaSuccess) e = cudaFuncSetAttribute(ElectronPhaseB<1, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(ElectronPhaseB<2, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(ElectronPhaseB<6, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if constexpr (NS == kSlots) {
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(ElectronPhaseB<8, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(ElectronPhaseB<10, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(ElectronPhaseB<14, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  }
   return e;
 }
 
@@ -2282,11 +2296,16 @@ cudaError_t PrepareBlockPhase(const DevTables<float>& T) {
 template <int NS>
 static void LaunchElectronPhaseBlockFor(const PhaseArgs& a, int blocks, cudaStream_t st) {
   const size_t smem = BlockPhaseSmemBytesFor<NS>(a.T, a.depthBins);
-  switch (KernelForm(a)) {
+  // the single-job forms are built for the default slot count
+  const int f = KernelForm(a) | ((NS == kSlots && a.njobs == 1 && !a.aggregate) ? kSingleJob : 0);
+  switch (f) {
     case 0: ElectronPhaseB<0, NS><<<blocks, kBlockThreads, smem, st>>>(a); break;
     case 1: ElectronPhaseB<1, NS><<<blocks, kBlockThreads, smem, st>>>(a); break;
     case 2: ElectronPhaseB<2, NS><<<blocks, kBlockThreads, smem, st>>>(a); break;
-    default: ElectronPhaseB<6, NS><<<blocks, kBlockThreads, smem, st>>>(a); break;
+    case 6: ElectronPhaseB<6, NS><<<blocks, kBlockThreads, smem, st>>>(a); break;
+    case 8: ElectronPhaseB<8, kSlots><<<blocks, kBlockThreads, smem, st>>>(a); break;
+    case 10: ElectronPhaseB<10, kSlots><<<blocks, kBlockThreads, smem, st>>>(a); break;
+    default: ElectronPhaseB<14, kSlots><<<blocks, kBlockThreads, smem, st>>>(a); break;
   }
 }
 
