@@ -189,6 +189,24 @@ int BuildImage(const HostTables& h, DevTables<R>& T, void** dptr) {
       fx.Add(reinterpret_cast<const void**>(&s.p), base + offs[m] * sizeof(R));
     }
     elecEnd = base + all.size() * sizeof(R);
+    // one grid and a fixed record stride for all materials (the data files
+    // write every material on the same energies)
+    bool uniform = h.nmat >= 1;
+    for (int m = 1; m < h.nmat && uniform; ++m) {
+      uniform = T.di[m].n == T.di[0].n && T.di[m].logMin == T.di[0].logMin &&
+                T.di[m].invLogDelta == T.di[0].invLogDelta && offs[m] == m * offs[1] &&
+                T.brem[m].n == T.brem[0].n && T.brem[m].logMin == T.brem[0].logMin &&
+                T.brem[m].invLogDelta == T.brem[0].invLogDelta && T.brem[m].emin == T.brem[0].emin &&
+                T.brem[m].emaxm == T.brem[0].emaxm;
+      const Curve& a = h.dedx[m];
+      for (size_t i = 0; uniform && i < a.x.size(); ++i) uniform = a.x[i] == h.dedx[0].x[i];
+      for (size_t i = 0; uniform && i < h.brem[m].x.size(); ++i) uniform = h.brem[m].x[i] == h.brem[0].x[i];
+    }
+    // the brem splines follow one another at (5n + padding) values each
+    const size_t bremStride = (size_t(5 * T.brem[0].n) + 3) & ~size_t(3);
+    T.elecUniform = uniform ? 1 : 0;
+    T.diStride = uniform && h.nmat > 1 ? int(offs[1]) : 0;
+    T.bremStride = uniform ? int(bremStride) : 0;
   }
   // photon linear tables, contiguous
   const size_t photBegin = (img.bytes.size() + 255) & ~size_t(255);

@@ -76,6 +76,12 @@ struct DevTables {
   int elecCount;       // ... for this many values (shared-memory staging)
   const R* photBase;   // the photon linear tables likewise
   int photCount;
+  // FP32: 1 when every material's dE/dx + 1/lambda_1 records and brem spline
+  // lie on material 0's grid, one material after another at a fixed stride
+  // (values between consecutive materials' records): material m's descriptor
+  // is then material 0's with its records moved by m strides
+  int elecUniform;
+  int diStride, bremStride;
 };
 
 // ---------------------------------------------------------------------------

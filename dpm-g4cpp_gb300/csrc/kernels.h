@@ -129,7 +129,8 @@ struct PhaseArgs {
                                //    tallyDepth, step counts or beamlet tally): the block kernels
                                //    built for that form run
   int plainGeom;               // 1: every job is a voxel phantom of material ids with nominal
-                               //    densities (no slab preset, no per-voxel density array)
+                               //    densities (no slab preset, no per-voxel density array), and
+                               //    the electron splines of all materials share one grid
   JobF job0;                   // the first job's record (a single-job run reads it from the
                                //    kernel parameters)
 };

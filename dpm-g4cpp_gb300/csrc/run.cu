@@ -285,6 +285,7 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
     plainTally = plainTally && hj[j].tallyDepth == 0 && hj[j].steps == nullptr && hj[j].btally == nullptr;
     plainGeom = plainGeom && hj[j].matByDepth == 0 && hj[j].rho == nullptr;
   }
+  plainGeom = plainGeom && T->t32.elecUniform != 0;
   JobF* dj;
   if (int rc = buf.Get(&dj, njobs)) return rc;
   CK(cudaMemcpyAsync(dj, hj.data(), njobs * sizeof(JobF), cudaMemcpyHostToDevice, st));

@@ -298,7 +298,9 @@ __device__ __forceinline__ void Score(const JobF& J, uint32_t meta, int ix, int 
 constexpr int kTallyAgg = 1, kTallyPlain = 2;
 // geometry form flag (set only together with kTallyPlain): every job is a
 // voxel phantom of material ids with the materials' nominal densities (no
-// slab preset indexed by depth, no per-voxel density array)
+// slab preset indexed by depth, no per-voxel density array), and the electron
+// splines of all materials lie on one grid at a fixed stride (DevTables::
+// elecUniform)
 constexpr int kGeomPlain = 4;
 // single-job form flag (electron block kernel): the run has one job, whose
 // record the kernel reads from its parameter block (constant-bank operands)
@@ -1346,6 +1348,30 @@ __device__ __forceinline__ void AnnihilateF(const PhaseArgs& a, const PState& p,
 // a voxel face only moves onto it, and the next one settles. One deposit at
 // most is scored, and one escape counted, per sub-step, at one place in the
 // code each (fewer inlined copies: the kernel is instruction-fetch bound).
+// the dE/dx + 1/lambda_1 and brem descriptors of material im: in the plain
+// form material 0's (kernel parameters, constant bank) with the records moved
+// by im strides, else the block's shared copies
+template <int TF>
+__device__ __forceinline__ SplinePairT<float> DiOf(const PhaseArgs& a, const ETables& et, int im) {
+  if constexpr ((TF & kGeomPlain) != 0) {
+    SplinePairT<float> d = a.T.di[0];
+    d.p += im * a.T.diStride;
+    return d;
+  } else {
+    return et.di[im];
+  }
+}
+template <int TF>
+__device__ __forceinline__ SplineT<float> BremOf(const PhaseArgs& a, const ETables& et, int im) {
+  if constexpr ((TF & kGeomPlain) != 0) {
+    SplineT<float> d = a.T.brem[0];
+    d.p += im * a.T.bremStride;
+    return d;
+  } else {
+    return et.brem[im];
+  }
+}
+
 template <int TF, class SA>
 __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, const JobF* jobs, SA& S,
                                         int k, EscTally& esc, unsigned long long& nsteps, const DepthAcc& dacc) {
@@ -1392,14 +1418,14 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
     // one record; a step that no event shortens ends with the same mid-step
     // energy, whose dE/dx is then already at hand
     const float le = __logf(p.e);
-    const DedxItr1 atE = SplinePairLe(et.di[im], p.e, le);
+    const DedxItr1 atE = SplinePairLe(DiOf<TF>(a, et, im), p.e, le);
     float dedx = atE.dedx * rho;
     float emid = fmaxf(p.e - 0.5f * step * dedx, ecut);
     const float lm = __logf(emid);
-    const DedxItr1 atMid = SplinePairLe(et.di[im], emid, lm);
+    const DedxItr1 atMid = SplinePairLe(DiOf<TF>(a, et, im), emid, lm);
     float dTr1 = atMid.itr1 * rho;
     const float dMol = s.invMol * T.mollerScale[im] * rho;
-    const float dBrem = SplineLe(et.brem[im], emid, lm) * rho;
+    const float dBrem = SplineLe(BremOf<TF>(a, et, im), emid, lm) * rho;
     const float sBrem = s.nBrem / dBrem;
     if (sBrem < step) { step = sBrem; what = 1; }
     const float sMol = s.nMol / dMol;
@@ -1408,7 +1434,7 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
     if (sEl < step) {
       sEl = s.nTr1 / (atE.itr1 * rho);
       emid = fmaxf(p.e - 0.5f * sEl * dedx, ecut);
-      dTr1 = SplinePairLe(et.di[im], emid, __logf(emid)).itr1 * rho;
+      dTr1 = SplinePairLe(DiOf<TF>(a, et, im), emid, __logf(emid)).itr1 * rho;
       sEl = fminf(step, s.nTr1 / dTr1);
       step = sEl;
       what = 3;
@@ -1417,7 +1443,7 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
     s.nMol = (what == 2) ? 0.f : s.nMol - step * dMol;
     s.nTr1 = (what == 3) ? 0.f : s.nTr1 - step * dTr1;
     emid = fmaxf(p.e - 0.5f * step * dedx, ecut);
-    dedx = SplinePairLe(et.di[im], emid, __logf(emid)).dedx * rho;
+    dedx = SplinePairLe(DiOf<TF>(a, et, im), emid, __logf(emid)).dedx * rho;
     const float de = step * dedx;
     const float ef = p.e - de;
     if (ef < ecut) {
