@@ -305,7 +305,10 @@ def main():
     nbins = int(mat.size)
     out_d = torch.empty(nbins, dtype=torch.float64).pin_memory().numpy()
     out_d2 = torch.empty(nbins, dtype=torch.float64).pin_memory().numpy()
-    e2e_steps = max(1, min(3, a.steps))
+    e2e_steps = max(1, a.steps)   # as many steps as the device-timed loop
+    p2 = dpm.Phantom.voxels(tables, pinned, 2.0)   # one untimed step: the first run on the library's own stream
+    dpm.run(tables, [dpm.Job(p2, src, H, seed_of(99))], batches=a.batches).close()
+    p2.close()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for k in range(e2e_steps):
