@@ -95,6 +95,10 @@ struct PTables {
 struct ETables {
   SplineT<float> dedx[kMaxMat], itr1[kMaxMat], brem[kMaxMat], k1, moller;
   SplinePairT<float> di[kMaxMat];   // dE/dx and 1/lambda_1 in one record per bin (read in place)
+  // nominal density and Moller scaling of each material: shared memory serves
+  // lanes in different materials in one access, the kernel parameters would
+  // serialise them
+  float density[kMaxMat], mollerScale[kMaxMat];
 };
 
 __device__ __forceinline__ SplineT<float> Rebase(const SplineT<float>& s, const float* gbase, float* sbase) {
@@ -112,6 +116,8 @@ __device__ void StageElectronTables(const DevTables<float>& T, float* sdata, ETa
       et->itr1[m] = Rebase(T.itr1[m], T.elecBase, sdata);
       et->brem[m] = Rebase(T.brem[m], T.elecBase, sdata);
       et->di[m] = T.di[m];   // read in place
+      et->density[m] = T.density[m];
+      et->mollerScale[m] = T.mollerScale[m];
     }
     et->k1 = Rebase(T.k1, T.elecBase, sdata);
     et->moller = Rebase(T.moller, T.elecBase, sdata);
@@ -155,6 +161,10 @@ __device__ void BindElectronTables(const DevTables<float>& T, ETables* et) {
   }
   et->k1 = T.k1;
   et->moller = T.moller;
+  for (int m = 0; m < T.nmat; ++m) {
+    et->density[m] = T.density[m];
+    et->mollerScale[m] = T.mollerScale[m];
+  }
 }
 
 // spline value at e whose log (of the unclamped value) is le
@@ -1412,7 +1422,7 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
   } else {
     ++nsteps;
     const float ecut = T.ecut;
-    const float rho = VoxelRhoT<TF>(J, T, p.ix, p.iy, p.iz, im);
+    const float rho = ((TF & kGeomPlain) != 0) ? et.density[im] : VoxelRhoT<TF>(J, T, p.ix, p.iy, p.iz, im);
     step = s.sGeom;
     // dE/dx and 1/lambda_1 at E and at the mid-step energy, each pair from
     // one record; a step that no event shortens ends with the same mid-step
@@ -1424,7 +1434,7 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
     const float lm = __logf(emid);
     const DedxItr1 atMid = SplinePairLe(DiOf<TF>(a, et, im), emid, lm);
     float dTr1 = atMid.itr1 * rho;
-    const float dMol = s.invMol * T.mollerScale[im] * rho;
+    const float dMol = s.invMol * et.mollerScale[im] * rho;
     const float dBrem = SplineLe(BremOf<TF>(a, et, im), emid, lm) * rho;
     const float sBrem = s.nBrem / dBrem;
     if (sBrem < step) { step = sBrem; what = 1; }
