@@ -1084,7 +1084,6 @@ constexpr int8_t kMatUnknown = -2;   // the slot's voxel changed since its mater
 // lane reads or writes with one 128-bit access
 template <int NS>
 struct SlotArraysT {
-  static constexpr int kCount = NS;
   float4 pos[NS];   // offset in the voxel lx, ly, lz; kinetic energy
   float4 dir[NS];   // direction dx, dy, dz; voxel (PackVox, as float bits)
   float4 mfp[NS];   // nTr1, nMol, invMol, nBrem
