@@ -131,8 +131,8 @@ struct PhaseArgs {
   int plainGeom;               // 1: every job is a voxel phantom of material ids with nominal
                                //    densities (no slab preset, no per-voxel density array), and
                                //    the electron splines of all materials share one grid
-  JobF job0;                   // the first job's record (a single-job run reads it from the
-                               //    kernel parameters)
+  int soloJob;                 // 1: every particle of this launch belongs to one job, job0
+  JobF job0;                   // that job's record (read from the kernel parameters), else job 0's
 };
 
 // shared-memory depth tally of a block (slab jobs): bins of all jobs of a run

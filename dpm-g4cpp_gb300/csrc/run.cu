@@ -154,17 +154,27 @@ int AllocQueue(DevBuf& b, Queue& q, unsigned long long cap) {
 struct Chunk {
   std::vector<Segment> segP, segE, segAll;   // photon primaries, electron primaries, all by slot
   long long nP = 0, nE = 0, nslots = 0;
+  int job = -1;   // the chunk's only job, or -1 (none yet, or several)
+  bool mixed = false;
 };
+
+// a job with at least this many histories in a batch group fills the GPU on
+// its own: it gets chunks of its own, which run the single-job kernel forms
+constexpr long long kSoloJobHistories = 1LL << 20;
 
 // Cuts batches [b0, b1) (of B) of every job into chunks of at most `chunk`
 // histories. Batch b of job j runs as sub-job ((b - b0) << 8) | j, which
 // scores into its own tally slice; a chunk may span several batches. Jobs
 // come one after another (all their batches together), so that a chunk holds
-// few jobs and their tallies stay in L2.
+// few jobs and their tallies stay in L2; a job of kSoloJobHistories or more
+// starts and ends on chunk boundaries.
 std::vector<Chunk> PlanGroup(const dpmx_job* jobs, int njobs, int b0, int b1, int B, long long chunk) {
   std::vector<Chunk> out;
   Chunk cur;
   for (int j = 0; j < njobs; ++j) {
+    const long long N = jobs[j].histories;
+    const bool solo = N * b1 / B - N * b0 / B >= std::min(chunk, kSoloJobHistories);
+    if (solo && cur.nslots > 0) { out.push_back(cur); cur = Chunk(); }
     for (int b = b0; b < b1; ++b) {
       const long long N = jobs[j].histories;
       long long first = N * b / B;
@@ -179,12 +189,15 @@ std::vector<Chunk> PlanGroup(const dpmx_job* jobs, int njobs, int b0, int b1, in
         if (jobs[j].source.particle == 0) { s.prefix = cur.nP; cur.nP += take; cur.segP.push_back(s); }
         else { s.prefix = cur.nE; cur.nE += take; cur.segE.push_back(s); }
         cur.segAll.push_back(s);
+        if (cur.nslots == 0 && !cur.mixed) cur.job = j;
+        else if (cur.job != j) { cur.job = -1; cur.mixed = true; }
         cur.nslots += take;
         first += take;
         left -= take;
         if (cur.nslots == chunk) { out.push_back(cur); cur = Chunk(); }
       }
     }
+    if (solo && cur.nslots > 0) { out.push_back(cur); cur = Chunk(); }
   }
   if (cur.nslots > 0) out.push_back(cur);
   return out;
@@ -357,7 +370,9 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
           a.depthStride = maxNz;
           a.plainTally = plainTally ? 1 : 0;
           a.plainGeom = plainGeom ? 1 : 0;
-          if (njobs > 0) a.job0 = hj[0];
+          // a chunk of one job runs the single-job forms with that job's record
+          a.soloJob = c.job >= 0 ? 1 : 0;
+          if (njobs > 0) a.job0 = hj[c.job >= 0 ? c.job : 0];
           // photons of generation g; their electrons join generation g
           a.segs = sP; a.nsegs = int(c.segP.size()); a.nPrimaries = (g == 0) ? c.nP : 0;
           a.in = qp[g & 1]; a.inCount = cntP + g * kStripes;

@@ -312,9 +312,11 @@ constexpr int kTallyAgg = 1, kTallyPlain = 2;
 // splines of all materials lie on one grid at a fixed stride (DevTables::
 // elecUniform)
 constexpr int kGeomPlain = 4;
-// single-job form flag (electron block kernel): the run has one job, whose
-// record the kernel reads from its parameter block (constant-bank operands)
-// instead of loading it from shared memory at every use
+// single-job form flag (electron block kernel): every particle of the launch
+// belongs to one job (a single-job run, or a chunk of one job in a batched
+// run), whose record the kernel reads from its parameter block
+// (constant-bank operands) instead of loading it from shared memory at every
+// use
 constexpr int kSingleJob = 8;
 template <int TF>
 __device__ __forceinline__ const JobF& JobRec(const PhaseArgs& a, const JobF* jobs, int job) {
@@ -2332,7 +2334,7 @@ template <int NS>
 static void LaunchElectronPhaseBlockFor(const PhaseArgs& a, int blocks, cudaStream_t st) {
   const size_t smem = BlockPhaseSmemBytesFor<NS>(a.T, a.depthBins);
   // the single-job forms are built for the default slot count
-  const int f = KernelForm(a) | ((NS == kSlots && a.njobs == 1 && !a.aggregate) ? kSingleJob : 0);
+  const int f = KernelForm(a) | ((NS == kSlots && a.soloJob && !a.aggregate) ? kSingleJob : 0);
   switch (f) {
     case 0: ElectronPhaseB<0, NS><<<blocks, kBlockThreads, smem, st>>>(a); break;
     case 1: ElectronPhaseB<1, NS><<<blocks, kBlockThreads, smem, st>>>(a); break;
