@@ -27,12 +27,17 @@ int HistLen(int maxIz);
     }                                                                                          \
   } while (0)
 
-// a non-blocking stream owned by one call, destroyed with it
+// a non-blocking stream owned by one call, destroyed with it (after its work
+// has finished, also when the call leaves early on an error: buffers it used
+// may go back to a pool next)
 struct StreamGuard {
   cudaStream_t st = nullptr;
   cudaError_t Create() { return cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking); }
   ~StreamGuard() {
-    if (st) cudaStreamDestroy(st);
+    if (st) {
+      cudaStreamSynchronize(st);
+      cudaStreamDestroy(st);
+    }
   }
 };
 

@@ -38,6 +38,7 @@ constexpr int kGen = 32;                              // generations per chunk
 constexpr int kCntStride = (kGen + 1) * kStripes;
 constexpr int kCtrPerChunk = 2 * kCntStride + 2 * (kGen + 1) + 2;
 constexpr long long kMaxChunk = 1LL << 24;            // default upper bound of histories per chunk
+constexpr long long kLaneMinHistories = 1LL << 23;    // runs of at least this many histories get two chunk lanes
 constexpr int kQueuePerPrimary = 6;                   // queue entries per primary of a chunk and generation
 constexpr bool kInterleaveSlices = false;             // batch slices: per bin (true) or one after another
 
@@ -321,29 +322,64 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
   Segment* dsegs;
   if (int rc = buf.Get(&dsegs, segs.size())) return rc;
   if (!segs.empty()) CK(cudaMemcpyAsync(dsegs, segs.data(), segs.size() * sizeof(Segment), cudaMemcpyHostToDevice, st));
-  double *histE, *histE0;
-  if (int rc = buf.Get(&histE, maxSlots)) return rc;
-  if (int rc = buf.Get(&histE0, maxSlots)) return rc;
+  // chunk lanes: consecutive chunks alternate between two streams (forked
+  // and joined inside the captured graph), each lane with its own queues and
+  // energy-check slots, so that one chunk's phases fill the SMs the other's
+  // leave idle at the end of each phase (a phase-profiled run keeps one lane)
+  const int nlanes = (nchunks >= 2 && !profile) ? 2 : 1;
+  StreamGuard lane2;
+  if (nlanes == 2) CK(lane2.Create());
+  double *histE[2] = {nullptr, nullptr}, *histE0[2] = {nullptr, nullptr};
+  for (int l = 0; l < nlanes; ++l) {
+    if (int rc = buf.Get(&histE[l], maxSlots)) return rc;
+    if (int rc = buf.Get(&histE0[l], maxSlots)) return rc;
+  }
   unsigned long long* ctr;
   if (int rc = buf.Get(&ctr, nchunks * kCtrPerChunk)) return rc;
   CK(cudaMemsetAsync(ctr, 0, nchunks * kCtrPerChunk * sizeof(unsigned long long), st));
   // queues: double-buffered electrons and photons; a generation holds well
   // under kQueuePerPrimary secondaries of each kind per primary
   const unsigned long long cap = (unsigned long long)std::max<long long>(maxSlots * kQueuePerPrimary, 1 << 18);
-  Queue qe[2], qp[2];
-  for (int k = 0; k < 2; ++k) {
-    if (int rc = AllocQueue(buf, qe[k], cap)) return rc;
-    if (int rc = AllocQueue(buf, qp[k], cap)) return rc;
-  }
+  Queue qeL[2][2], qpL[2][2];   // [lane][generation parity]
+  for (int l = 0; l < nlanes; ++l)
+    for (int k = 0; k < 2; ++k) {
+      if (int rc = AllocQueue(buf, qeL[l][k], cap)) return rc;
+      if (int rc = AllocQueue(buf, qpL[l][k], cap)) return rc;
+    }
+  // fork and join events of the lanes, one pair per batch group
+  std::vector<cudaEvent_t> evFork, evJoin;
+  struct EventsGuard {
+    std::vector<cudaEvent_t>* v[2];
+    ~EventsGuard() {
+      for (auto* x : v)
+        for (cudaEvent_t e : *x) cudaEventDestroy(e);
+    }
+  } evGuard{{&evFork, &evJoin}};
+  if (nlanes == 2)
+    for (int gi = 0; gi < ngroups; ++gi) {
+      cudaEvent_t f, j;
+      CK(cudaEventCreateWithFlags(&f, cudaEventDisableTiming));
+      evFork.push_back(f);
+      CK(cudaEventCreateWithFlags(&j, cudaEventDisableTiming));
+      evJoin.push_back(j);
+    }
   const int blocks = nsm * cfg.blocksPerSM;
   const int eblocks = nsm * BlockPhaseBlocksPerSM();   // block-batched electron phase: one wave
   if (cfg.eblock) CK(PrepareBlockPhase(T->t32));
   CK(PreparePhotonPhase(T->t32));
   long long nl = 0;
-  auto enqueue = [&](cudaStream_t s) -> int {
+  auto enqueue = [&](cudaStream_t s0) -> int {
     size_t segCur = 0, ci = 0;
     for (int gi = 0; gi < ngroups; ++gi) {
+      if (nlanes == 2) {
+        CK(cudaEventRecord(evFork[gi], s0));
+        CK(cudaStreamWaitEvent(lane2.st, evFork[gi], 0));
+      }
       for (auto& c : plan[gi]) {
+        const int lane = int(ci % size_t(nlanes));
+        const cudaStream_t s = lane == 0 ? s0 : lane2.st;
+        Queue* qe = qeL[lane];
+        Queue* qp = qpL[lane];
         unsigned long long* cc = ctr + ci * kCtrPerChunk;
         unsigned long long* cntE = cc;                       // [gen][stripe]
         unsigned long long* cntP = cc + kCntStride;
@@ -354,15 +390,15 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
         const Segment* sP = dsegs + segCur;
         const Segment* sE = sP + c.segP.size();
         const Segment* sA = sE + c.segE.size();
-        CK(cudaMemsetAsync(histE, 0, c.nslots * sizeof(double), s));
+        CK(cudaMemsetAsync(histE[lane], 0, c.nslots * sizeof(double), s));
         for (int g = 0; g < kGen; ++g) {
           PhaseArgs a;
           std::memset(&a, 0, sizeof(a));
           a.T = T->t32;
           a.jobs = dj;
           a.njobs = njobs;
-          a.histE = histE;
-          a.histE0 = histE0;
+          a.histE = histE[lane];
+          a.histE0 = histE0[lane];
           a.overflow = ovf;
           a.fault = fault;
           a.aggregate = cfg.aggregate;
@@ -406,16 +442,21 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
           if (profile) CK(cudaEventRecord(evE.back(), s));
           ++nl;
         }
-        CK(LaunchEnergyCheck(histE, histE0, c.nslots, sA, int(c.segAll.size()), dj, s));
+        CK(LaunchEnergyCheck(histE[lane], histE0[lane], c.nslots, sA, int(c.segAll.size()), dj, s));
         ++nl;
         segCur += c.segP.size() + c.segE.size() + c.segAll.size();
         ++ci;
       }
+      if (nlanes == 2) {
+        CK(cudaEventRecord(evJoin[gi], lane2.st));
+        CK(cudaStreamWaitEvent(s0, evJoin[gi], 0));
+      }
       const int nslice = std::min(batches, (gi + 1) * R) - gi * R;
-      if (R == 1) CK(LaunchFold(tB, dose, dose2, total, s));
-      else CK(LaunchFoldSlices(tB, dose, dose2, total, binStride, sliceStride, nslice, s));
+      if (R == 1) CK(LaunchFold(tB, dose, dose2, total, s0));
+      else CK(LaunchFoldSlices(tB, dose, dose2, total, binStride, sliceStride, nslice, s0));
       ++nl;
     }
+    const cudaStream_t s = s0;
     // results into the per-job buffers, with their sums
     CK(cudaMemsetAsync(dsum, 0, njobs * sizeof(double), s));
     CK(cudaMemsetAsync(dlast, 0, njobs * sizeof(unsigned long long), s));
@@ -707,9 +748,10 @@ Cfg DefaultCfg(const dpmx_run_options* o, long long totalHist) {
   if (o && o->blocks_per_sm > 0) c.blocksPerSM = o->blocks_per_sm;
   if (o && o->chunk_histories > 0) c.chunk = o->chunk_histories;
   else {
-    // as few chunks as the bound allows, of equal size
+    // as few chunks as the bound allows, of equal size, and at least two
+    // (one per lane) for runs of kLaneMinHistories or more
     const long long n = std::max(1LL, totalHist);
-    const long long k = (n + kMaxChunk - 1) / kMaxChunk;
+    const long long k = std::max((n + kMaxChunk - 1) / kMaxChunk, n >= kLaneMinHistories ? 2LL : 1LL);
     c.chunk = std::max<long long>(1 << 14, (n + k - 1) / k);
   }
   if (o && o->tally_aggregate >= 0) c.aggregate = o->tally_aggregate;

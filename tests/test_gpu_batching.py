@@ -64,6 +64,23 @@ def test_schedule_invariance(tables_wlb, dpm):
         assert_same(tallies(r, 3), base)
 
 
+def test_chunk_lanes_equal_one_chunk(tables_wlb, dpm):
+    """a run of 2^23 or more histories is cut into at least two chunks that
+    run on two streams at once (chunk lanes); its tally equals the same job run
+    as one chunk up to the order of FP64 additions"""
+    wl = importlib.import_module("dpm-g4cpp_gb300.workloads")
+    ph = dpm.Phantom.voxels(tables_wlb, wl.precision_phantom(nx=64, ny=64, nz=128, v=4.0), 4.0)
+    n = 8_400_000
+    job = dpm.Job(ph, wl.precision_source(), n, 5)
+    two = dpm.run(tables_wlb, [job], batches=2)
+    assert two.config["chunk_histories"] == n // 2
+    one = dpm.run(tables_wlb, [job], batches=2, chunk_histories=n)
+    assert_same(tallies(two, 1), tallies(one, 1))
+    for r in (one, two):
+        st = r.stats(0)
+        assert st.lost == 0 and st.residual_violations == 0 and st.histories == n
+
+
 def test_autotuned_run_equals_its_configuration(tables_wlb, dpm):
     """the autotuner may pick the lane kernels, which draw other random numbers
     than the block kernels; a tuned run equals a plain run of the chosen shape"""
