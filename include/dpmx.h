@@ -113,7 +113,9 @@ typedef struct {
   int batches;               /* statistical batches for dose^2 (default 10) */
   int block_size;            /* threads per block (0: default / tuned) */
   int blocks_per_sm;         /* resident blocks per SM (0: default / tuned) */
-  long long chunk_histories; /* histories per transport chunk (0: default / tuned) */
+  long long chunk_histories; /* histories per transport chunk (0: as few equal chunks of at most
+                                2^24 as the run needs, and at least two for runs of 2^23 or more;
+                                a run of two or more chunks runs them on two streams) */
   int tally_aggregate;       /* FP32: -1 default, 0 plain atomics, 1 warp-aggregated */
   int use_graph;             /* FP32: capture each batch in a CUDA graph (default 1) */
   int tag_beamlets;          /* FP32: also tally dose per beamlet (influence matrix) */
