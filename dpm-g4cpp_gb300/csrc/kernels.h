@@ -147,9 +147,9 @@ cudaError_t LaunchElectronPhase(const PhaseArgs& a, int blocks, int threads, cud
 // dose += t, dose2 += t^2, t = 0 over n bins
 cudaError_t LaunchFold(double* t, double* dose, double* dose2, long long n, cudaStream_t st);
 // the same over m batch slices, bin i of slice b at t[i * binStride + b * sliceStride]:
-// dose[i] += sum_b t, dose2[i] += sum_b t^2
+// dose[i] += sum_b t, dose2[i] += sum_b t^2; clear: zero the slices after
 cudaError_t LaunchFoldSlices(double* t, double* dose, double* dose2, long long n, long long binStride,
-                             long long sliceStride, int m, cudaStream_t st);
+                             long long sliceStride, int m, bool clear, cudaStream_t st);
 // *sum += sum of d[0..n), *lastNz = max(*lastNz, 1 + index of the last non-zero bin)
 cudaError_t LaunchTallySummary(const double* d, long long n, double* sum, unsigned long long* lastNz,
                                cudaStream_t st);

@@ -456,7 +456,7 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
       }
       const int nslice = std::min(batches, (gi + 1) * R) - gi * R;
       if (R == 1) CK(LaunchFold(tB, dose, dose2, total, s0));
-      else CK(LaunchFoldSlices(tB, dose, dose2, total, binStride, sliceStride, nslice, s0));
+      else CK(LaunchFoldSlices(tB, dose, dose2, total, binStride, sliceStride, nslice, gi + 1 < ngroups, s0));
       ++nl;
     }
     const cudaStream_t s = s0;

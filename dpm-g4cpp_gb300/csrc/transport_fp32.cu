@@ -2072,6 +2072,11 @@ __global__ void FoldKernel(double* t, double* dose, double* dose2, long long n) 
   }
 }
 
+// adds the m batch slices of each bin to dose and dose^2 (slices in order);
+// ZERO: clears the slices for the next batch group (the last group's slices
+// are cleared by the next run's memset: without the stores the loads of a
+// bin's slices overlap, 0.26 against 0.33 ms for 10 slices of 4.2 M bins)
+template <bool ZERO>
 __global__ void FoldSlicesKernel(double* t, double* dose, double* dose2, long long n, long long binStride,
                                  long long sliceStride, int m) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
@@ -2083,7 +2088,7 @@ __global__ void FoldSlicesKernel(double* t, double* dose, double* dose2, long lo
       if (v != 0.0) {
         s += v;
         s2 += v * v;
-        ti[b * sliceStride] = 0.0;
+        if (ZERO) ti[b * sliceStride] = 0.0;
         any = true;
       }
     }
@@ -2365,9 +2370,10 @@ cudaError_t LaunchFold(double* t, double* dose, double* dose2, long long n, cuda
 }
 
 cudaError_t LaunchFoldSlices(double* t, double* dose, double* dose2, long long n, long long binStride,
-                             long long sliceStride, int m, cudaStream_t st) {
+                             long long sliceStride, int m, bool clear, cudaStream_t st) {
   const int blocks = int(std::min<long long>((n + 255) / 256, 152LL * 16));
-  FoldSlicesKernel<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(t, dose, dose2, n, binStride, sliceStride, m);
+  if (clear) FoldSlicesKernel<true><<<blocks > 0 ? blocks : 1, 256, 0, st>>>(t, dose, dose2, n, binStride, sliceStride, m);
+  else FoldSlicesKernel<false><<<blocks > 0 ? blocks : 1, 256, 0, st>>>(t, dose, dose2, n, binStride, sliceStride, m);
   return cudaGetLastError();
 }
 
