@@ -35,6 +35,27 @@ def test_nominal_density_reproduces_plain(tables_wlb, dpm, precision):
     np.testing.assert_allclose(a.tally(0)[0], b.tally(0)[0], rtol=1e-10, atol=1e-12)
 
 
+def test_nominal_densities_reproduce_plain_materials(tables_wlb, dpm):
+    """three materials at their nominal densities given per voxel: the run
+    takes the kernels' general geometry form (densities from the voxel array,
+    spline descriptors per material from shared memory) and must equal the
+    plain form of the same phantom (densities by material, descriptors of
+    material 0 moved by a fixed stride) up to the order of FP64 additions"""
+    m = np.zeros((32, 12, 12), dtype=np.uint8)
+    m[8:16] = 1                                    # lung
+    m[20:26] = 2                                   # bone
+    rho = np.zeros(m.shape, dtype=np.float32)
+    for k in range(3):
+        rho[m == k] = np.float32(tables_wlb.density(k))
+    src = dpm.Source(particle=0, e0=10.0, e1=10.0, shape=1, fx=10.0, fy=10.0)
+    a = dpm.run(tables_wlb, [dpm.Job(dpm.Phantom.voxels(tables_wlb, m, 2.0), src, 50000, 9)])
+    b = dpm.run(tables_wlb, [dpm.Job(dpm.Phantom.voxels(tables_wlb, m, 2.0, density=rho), src, 50000, 9)])
+    (da, qa, _), (db, qb, _) = a.tally(0), b.tally(0)
+    assert da.sum() > 0
+    np.testing.assert_allclose(da, db, rtol=1e-10, atol=1e-12 * da.max())
+    np.testing.assert_allclose(qa, qb, rtol=1e-10, atol=1e-12 * qa.max())
+
+
 def test_fp64_density_matches_oracle(tables_wlb, oracle_wlb, dpm):
     m, rho = _phantom()
     src = dpm.Source(particle=-1, e0=12.0, e1=12.0, shape=1, fx=12.0, fy=12.0)
