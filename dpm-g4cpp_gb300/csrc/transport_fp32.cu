@@ -220,13 +220,17 @@ __device__ __forceinline__ unsigned long long StripedIndex(const Queue& q, const
   return (unsigned long long)s * q.stripeCap + (item - prefix[s]);
 }
 
+// queue records are written once and read once, a generation's worth at a
+// time (hundreds of MB): loads and stores carry the streaming (evict-first)
+// hint, so that they do not push the phantom, tables and tallies out of L2
 __device__ __forceinline__ void LoadParticle(const Queue& q, unsigned long long i, PState& p) {
-  const uint32_t v = q.vox[i];
+  const uint32_t v = __ldcs(q.vox + i);
   p.ix = int(v & 0x7ffu); p.iy = int((v >> 11) & 0x7ffu); p.iz = int(v >> 22);
-  p.lx = q.lx[i]; p.ly = q.ly[i]; p.lz = q.lz[i];
-  p.dx = q.dx[i]; p.dy = q.dy[i]; p.dz = q.dz[i];
-  p.e = q.e[i];
-  p.hist = q.hist[i]; p.slot = q.slot[i]; p.ulo = q.uidlo[i]; p.uhi = q.uidhi[i]; p.meta = q.meta[i];
+  p.lx = __ldcs(q.lx + i); p.ly = __ldcs(q.ly + i); p.lz = __ldcs(q.lz + i);
+  p.dx = __ldcs(q.dx + i); p.dy = __ldcs(q.dy + i); p.dz = __ldcs(q.dz + i);
+  p.e = __ldcs(q.e + i);
+  p.hist = __ldcs(q.hist + i); p.slot = __ldcs(q.slot + i); p.ulo = __ldcs(q.uidlo + i); p.uhi = __ldcs(q.uidhi + i);
+  p.meta = __ldcs(q.meta + i);
 }
 
 // appends p to q with one atomic per group of converged lanes; returns false
@@ -247,11 +251,12 @@ __device__ __forceinline__ bool Append(const Queue& q, unsigned long long* count
     return false;
   }
   const unsigned long long i = (unsigned long long)stripe * q.stripeCap + j;
-  q.vox[i] = PackVox(p.ix, p.iy, p.iz);
-  q.lx[i] = p.lx; q.ly[i] = p.ly; q.lz[i] = p.lz;
-  q.dx[i] = p.dx; q.dy[i] = p.dy; q.dz[i] = p.dz;
-  q.e[i] = p.e;
-  q.hist[i] = p.hist; q.slot[i] = p.slot; q.uidlo[i] = p.ulo; q.uidhi[i] = p.uhi; q.meta[i] = p.meta;
+  __stcs(q.vox + i, PackVox(p.ix, p.iy, p.iz));
+  __stcs(q.lx + i, p.lx); __stcs(q.ly + i, p.ly); __stcs(q.lz + i, p.lz);
+  __stcs(q.dx + i, p.dx); __stcs(q.dy + i, p.dy); __stcs(q.dz + i, p.dz);
+  __stcs(q.e + i, p.e);
+  __stcs(q.hist + i, p.hist); __stcs(q.slot + i, p.slot); __stcs(q.uidlo + i, p.ulo); __stcs(q.uidhi + i, p.uhi);
+  __stcs(q.meta + i, p.meta);
   return true;
 }
 
