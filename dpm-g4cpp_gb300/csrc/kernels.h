@@ -131,6 +131,9 @@ struct PhaseArgs {
   int plainGeom;               // 1: every job is a voxel phantom of material ids with nominal
                                //    densities (no slab preset, no per-voxel density array), and
                                //    the electron splines of all materials share one grid
+  int slabForm;                // 1: every job is a slab preset whose depth bins fit the block's
+                               //    shared depth tally (depthBins > 0), no beamlet tally, and the
+                               //    electron splines of all materials share one grid
   int soloJob;                 // 1: every particle of this launch belongs to one job, job0
   JobF job0;                   // that job's record (read from the kernel parameters), else job 0's
 };

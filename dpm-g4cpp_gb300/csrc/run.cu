@@ -303,6 +303,12 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
     plainGeom = plainGeom && hj[j].matByDepth == 0 && hj[j].rho == nullptr;
   }
   plainGeom = plainGeom && T->t32.elecUniform != 0;
+  // slab presets whose depth tallies stay in the blocks' shared memory run
+  // the slab kernel forms
+  bool slabForm = depthBins > 0 && T->t32.elecUniform != 0;
+  for (int j = 0; j < njobs; ++j)
+    slabForm = slabForm && hj[j].tallyDepth == 1 && hj[j].matByDepth == 1 && hj[j].rho == nullptr &&
+               hj[j].btally == nullptr && hj[j].dbase >= 0;
   JobF* dj;
   if (int rc = buf.Get(&dj, njobs)) return rc;
   CK(cudaMemcpyAsync(dj, hj.data(), njobs * sizeof(JobF), cudaMemcpyHostToDevice, st));
@@ -409,6 +415,7 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
           a.depthStride = maxNz;
           a.plainTally = plainTally ? 1 : 0;
           a.plainGeom = plainGeom ? 1 : 0;
+          a.slabForm = slabForm ? 1 : 0;
           // a chunk of one job runs the single-job forms with that job's record
           a.soloJob = c.job >= 0 ? 1 : 0;
           if (njobs > 0) a.job0 = hj[c.job >= 0 ? c.job : 0];

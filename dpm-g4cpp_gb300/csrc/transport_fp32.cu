@@ -323,6 +323,10 @@ constexpr int kGeomPlain = 4;
 // (constant-bank operands) instead of loading it from shared memory at every
 // use
 constexpr int kSingleJob = 8;
+// slab form flags (set together): every job is a slab preset (materials by
+// depth, nominal densities, electron splines on one grid) whose depth bins
+// fit the block's shared-memory depth tally, and no beamlet tally
+constexpr int kTallyDepth = 16, kGeomSlab = 32;
 template <int TF>
 __device__ __forceinline__ const JobF& JobRec(const PhaseArgs& a, const JobF* jobs, int job) {
   if constexpr ((TF & kSingleJob) != 0) return a.job0;
@@ -331,7 +335,11 @@ __device__ __forceinline__ const JobF& JobRec(const PhaseArgs& a, const JobF* jo
 template <int TF>
 __device__ __forceinline__ void ScoreT(const JobF& J, uint32_t meta, int ix, int iy, int iz, uint32_t hist, float e,
                                        const DepthAcc& d) {
-  if constexpr ((TF & kTallyPlain) != 0) {
+  if constexpr ((TF & kTallyDepth) != 0) {
+    const int b = J.dbase + int(SliceOfSub(meta >> 2)) * d.sliceStride + iz;
+    atomicAdd(d.e + b, double(e));
+    atomicAdd(d.n + b, 1u);
+  } else if constexpr ((TF & kTallyPlain) != 0) {
     const uint32_t idx = (uint32_t(iz) * uint32_t(J.ny) + uint32_t(iy)) * uint32_t(J.nx) + uint32_t(ix);
     ScoreBin(J, SliceOfSub(meta >> 2), idx, double(e), TF & kTallyAgg);
   } else {
@@ -390,7 +398,10 @@ __device__ __forceinline__ int MaterialAt(const JobF& J, int ix, int iy, int iz)
 // the 3-D id array and the material's nominal density only)
 template <int TF>
 __device__ __forceinline__ int MaterialAtT(const JobF& J, int ix, int iy, int iz) {
-  if constexpr ((TF & kGeomPlain) != 0) {
+  if constexpr ((TF & kGeomSlab) != 0) {
+    const uint8_t m = __ldg(J.mat + iz);
+    return m == kVacuum ? -1 : int(m);
+  } else if constexpr ((TF & kGeomPlain) != 0) {
     const uint8_t m = __ldg(J.mat + (uint32_t(iz) * uint32_t(J.ny) + uint32_t(iy)) * uint32_t(J.nx) + uint32_t(ix));
     return m == kVacuum ? -1 : int(m);
   } else {
@@ -399,7 +410,7 @@ __device__ __forceinline__ int MaterialAtT(const JobF& J, int ix, int iy, int iz
 }
 template <int TF>
 __device__ __forceinline__ float VoxelRhoT(const JobF& J, const DevTables<float>& T, int ix, int iy, int iz, int im) {
-  if constexpr ((TF & kGeomPlain) != 0) return T.density[im];
+  if constexpr ((TF & (kGeomPlain | kGeomSlab)) != 0) return T.density[im];
   else return VoxelRho(J, T, ix, iy, iz, im);
 }
 
@@ -1369,7 +1380,7 @@ __device__ __forceinline__ void AnnihilateF(const PhaseArgs& a, const PState& p,
 // by im strides, else the block's shared copies
 template <int TF>
 __device__ __forceinline__ SplinePairT<float> DiOf(const PhaseArgs& a, const ETables& et, int im) {
-  if constexpr ((TF & kGeomPlain) != 0) {
+  if constexpr ((TF & (kGeomPlain | kGeomSlab)) != 0) {
     SplinePairT<float> d = a.T.di[0];
     d.p += im * a.T.diStride;
     return d;
@@ -1379,7 +1390,7 @@ __device__ __forceinline__ SplinePairT<float> DiOf(const PhaseArgs& a, const ETa
 }
 template <int TF>
 __device__ __forceinline__ SplineT<float> BremOf(const PhaseArgs& a, const ETables& et, int im) {
-  if constexpr ((TF & kGeomPlain) != 0) {
+  if constexpr ((TF & (kGeomPlain | kGeomSlab)) != 0) {
     SplineT<float> d = a.T.brem[0];
     d.p += im * a.T.bremStride;
     return d;
@@ -1428,7 +1439,7 @@ __device__ __forceinline__ int StepSlot(const PhaseArgs& a, const ETables& et, c
   } else {
     ++nsteps;
     const float ecut = T.ecut;
-    const float rho = ((TF & kGeomPlain) != 0) ? et.density[im] : VoxelRhoT<TF>(J, T, p.ix, p.iy, p.iz, im);
+    const float rho = ((TF & (kGeomPlain | kGeomSlab)) != 0) ? et.density[im] : VoxelRhoT<TF>(J, T, p.ix, p.iy, p.iz, im);
     step = s.sGeom;
     // dE/dx and 1/lambda_1 at E and at the mid-step energy, each pair from
     // one record; a step that no event shortens ends with the same mid-step
@@ -2271,11 +2282,12 @@ __global__ void __launch_bounds__(256) RingSelfTestKernel(int nslots, int rounds
 int ElectronPhaseSmemBytes(const DevTables<float>& T) { return int(T.elecCount * sizeof(float)); }
 
 // template flags of the block kernels a run's phase arguments select: 0 or
-// kTallyAgg (the general forms), kTallyPlain, kTallyPlain | kGeomPlain (warp
-// aggregation, measured slower on every workload, is built for the general
-// form only)
+// kTallyAgg (the general forms), kTallyPlain, kTallyPlain | kGeomPlain,
+// kTallyDepth | kGeomSlab (warp aggregation, measured slower on every
+// workload, is built for the general form only)
 static int KernelForm(const PhaseArgs& a) {
   if (a.aggregate) return kTallyAgg;
+  if (a.slabForm) return kTallyDepth | kGeomSlab;
   if (!a.plainTally) return 0;
   return a.plainGeom ? (kTallyPlain | kGeomPlain) : kTallyPlain;
 }
@@ -2293,6 +2305,7 @@ cudaError_t PreparePhotonPhase(const DevTables<float>& T) {
   if (e == cudaSuccess) e = cudaFuncSetAttribute(PhotonPhaseB<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(PhotonPhaseB<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(PhotonPhaseB<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(PhotonPhaseB<48>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
   return e;
 }
 
@@ -2301,10 +2314,11 @@ int PhotonBlockBlocksPerSM() { return kPBlockMinBlocks; }
 cudaError_t LaunchPhotonPhaseBlock(const PhaseArgs& a, int blocks, cudaStream_t st) {
   const size_t smem = PhotonBlockSmemBytes(a.depthBins);
   switch (KernelForm(a)) {
-    case 0: PhotonPhaseB<0><<<blocks, kPBlockThreads, smem, st>>>(a); break;
     case 1: PhotonPhaseB<1><<<blocks, kPBlockThreads, smem, st>>>(a); break;
     case 2: PhotonPhaseB<2><<<blocks, kPBlockThreads, smem, st>>>(a); break;
-    default: PhotonPhaseB<6><<<blocks, kPBlockThreads, smem, st>>>(a); break;
+    case 6: PhotonPhaseB<6><<<blocks, kPBlockThreads, smem, st>>>(a); break;
+    case 48: PhotonPhaseB<48><<<blocks, kPBlockThreads, smem, st>>>(a); break;
+    default: PhotonPhaseB<0><<<blocks, kPBlockThreads, smem, st>>>(a); break;   // the general form
   }
   return cudaGetLastError();
 }
@@ -2327,10 +2341,12 @@ static cudaError_t PrepareBlockPhaseFor(const DevTables<float>& T) {
   if (e == cudaSuccess) e = cudaFuncSetAttribute(ElectronPhaseB<1, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(ElectronPhaseB<2, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(ElectronPhaseB<6, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(ElectronPhaseB<48, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if constexpr (NS == kSlots) {
     if (e == cudaSuccess) e = cudaFuncSetAttribute(ElectronPhaseB<8, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(ElectronPhaseB<10, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(ElectronPhaseB<14, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(ElectronPhaseB<56, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   }
   return e;
 }
@@ -2346,13 +2362,15 @@ static void LaunchElectronPhaseBlockFor(const PhaseArgs& a, int blocks, cudaStre
   // the single-job forms are built for the default slot count
   const int f = KernelForm(a) | ((NS == kSlots && a.soloJob && !a.aggregate) ? kSingleJob : 0);
   switch (f) {
-    case 0: ElectronPhaseB<0, NS><<<blocks, kBlockThreads, smem, st>>>(a); break;
     case 1: ElectronPhaseB<1, NS><<<blocks, kBlockThreads, smem, st>>>(a); break;
     case 2: ElectronPhaseB<2, NS><<<blocks, kBlockThreads, smem, st>>>(a); break;
     case 6: ElectronPhaseB<6, NS><<<blocks, kBlockThreads, smem, st>>>(a); break;
     case 8: ElectronPhaseB<8, kSlots><<<blocks, kBlockThreads, smem, st>>>(a); break;
     case 10: ElectronPhaseB<10, kSlots><<<blocks, kBlockThreads, smem, st>>>(a); break;
-    default: ElectronPhaseB<14, kSlots><<<blocks, kBlockThreads, smem, st>>>(a); break;
+    case 14: ElectronPhaseB<14, kSlots><<<blocks, kBlockThreads, smem, st>>>(a); break;
+    case 48: ElectronPhaseB<48, NS><<<blocks, kBlockThreads, smem, st>>>(a); break;
+    case 56: ElectronPhaseB<56, kSlots><<<blocks, kBlockThreads, smem, st>>>(a); break;
+    default: ElectronPhaseB<0, NS><<<blocks, kBlockThreads, smem, st>>>(a); break;   // the general form
   }
 }
 
