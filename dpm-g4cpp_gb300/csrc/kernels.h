@@ -134,6 +134,7 @@ struct PhaseArgs {
   int slabForm;                // 1: every job is a slab preset whose depth bins fit the block's
                                //    shared depth tally (depthBins > 0), no beamlet tally, and the
                                //    electron splines of all materials share one grid
+  int tagForm;                 // 1: every job scores a 3-D voxel tally and a beamlet tally only
   int soloJob;                 // 1: every particle of this launch belongs to one job, job0
   JobF job0;                   // that job's record (read from the kernel parameters), else job 0's
 };

@@ -305,6 +305,10 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
   plainGeom = plainGeom && T->t32.elecUniform != 0;
   // slab presets whose depth tallies stay in the blocks' shared memory run
   // the slab kernel forms
+  // beamlet-tagged runs of 3-D voxel jobs run the tagged tally forms
+  bool tagForm = depthBins == 0 && njobs > 0;
+  for (int j = 0; j < njobs; ++j)
+    tagForm = tagForm && hj[j].tallyDepth == 0 && hj[j].steps == nullptr && hj[j].btally != nullptr;
   bool slabForm = depthBins > 0 && T->t32.elecUniform != 0;
   for (int j = 0; j < njobs; ++j)
     slabForm = slabForm && hj[j].tallyDepth == 1 && hj[j].matByDepth == 1 && hj[j].rho == nullptr &&
@@ -416,6 +420,7 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
           a.plainTally = plainTally ? 1 : 0;
           a.plainGeom = plainGeom ? 1 : 0;
           a.slabForm = slabForm ? 1 : 0;
+          a.tagForm = tagForm ? 1 : 0;
           // a chunk of one job runs the single-job forms with that job's record
           a.soloJob = c.job >= 0 ? 1 : 0;
           if (njobs > 0) a.job0 = hj[c.job >= 0 ? c.job : 0];

@@ -327,6 +327,9 @@ constexpr int kSingleJob = 8;
 // depth, nominal densities, electron splines on one grid) whose depth bins
 // fit the block's shared-memory depth tally, and no beamlet tally
 constexpr int kTallyDepth = 16, kGeomSlab = 32;
+// tagged tally form flag: every job scores a 3-D voxel tally and a beamlet
+// tally (influence matrix), nothing else
+constexpr int kTallyTag = 64;
 template <int TF>
 __device__ __forceinline__ const JobF& JobRec(const PhaseArgs& a, const JobF* jobs, int job) {
   if constexpr ((TF & kSingleJob) != 0) return a.job0;
@@ -339,6 +342,12 @@ __device__ __forceinline__ void ScoreT(const JobF& J, uint32_t meta, int ix, int
     const int b = J.dbase + int(SliceOfSub(meta >> 2)) * d.sliceStride + iz;
     atomicAdd(d.e + b, double(e));
     atomicAdd(d.n + b, 1u);
+  } else if constexpr ((TF & kTallyTag) != 0) {
+    const uint32_t idx = (uint32_t(iz) * uint32_t(J.ny) + uint32_t(iy)) * uint32_t(J.nx) + uint32_t(ix);
+    const double de = double(e);
+    ScoreBin(J, SliceOfSub(meta >> 2), idx, de, 0);
+    const long long nvox = (long long)J.nx * J.ny * J.nz;
+    atomicAdd(J.btally + (long long)(hist % uint32_t(J.nbeamlets)) * nvox + (long long)idx, de);
   } else if constexpr ((TF & kTallyPlain) != 0) {
     const uint32_t idx = (uint32_t(iz) * uint32_t(J.ny) + uint32_t(iy)) * uint32_t(J.nx) + uint32_t(ix);
     ScoreBin(J, SliceOfSub(meta >> 2), idx, double(e), TF & kTallyAgg);
@@ -2283,11 +2292,12 @@ int ElectronPhaseSmemBytes(const DevTables<float>& T) { return int(T.elecCount *
 
 // template flags of the block kernels a run's phase arguments select: 0 or
 // kTallyAgg (the general forms), kTallyPlain, kTallyPlain | kGeomPlain,
-// kTallyDepth | kGeomSlab (warp aggregation, measured slower on every
-// workload, is built for the general form only)
+// kTallyDepth | kGeomSlab, kTallyTag | kGeomPlain (warp aggregation,
+// measured slower on every workload, is built for the general form only)
 static int KernelForm(const PhaseArgs& a) {
   if (a.aggregate) return kTallyAgg;
   if (a.slabForm) return kTallyDepth | kGeomSlab;
+  if (a.tagForm) return a.plainGeom ? (kTallyTag | kGeomPlain) : 0;
   if (!a.plainTally) return 0;
   return a.plainGeom ? (kTallyPlain | kGeomPlain) : kTallyPlain;
 }
@@ -2306,6 +2316,7 @@ cudaError_t PreparePhotonPhase(const DevTables<float>& T) {
   if (e == cudaSuccess) e = cudaFuncSetAttribute(PhotonPhaseB<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(PhotonPhaseB<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(PhotonPhaseB<48>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(PhotonPhaseB<68>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
   return e;
 }
 
@@ -2318,6 +2329,7 @@ cudaError_t LaunchPhotonPhaseBlock(const PhaseArgs& a, int blocks, cudaStream_t 
     case 2: PhotonPhaseB<2><<<blocks, kPBlockThreads, smem, st>>>(a); break;
     case 6: PhotonPhaseB<6><<<blocks, kPBlockThreads, smem, st>>>(a); break;
     case 48: PhotonPhaseB<48><<<blocks, kPBlockThreads, smem, st>>>(a); break;
+    case 68: PhotonPhaseB<68><<<blocks, kPBlockThreads, smem, st>>>(a); break;
     default: PhotonPhaseB<0><<<blocks, kPBlockThreads, smem, st>>>(a); break;   // the general form
   }
   return cudaGetLastError();
@@ -2342,11 +2354,13 @@ static cudaError_t PrepareBlockPhaseFor(const DevTables<float>& T) {
   if (e == cudaSuccess) e = cudaFuncSetAttribute(ElectronPhaseB<2, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(ElectronPhaseB<6, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(ElectronPhaseB<48, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(ElectronPhaseB<68, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if constexpr (NS == kSlots) {
     if (e == cudaSuccess) e = cudaFuncSetAttribute(ElectronPhaseB<8, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(ElectronPhaseB<10, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(ElectronPhaseB<14, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(ElectronPhaseB<56, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(ElectronPhaseB<76, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   }
   return e;
 }
@@ -2370,6 +2384,8 @@ static void LaunchElectronPhaseBlockFor(const PhaseArgs& a, int blocks, cudaStre
     case 14: ElectronPhaseB<14, kSlots><<<blocks, kBlockThreads, smem, st>>>(a); break;
     case 48: ElectronPhaseB<48, NS><<<blocks, kBlockThreads, smem, st>>>(a); break;
     case 56: ElectronPhaseB<56, kSlots><<<blocks, kBlockThreads, smem, st>>>(a); break;
+    case 68: ElectronPhaseB<68, NS><<<blocks, kBlockThreads, smem, st>>>(a); break;
+    case 76: ElectronPhaseB<76, kSlots><<<blocks, kBlockThreads, smem, st>>>(a); break;
     default: ElectronPhaseB<0, NS><<<blocks, kBlockThreads, smem, st>>>(a); break;   // the general form
   }
 }

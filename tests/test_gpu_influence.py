@@ -30,6 +30,18 @@ def test_columns_sum_to_dose(setup):
     assert setup["A"].nnz > 0
 
 
+def test_tagged_dose_equals_untagged(setup, tables_wlb, dpm):
+    """the tagged run (kernels of the tagged tally form) and the same job
+    untagged (the plain form) give the same dose up to the order of FP64
+    additions: the beamlet tally does not touch the transport"""
+    res = setup["res"]
+    job = res._jobs[0]
+    plain = dpm.run(tables_wlb, [job], batches=4)
+    (dt, qt, _), (dp, qp, _) = res.tally(0), plain.tally(0)
+    np.testing.assert_allclose(dt, dp, rtol=1e-10, atol=1e-12 * dp.max())
+    np.testing.assert_allclose(qt, qp, rtol=1e-10, atol=1e-12 * qp.max())
+
+
 def test_products_match_cpu(setup):
     import torch
     A = setup["A"]
