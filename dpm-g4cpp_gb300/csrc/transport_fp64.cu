@@ -485,13 +485,17 @@ __device__ void RunHistories(const DevTables<double>& T, const G& geom, const So
   AccumulateCounters(cnt, dep, esc, e0sum, maxres, steps, viol, lost);
 }
 
-__global__ void __launch_bounds__(128) SlabKernel(DevTables<double> T, SlabGeo geom, SourceD src, long long first,
+// six blocks of 128 threads per SM (80 registers, 24 warps): the history
+// loop waits on its FP64 arithmetic and its local-memory secondary stack, and
+// more resident warps hide it (slab workload 1.35e6 against 9.0e5 histories/s
+// at 4 blocks and 128 registers; 8 blocks spill 1 KB)
+__global__ void __launch_bounds__(128, 6) SlabKernel(DevTables<double> T, SlabGeo geom, SourceD src, long long first,
                                                   long long n, uint64_t seed, double lbox, double* histEdep,
                                                   RunCounters* cnt) {
   RunHistories(T, geom, src, first, n, seed, true, lbox, histEdep, cnt);
 }
 
-__global__ void __launch_bounds__(128) GridKernel(DevTables<double> T, GridGeo geom, SourceD src, long long first,
+__global__ void __launch_bounds__(128, 6) GridKernel(DevTables<double> T, GridGeo geom, SourceD src, long long first,
                                                   long long n, uint64_t seed, double* histEdep, RunCounters* cnt) {
   RunHistories(T, geom, src, first, n, seed, false, 0.0, histEdep, cnt);
 }
