@@ -2,13 +2,15 @@
 // beamlet-tagged FP64 tally of an FP32 run, stored as CSR with FP32 values,
 // plus the same entries grouped by column (CSR of A^T), and the two products
 // of the differentiable dose D = A w:
-//   forward  y = A x     kRowLanes lanes per row (coalesced row segments),
+//   forward  y = A x     2-16 lanes per row by the matrix's mean row length,
 //                        x staged in shared memory, FP64 accumulation
 //   backward x = A^T y   CSR of A^T: `splits` blocks per column each reduce a
 //                        slice of the column, then one pass sums the slices
 //                        (no atomics: the result does not depend on timing)
-// Both are HBM-bound: each streams its CSR arrays once (4 B value + 4 B index
-// per entry + 8 B pointer per row) and gathers the dense vector from L2.
+// Each streams its CSR arrays once (4 B value + 4 B index per entry + 8 B
+// pointer per row) and gathers the dense vector from L2 or shared memory; the
+// FP64 conversion and multiply-add of every entry run on GB300's FP64 units
+// (1/64 of the FP32 rate), which bound them about as much as the traffic.
 #include <cstring>
 #include <memory>
 
@@ -38,9 +40,13 @@ __global__ void FillCsrKernel(const double* dense, long long nvox, int nb, doubl
   }
 }
 
-constexpr int kRowLanes = 16;      // lanes per row of y = A x
 constexpr int kColChunk = 2048;    // rows per block when grouping entries by column
 
+// y = A x with LANES lanes per row, chosen per matrix from its mean row length
+// (a lane sums its share of the row, then the lanes reduce); config 4's matrix
+// (53 entries a row) runs y = A x in 0.73 ms with 2 lanes, 0.77 with 4, 1.05
+// with 8, 1.18 with 16 and 0.83 with 1
+template <int LANES>
 __global__ void __launch_bounds__(256) SpmvKernel(const int64_t* rowPtr, const int32_t* col, const float* val,
                                                   long long rows, long long cols, const double* x, double* y,
                                                   int stageX) {
@@ -50,14 +56,15 @@ __global__ void __launch_bounds__(256) SpmvKernel(const int64_t* rowPtr, const i
     __syncthreads();
   }
   const double* xv = stageX ? xs : x;
-  const int sub = threadIdx.x % kRowLanes;
-  const long long first = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / kRowLanes;
-  const long long stride = (long long)gridDim.x * blockDim.x / kRowLanes;
+  const int sub = threadIdx.x % LANES;
+  const long long first = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / LANES;
+  const long long stride = (long long)gridDim.x * blockDim.x / LANES;
   for (long long i = first; i < rows; i += stride) {
     double s = 0.0;
     const int64_t e = rowPtr[i + 1];
-    for (int64_t k = rowPtr[i] + sub; k < e; k += kRowLanes) s += double(__ldg(val + k)) * xv[__ldg(col + k)];
-    for (int o = kRowLanes / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, kRowLanes);
+    for (int64_t k = rowPtr[i] + sub; k < e; k += LANES) s += double(__ldg(val + k)) * xv[__ldg(col + k)];
+#pragma unroll
+    for (int o = LANES / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, LANES);
     if (sub == 0) y[i] = s;
   }
 }
@@ -157,11 +164,19 @@ cudaError_t LaunchFillCsr(const double* dense, long long nvox, int nb, double th
   return cudaGetLastError();
 }
 cudaError_t LaunchSpmv(const int64_t* rowPtr, const int32_t* col, const float* val, long long rows, long long cols,
-                       const double* x, double* y, cudaStream_t st) {
+                       long long nnz, const double* x, double* y, cudaStream_t st) {
   const int stageX = cols <= 6144 ? 1 : 0;
-  const long long threads = rows * kRowLanes;
+  const double mean = rows > 0 ? double(nnz) / double(rows) : 0.0;
+  const int lanes = mean < 64 ? 2 : mean < 256 ? 4 : mean < 1024 ? 8 : 16;
+  const long long threads = rows * lanes;
   const int blocks = int(std::max<long long>(1, std::min<long long>((threads + 255) / 256, 152LL * 8)));
-  SpmvKernel<<<blocks, 256, stageX ? cols * sizeof(double) : 0, st>>>(rowPtr, col, val, rows, cols, x, y, stageX);
+  const size_t smem = stageX ? cols * sizeof(double) : 0;
+  switch (lanes) {
+    case 2: SpmvKernel<2><<<blocks, 256, smem, st>>>(rowPtr, col, val, rows, cols, x, y, stageX); break;
+    case 4: SpmvKernel<4><<<blocks, 256, smem, st>>>(rowPtr, col, val, rows, cols, x, y, stageX); break;
+    case 8: SpmvKernel<8><<<blocks, 256, smem, st>>>(rowPtr, col, val, rows, cols, x, y, stageX); break;
+    default: SpmvKernel<16><<<blocks, 256, smem, st>>>(rowPtr, col, val, rows, cols, x, y, stageX); break;
+  }
   return cudaGetLastError();
 }
 cudaError_t LaunchSpmvT(const dpmx_csr* a, const double* y, double* x, cudaStream_t st) {
@@ -278,7 +293,7 @@ int dpmx_csr_device(const dpmx_csr* a, const int64_t** row_ptr, const int32_t** 
 
 int dpmx_csr_spmv(const dpmx_csr* a, const double* x, double* y, void* stream) {
   if (!a || !x || !y) return Fail(DPMX_ERR_ARG, "null argument");
-  CK(LaunchSpmv(a->rowPtr, a->col, a->val, a->rows, a->cols, x, y, static_cast<cudaStream_t>(stream)));
+  CK(LaunchSpmv(a->rowPtr, a->col, a->val, a->rows, a->cols, a->nnz, x, y, static_cast<cudaStream_t>(stream)));
   return DPMX_OK;
 }
 

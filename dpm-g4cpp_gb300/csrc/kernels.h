@@ -185,7 +185,7 @@ cudaError_t LaunchCountNnz(const double* dense, long long nvox, int nb, double t
 cudaError_t LaunchFillCsr(const double* dense, long long nvox, int nb, double thr, const long long* rowPtr,
                           int32_t* col, float* val, cudaStream_t st);
 cudaError_t LaunchSpmv(const int64_t* rowPtr, const int32_t* col, const float* val, long long rows, long long cols,
-                       const double* x, double* y, cudaStream_t st);
+                       long long nnz, const double* x, double* y, cudaStream_t st);
 cudaError_t LaunchMaxAbs(const double* a, long long n, unsigned long long* outBits, cudaStream_t st);
 
 }  // namespace dpmx
