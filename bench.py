@@ -101,37 +101,55 @@ class ClockSampler:
 
     def __init__(self, gpu):
         self.gpu = gpu
-        self.rows = []
+        self.rows = []          # (arrival time, fields)
         self.proc = None
+        self.t0 = self.t1 = None
 
     def start(self):
+        """Starts sampling every 50 ms and returns once the first sample has
+        arrived, so that the timed region that follows is covered."""
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
         except OSError:
             self.proc = None
+            return
+        t = time.time()
+        while not self.rows and time.time() - t < 5.0 and self.proc.poll() is None:
+            time.sleep(0.01)
+
+    def begin(self):
+        self.t0 = time.time()
+
+    def end(self):
+        self.t1 = time.time()
 
     def _read(self):
         for line in self.proc.stdout:
-            self.rows.append([x.strip() for x in line.split(",")])
+            self.rows.append((time.time(), [x.strip() for x in line.split(",")]))
 
     def stop(self):
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        time.sleep(0.25)
+        time.sleep(0.1)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
-        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        # the samples taken between begin() and end() (a line arrives a few ms
+        # after its sample); all of them when the region was shorter than one period
+        rows = [r for t, r in self.rows if self.t0 is not None and self.t1 is not None and self.t0 <= t <= self.t1 + 0.02]
+        if not rows:
+            rows = [r for _, r in self.rows]
+        sm = [float(r[1]) for r in rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = set()
-        for r in self.rows:
+        for r in rows:
             for k, n in enumerate(names):
                 if len(r) > 5 + k and r[5 + k].lower().startswith("active"):
                     reasons.add(n)
@@ -279,6 +297,7 @@ def main():
     launches = 0
     stats = []
     torch.cuda.synchronize()
+    clocks.begin()
     for k in range(a.steps):
         with torch.cuda.stream(stream):
             flush.fill_(float(k))      # L2 flush between timed steps, on the timed stream, before its events
@@ -289,6 +308,7 @@ def main():
         stats.append(r.stats(0))
         r.close()
     torch.cuda.synchronize()
+    clocks.end()
     clk = clocks.stop()
     ms = sum(e0.elapsed_time(e1) for e0, e1 in ev)
     t = torch.tensor([ms], dtype=torch.float64, device="cuda")

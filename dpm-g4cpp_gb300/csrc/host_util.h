@@ -41,6 +41,24 @@ struct StreamGuard {
   }
 };
 
+// CUDA events made by one call, destroyed with it (also when the call leaves
+// early on an error)
+struct EventSet {
+  std::vector<cudaEvent_t> v;
+  cudaError_t Add(cudaEvent_t* out, unsigned flags = cudaEventDefault) {
+    cudaEvent_t e = nullptr;
+    const cudaError_t r = cudaEventCreateWithFlags(&e, flags);
+    if (r == cudaSuccess) {
+      v.push_back(e);
+      *out = e;
+    }
+    return r;
+  }
+  ~EventSet() {
+    for (cudaEvent_t e : v) cudaEventDestroy(e);
+  }
+};
+
 struct JobOut;
 // returns a job's device buffers to the scratch pool. A run has finished all
 // its own work on them when dpmx_run returns, so this waits for nothing; the

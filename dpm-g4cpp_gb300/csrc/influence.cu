@@ -197,6 +197,39 @@ cudaError_t LaunchMaxAbs(const double* a, long long n, unsigned long long* outBi
 
 using namespace dpmx;
 
+namespace {
+
+// stream-ordered temporaries of one call: freed on its stream where the call
+// frees them, or when it leaves early on an error
+struct AsyncTemps {
+  cudaStream_t st;
+  std::vector<void*> v;
+  explicit AsyncTemps(cudaStream_t s) : st(s) {}
+  template <class T> cudaError_t Get(T** p, size_t bytes) {
+    void* q = nullptr;
+    const cudaError_t e = cudaMallocAsync(&q, bytes, st);
+    if (e == cudaSuccess) {
+      v.push_back(q);
+      *p = static_cast<T*>(q);
+    }
+    return e;
+  }
+  cudaError_t Free(void* p) {
+    for (void*& q : v)
+      if (q == p) {
+        q = nullptr;
+        return cudaFreeAsync(p, st);
+      }
+    return cudaSuccess;
+  }
+  ~AsyncTemps() {
+    for (void* q : v)
+      if (q) cudaFreeAsync(q, st);
+  }
+};
+
+}  // namespace
+
 extern "C" {
 
 int dpmx_influence_build(const dpmx_result* r, int job, double threshold, dpmx_csr** out) {
@@ -209,15 +242,16 @@ int dpmx_influence_build(const dpmx_result* r, int job, double threshold, dpmx_c
   StreamGuard sg;
   CK(sg.Create());
   const cudaStream_t st = sg.st;
+  AsyncTemps tmps(st);
   const long long nvox = o.nvox;
   const int nb = o.nbeamlets;
   unsigned long long* dmax = nullptr;
-  CK(cudaMallocAsync(&dmax, sizeof(unsigned long long), st));
+  CK(tmps.Get(&dmax, sizeof(unsigned long long)));
   CK(cudaMemsetAsync(dmax, 0, sizeof(unsigned long long), st));
   CK(LaunchMaxAbs(o.d_btally, nvox * nb, dmax, st));
   unsigned long long bits = 0;
   CK(cudaMemcpyAsync(&bits, dmax, sizeof(bits), cudaMemcpyDeviceToHost, st));
-  CK(cudaFreeAsync(dmax, st));
+  CK(tmps.Free(dmax));
   CK(cudaStreamSynchronize(st));
   double mx;
   std::memcpy(&mx, &bits, sizeof(mx));
@@ -227,16 +261,16 @@ int dpmx_influence_build(const dpmx_result* r, int job, double threshold, dpmx_c
   a->cols = nb;
   CK(cudaMalloc(&a->rowPtr, (nvox + 1) * sizeof(int64_t)));
   long long* cnt = nullptr;
-  CK(cudaMallocAsync(&cnt, (nvox + 1) * sizeof(long long), st));
+  CK(tmps.Get(&cnt, (nvox + 1) * sizeof(long long)));
   CK(cudaMemsetAsync(cnt, 0, (nvox + 1) * sizeof(long long), st));
   CK(LaunchCountNnz(o.d_btally, nvox, nb, thr, cnt, st));
   size_t tmpBytes = 0;
   cub::DeviceScan::ExclusiveSum(nullptr, tmpBytes, cnt, reinterpret_cast<long long*>(a->rowPtr), nvox + 1, st);
   void* tmp = nullptr;
-  CK(cudaMallocAsync(&tmp, tmpBytes, st));
+  CK(tmps.Get(&tmp, tmpBytes));
   CK(cub::DeviceScan::ExclusiveSum(tmp, tmpBytes, cnt, reinterpret_cast<long long*>(a->rowPtr), nvox + 1, st));
-  CK(cudaFreeAsync(tmp, st));
-  CK(cudaFreeAsync(cnt, st));
+  CK(tmps.Free(tmp));
+  CK(tmps.Free(cnt));
   long long nnz = 0;
   CK(cudaMemcpyAsync(&nnz, a->rowPtr + nvox, sizeof(long long), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
@@ -249,15 +283,15 @@ int dpmx_influence_build(const dpmx_result* r, int job, double threshold, dpmx_c
   const long long nblk = (long long)nb * nchunks;
   long long* ccnt = nullptr;
   long long* coff = nullptr;
-  CK(cudaMallocAsync(&ccnt, nblk * sizeof(long long), st));
-  CK(cudaMallocAsync(&coff, nblk * sizeof(long long), st));
+  CK(tmps.Get(&ccnt, nblk * sizeof(long long)));
+  CK(tmps.Get(&coff, nblk * sizeof(long long)));
   ColCountKernel<<<int(nblk), 256, 0, st>>>(o.d_btally, nvox, nchunks, thr, ccnt);
   CK(cudaGetLastError());
   tmpBytes = 0;
   cub::DeviceScan::ExclusiveSum(nullptr, tmpBytes, ccnt, coff, nblk, st);
-  CK(cudaMallocAsync(&tmp, tmpBytes, st));
+  CK(tmps.Get(&tmp, tmpBytes));
   CK(cub::DeviceScan::ExclusiveSum(tmp, tmpBytes, ccnt, coff, nblk, st));
-  CK(cudaFreeAsync(tmp, st));
+  CK(tmps.Free(tmp));
   CK(cudaMalloc(&a->colPtr, (nb + 1) * sizeof(int64_t)));
   CK(cudaMalloc(&a->rowT, std::max<long long>(1, nnz) * sizeof(int32_t)));
   CK(cudaMalloc(&a->valT, std::max<long long>(1, nnz) * sizeof(float)));
@@ -268,8 +302,8 @@ int dpmx_influence_build(const dpmx_result* r, int job, double threshold, dpmx_c
   // enough column slices to fill the GPU with blocks of A^T y
   a->splits = int(std::max<long long>(1, (4LL * 152 * 4 + nb - 1) / nb));
   CK(cudaMalloc(&a->partial, (long long)nb * a->splits * sizeof(double)));
-  CK(cudaFreeAsync(ccnt, st));
-  CK(cudaFreeAsync(coff, st));
+  CK(tmps.Free(ccnt));
+  CK(tmps.Free(coff));
   CK(cudaStreamSynchronize(st));
   *out = a.release();
   return DPMX_OK;

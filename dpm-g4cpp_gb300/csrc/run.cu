@@ -359,21 +359,16 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
       if (int rc = AllocQueue(buf, qeL[l][k], cap)) return rc;
       if (int rc = AllocQueue(buf, qpL[l][k], cap)) return rc;
     }
+  // every event of the run (lane fork and join, phase timing, run timing)
+  EventSet evs;
   // fork and join events of the lanes, one pair per batch group
   std::vector<cudaEvent_t> evFork, evJoin;
-  struct EventsGuard {
-    std::vector<cudaEvent_t>* v[2];
-    ~EventsGuard() {
-      for (auto* x : v)
-        for (cudaEvent_t e : *x) cudaEventDestroy(e);
-    }
-  } evGuard{{&evFork, &evJoin}};
   if (nlanes == 2)
     for (int gi = 0; gi < ngroups; ++gi) {
       cudaEvent_t f, j;
-      CK(cudaEventCreateWithFlags(&f, cudaEventDisableTiming));
+      CK(evs.Add(&f, cudaEventDisableTiming));
       evFork.push_back(f);
-      CK(cudaEventCreateWithFlags(&j, cudaEventDisableTiming));
+      CK(evs.Add(&j, cudaEventDisableTiming));
       evJoin.push_back(j);
     }
   const int blocks = nsm * cfg.blocksPerSM;
@@ -432,8 +427,8 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
           a.head = headP + g;
           if (profile) {
             evP.resize(evP.size() + 2);
-            CK(cudaEventCreate(&evP[evP.size() - 2]));
-            CK(cudaEventCreate(&evP.back()));
+            CK(evs.Add(&evP[evP.size() - 2]));
+            CK(evs.Add(&evP.back()));
             CK(cudaEventRecord(evP[evP.size() - 2], s));
           }
           if (cfg.pblock) CK(LaunchPhotonPhaseBlock(a, nsm * PhotonBlockBlocksPerSM(), s));
@@ -448,8 +443,8 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
           a.head = headE + g;
           if (profile) {
             evE.resize(evE.size() + 2);
-            CK(cudaEventCreate(&evE[evE.size() - 2]));
-            CK(cudaEventCreate(&evE.back()));
+            CK(evs.Add(&evE[evE.size() - 2]));
+            CK(evs.Add(&evE.back()));
             CK(cudaEventRecord(evE[evE.size() - 2], s));
           }
           if (cfg.eblock) CK(LaunchElectronPhaseBlock(a, eblocks, cfg.eslots, s));
@@ -486,8 +481,8 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
   };
 
   cudaEvent_t e0, e1;
-  CK(cudaEventCreate(&e0));
-  CK(cudaEventCreate(&e1));
+  CK(evs.Add(&e0));
+  CK(evs.Add(&e1));
   int rc = DPMX_OK;
   if (useGraph) {
     // The executable graph of the calling thread's previous run is kept: a new
@@ -508,7 +503,11 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
     if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
     CK(ce);
     bool updated = false;
-    if (tlExec && tlDev == dev) {
+    if (tlExec && tlDev != dev) {   // made on another device: not updatable here
+      cudaGraphExecDestroy(tlExec);
+      tlExec = nullptr;
+    }
+    if (tlExec) {
       cudaGraphExecUpdateResultInfo info;
       if (cudaGraphExecUpdate(tlExec, graph, &info) == cudaSuccess) {
         updated = true;
@@ -537,8 +536,6 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
   }
   float fms = 0.f;
   CK(cudaEventElapsedTime(&fms, e0, e1));
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   *ms = fms;
   *launches = nl;
   // results: leftovers beyond the last generation and queue overflows are losses
@@ -569,8 +566,6 @@ int RunFp32(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
       CK(cudaEventElapsedTime(&x, evP[k], evP[k + 1]));
       tp += x;
     }
-    for (auto e : evE) cudaEventDestroy(e);
-    for (auto e : evP) cudaEventDestroy(e);
     double hist = 0, primE = 0, primP = 0;
     for (int j = 0; j < njobs; ++j) {
       hist += double(jobs[j].histories);
@@ -632,9 +627,10 @@ int RunFp64(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
   for (auto& o : outs) maxT = std::max(maxT, o.tallySize);
   double* tB;
   if (int rc = buf.Get(&tB, maxT)) return rc;
+  EventSet evs;
   cudaEvent_t e0, e1;
-  CK(cudaEventCreate(&e0));
-  CK(cudaEventCreate(&e1));
+  CK(evs.Add(&e0));
+  CK(evs.Add(&e1));
   CK(cudaEventRecord(e0, st));
   long long nl = 0;
   long long histOff = 0;
@@ -674,8 +670,6 @@ int RunFp64(const dpmx_tables* T, const dpmx_job* jobs, int njobs, int batches, 
   CK(cudaStreamSynchronize(st));
   float fms = 0.f;
   CK(cudaEventElapsedTime(&fms, e0, e1));
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   *ms = fms;
   *launches = nl;
   std::vector<RunCounters> hcnt(njobs);
