@@ -273,7 +273,7 @@ __global__ void __launch_bounds__(256) MaxMaterialKernel(const uint8_t* m, unsig
   const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
   for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += stride) {
     const uint4 w = q[i];
-    best = max(max(MaxNonVacuum(w.x), MaxNonVacuum(w.y)), max(MaxNonVacuum(w.z), MaxNonVacuum(w.w)));
+    best = max(best, max(max(MaxNonVacuum(w.x), MaxNonVacuum(w.y)), max(MaxNonVacuum(w.z), MaxNonVacuum(w.w))));
   }
   if (blockIdx.x == 0 && threadIdx.x < n - n16 * 16) {   // the last n % 16 bytes
     const unsigned v = m[n16 * 16 + threadIdx.x];

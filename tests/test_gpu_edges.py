@@ -122,10 +122,12 @@ def test_photon_kernels_give_the_same_histories(tables_wlb, dpm, kind):
     assert close.mean() > 0.999, close.mean()
 
 
-@pytest.mark.parametrize("shape", [(16, 16, 16), (7, 5, 3), (1, 1, 1), (33, 17, 9)])
+@pytest.mark.parametrize("shape", [(16, 16, 16), (7, 5, 3), (1, 1, 1), (33, 17, 9), (40, 512, 512)])
 def test_material_ids_checked_on_upload(tables_wlb, dpm, shape):
     """ids beyond the data set are refused wherever they sit (also in the
-    last bytes of an array whose size is no multiple of 16); vacuum is not"""
+    last bytes of an array whose size is no multiple of 16, and in an array
+    of 10.5M voxels, where each thread of the check reads several 16-byte
+    words); vacuum is not"""
     nmat = tables_wlb.num_materials
     m = np.zeros(shape, dtype=np.uint8)
     m.reshape(-1)[-1] = 255
