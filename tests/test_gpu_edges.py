@@ -5,6 +5,8 @@
   :282-287, :495-500), so nothing is scored behind a vacuum layer;
 * the block-local depth tally of slab jobs gives the same dose as global
   atomics (a history's deposits do not depend on the batching);
+* phantoms at the largest dimensions (2047 x 2047 x 1023 voxels: the packed
+  voxel index), beams into their last column and through their last planes;
 * the full-size precision workload (128x128x256 x 2 mm, 1e7 histories):
   every history conserves energy, nothing is lost, and the FP32 dose agrees
   with the FP64 plain form within statistics.
@@ -140,3 +142,36 @@ def test_material_ids_checked_on_upload(tables_wlb, dpm, shape):
         with pytest.raises(dpm.DpmxError) as e:
             dpm.Phantom.voxels(tables_wlb, bad, 2.0)
         assert e.value.code == dpm.ERR_ARG
+
+
+@pytest.mark.parametrize("shape,particle", [((1023, 2, 2047), 0), ((2, 2047, 2047), -1)])
+def test_largest_phantom_dimensions(tables_wlb, dpm, shape, particle):
+    """phantoms at the largest dimensions (2047 voxels in x and y, 1023 in z:
+    the 11/11/10-bit packed voxel index of the queues and slots), a 10 MeV
+    pencil beam into the last column (x = 2046, and y = 2046 on the wide
+    phantom): photons through 1023 planes, electrons through 2. Both forms
+    conserve energy, lose nothing, score in the beam's column (and, on the
+    deep phantom, in its last planes) and agree on the deposited energy."""
+    nz, ny, nx = shape
+    ph = dpm.Phantom.voxels(tables_wlb, np.zeros(shape, dtype=np.uint8), 1.0)
+    cx = 0.5 * nx - 0.5                                           # centre of column nx - 1 [mm]
+    cy = 0.5 * ny - 0.5 if ny > 2 else 0.0
+    src = dpm.Source(particle=particle, e0=10.0, e1=10.0, shape=0, cx=cx, cy=cy)
+    n = 20000
+    edep = {}
+    for prec in (dpm.FP64_PLAIN, dpm.FP32_EVENT):
+        r = dpm.run(tables_wlb, [dpm.Job(ph, src, n, 21)], precision=prec, batches=4)
+        st = r.stats(0)
+        assert st.lost == 0 and st.residual_violations == 0
+        assert abs(st.edep + st.escaped - st.primary_energy) <= 1e-6 * st.primary_energy
+        d = r.tally(0)[0].reshape(shape)
+        assert d.sum() > 0.0
+        assert d[:, :, nx - 3:].sum() > 0.5 * d.sum()            # the beam's column and its neighbours
+        if ny > 2:
+            assert d[:, ny - 3:, :].sum() > 0.5 * d.sum()
+        if nz > 2:
+            assert d[nz - 24:].sum() > 0.0                       # the beam reaches the last planes
+        edep[prec] = st.edep / n
+    # the two forms' mean deposits per history agree within a few standard
+    # errors (the deposit of one history lies in [0, 10] MeV)
+    assert abs(edep[dpm.FP32_EVENT] - edep[dpm.FP64_PLAIN]) < 4 * 10.0 * np.sqrt(2.0 / n)
