@@ -730,7 +730,7 @@ int CheckJobs(const dpmx_tables* t, const dpmx_job* jobs, int njobs) {
   for (int j = 0; j < njobs; ++j) {
     const dpmx_job& J = jobs[j];
     if (!J.phantom || J.phantom->tables != t) return Fail(DPMX_ERR_ARG, "job phantom missing or built on other tables");
-    if (J.histories < 0 || J.first_history < 0 || J.first_history + J.histories > 0xffffffffLL)
+    if (J.histories < 0 || J.first_history < 0 || J.first_history + J.histories > (1LL << 32))
       return Fail(DPMX_ERR_ARG, "history indices must lie in [0, 2^32)");
     const dpmx_source& s = J.source;
     if (s.particle != -1 && s.particle != 0) return Fail(DPMX_ERR_ARG, "source particle must be -1 (e-) or 0 (photon)");

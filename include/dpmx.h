@@ -105,7 +105,9 @@ typedef struct {
   uint64_t seed;
   long long first_history;   /* index of the job's first history: history h always
                                 uses random stream h, so a job split into ranges
-                                (e.g. across GPUs) sums to the unsplit result */
+                                (e.g. across GPUs) sums to the unsplit result;
+                                indices lie in [0, 2^32): first_history +
+                                histories <= 2^32, else DPMX_ERR_ARG */
 } dpmx_job;
 
 typedef struct {

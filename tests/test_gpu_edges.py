@@ -175,3 +175,30 @@ def test_largest_phantom_dimensions(tables_wlb, dpm, shape, particle):
     # the two forms' mean deposits per history agree within a few standard
     # errors (the deposit of one history lies in [0, 10] MeV)
     assert abs(edep[dpm.FP32_EVENT] - edep[dpm.FP64_PLAIN]) < 4 * 10.0 * np.sqrt(2.0 / n)
+
+
+def test_history_index_range(tables_wlb, dpm):
+    """a history's index is the counter of its random streams, so indices lie
+    in [0, 2^32): jobs beyond are refused; the last 2000 indices run in both
+    forms, and split into two jobs they give the one job's dose (the FP64
+    form to summation order, the FP32 form within its rounding)"""
+    m = np.zeros((24, 12, 12), dtype=np.uint8)
+    ph = dpm.Phantom.voxels(tables_wlb, m, 2.0)
+    src = dpm.Source(particle=0, e0=6.0, e1=6.0, shape=1, fx=10.0, fy=10.0)
+    top = 2 ** 32
+    for bad in (dict(histories=1001, first_history=top - 1000), dict(histories=-1), dict(histories=10, first_history=-5)):
+        with pytest.raises(dpm.DpmxError) as e:
+            dpm.run(tables_wlb, [dpm.Job(ph, src, seed=3, **bad)])
+        assert e.value.code == dpm.ERR_ARG
+    for prec in (dpm.FP64_PLAIN, dpm.FP32_EVENT):
+        one = dpm.run(tables_wlb, [dpm.Job(ph, src, 2000, 3, first_history=top - 2000)], precision=prec, batches=2)
+        two = dpm.run(tables_wlb, [dpm.Job(ph, src, 1000, 3, first_history=top - 2000),
+                                   dpm.Job(ph, src, 1000, 3, first_history=top - 1000)], precision=prec, batches=1)
+        st = one.stats(0)
+        assert st.histories == 2000 and st.lost == 0 and st.residual_violations == 0
+        assert abs(st.edep + st.escaped - st.primary_energy) <= 1e-6 * st.primary_energy
+        d1 = one.tally(0)[0]
+        d2 = two.tally(0)[0] + two.tally(1)[0]
+        assert d1.sum() > 0.0
+        tol = 1e-10 if prec == dpm.FP64_PLAIN else 1e-4
+        np.testing.assert_allclose(d2, d1, rtol=tol, atol=tol * d1.max())
