@@ -7,6 +7,7 @@
   atomics (a history's deposits do not depend on the batching);
 * phantoms at the largest dimensions (2047 x 2047 x 1023 voxels: the packed
   voxel index), beams into their last column and through their last planes;
+  voxels of 0.05 and 20 mm; history indices up to 2^32 - 1;
 * the full-size precision workload (128x128x256 x 2 mm, 1e7 histories):
   every history conserves energy, nothing is lost, and the FP32 dose agrees
   with the FP64 plain form within statistics.
@@ -202,3 +203,29 @@ def test_history_index_range(tables_wlb, dpm):
         assert d1.sum() > 0.0
         tol = 1e-10 if prec == dpm.FP64_PLAIN else 1e-4
         np.testing.assert_allclose(d2, d1, rtol=tol, atol=tol * d1.max())
+
+
+@pytest.mark.parametrize("v,e,shape", [(0.05, 2.0, (40, 12, 12)), (20.0, 12.0, (12, 6, 6))])
+def test_voxel_size_extremes(tables_wlb, dpm, v, e, shape):
+    """0.05 mm voxels (a 2 MeV electron crosses dozens in one condensed-history
+    step: the FP32 form's voxel-local offsets and boundary pushes at their
+    finest) and 20 mm voxels (a 12 MeV electron's track fits in three): the
+    FP32 form's dose agrees with the FP64 form's voxel by voxel"""
+    from importlib import import_module
+    dc = import_module("dpm-g4cpp_gb300.dosecheck")
+    ph = dpm.Phantom.voxels(tables_wlb, np.zeros(shape, dtype=np.uint8), v)
+    src = dpm.Source(particle=-1, e0=e, e1=e)
+    est = {}
+    for prec, n in ((dpm.FP64_PLAIN, 40000), (dpm.FP32_EVENT, 400000)):
+        r = dpm.run(tables_wlb, [dpm.Job(ph, src, n, 8)], precision=prec, batches=10)
+        st = r.stats(0)
+        assert st.lost == 0 and st.residual_violations == 0
+        assert abs(st.edep + st.escaped - st.primary_energy) <= 1e-6 * st.primary_energy
+        d, q, _ = r.tally(0)
+        est[prec] = dc.batch_estimate(d, q, 10, n)
+    m32, s32 = est[dpm.FP32_EVENT]
+    m64, s64 = est[dpm.FP64_PLAIN]
+    c = dc.compare(m32, s32, 10, m64, s64, 10)
+    assert c["voxels"] >= 10
+    assert c["within_2sigma"] > 0.88, c
+    assert abs(c["mean_signed_pct"]) < 1.0, c
