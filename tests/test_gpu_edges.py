@@ -7,7 +7,8 @@
   atomics (a history's deposits do not depend on the batching);
 * phantoms at the largest dimensions (2047 x 2047 x 1023 voxels: the packed
   voxel index), beams into their last column and through their last planes;
-  voxels of 0.05 and 20 mm; history indices up to 2^32 - 1;
+  voxels of 0.05 and 20 mm; history indices up to 2^32 - 1; sources at the
+  ends of the data set's energy range and every spectrum form;
 * the full-size precision workload (128x128x256 x 2 mm, 1e7 histories):
   every history conserves energy, nothing is lost, and the FP32 dose agrees
   with the FP64 plain form within statistics.
@@ -229,3 +230,30 @@ def test_voxel_size_extremes(tables_wlb, dpm, v, e, shape):
     assert c["voxels"] >= 10
     assert c["within_2sigma"] > 0.88, c
     assert abs(c["mean_signed_pct"]) < 1.0, c
+
+
+@pytest.mark.parametrize("particle,spectrum,e0,e1", [
+    (0, 0, 0.0501, 0.0501),    # photons just above the photon cut (0.05 MeV)
+    (0, 0, 20.99, 20.99),      # photons just below the top of the tables (21 MeV)
+    (-1, 0, 0.2001, 0.2001),   # electrons just above the electron cut (0.2 MeV)
+    (-1, 0, 20.99, 20.99),     # electrons just below the top of the tables
+    (0, 2, 0.5, 20.0),         # falling spectrum p(E) ~ (e1 - E)
+    (-1, 1, 20.0, 1.0),        # uniform spectrum given high to low
+])
+def test_source_energy_extremes(tables_wlb, dpm, particle, spectrum, e0, e1):
+    """sources at the ends of the data set's energy range and the other
+    spectrum forms: both forms conserve every history's energy, lose
+    nothing, and agree on the mean deposit per history"""
+    ph = dpm.Phantom.voxels(tables_wlb, np.zeros((64, 32, 32), dtype=np.uint8), 2.0)
+    src = dpm.Source(particle=particle, spectrum=spectrum, e0=e0, e1=e1, shape=1, fx=20.0, fy=20.0)
+    mean = {}
+    for prec, n in ((dpm.FP64_PLAIN, 20000), (dpm.FP32_EVENT, 200000)):
+        r = dpm.run(tables_wlb, [dpm.Job(ph, src, n, 17)], precision=prec, batches=4)
+        st = r.stats(0)
+        assert st.histories == n and st.lost == 0 and st.residual_violations == 0
+        assert abs(st.edep + st.escaped - st.primary_energy) <= 1e-6 * st.primary_energy
+        assert st.edep > 0.0
+        mean[prec] = st.edep / n
+    # a history deposits between 0 and its energy: sd <= max(e0, e1) / 2
+    se = 0.5 * max(e0, e1) * np.sqrt(1.0 / 20000 + 1.0 / 200000)
+    assert abs(mean[dpm.FP32_EVENT] - mean[dpm.FP64_PLAIN]) < 5.0 * se, (mean, se)
