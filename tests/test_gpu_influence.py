@@ -156,3 +156,25 @@ def test_torch_operators(setup, tables_wlb, dpm):
         assert torch.equal(ops.csr_rmatvec(h, g), A.rmatvec(g))
     finally:
         ops.csr_free(h)
+
+
+def test_largest_beamlet_grid(tables_wlb, dpm):
+    """65535 beamlets (255 x 257, the largest grid) on a small phantom: the
+    tagged run's columns still sum to its dose, the matrix has one column
+    per beamlet, products match the CPU; a 65536-beamlet grid is refused"""
+    import torch
+    ph = dpm.Phantom.voxels(tables_wlb, np.zeros((8, 8, 8), dtype=np.uint8), 2.0)
+    src = dpm.Source(particle=0, e0=6.0, e1=6.0, shape=2, nbx=255, nby=257, fx=0.06, fy=0.06)
+    res = dpm.run(tables_wlb, [dpm.Job(ph, src, 4 * 65535, 5)], batches=4, tag_beamlets=True)
+    A = res.influence(0)
+    S = A.to_scipy().astype(np.float64)
+    dose = res.tally(0)[0].reshape(-1)
+    assert (A.rows, A.cols) == (512, 65535) and S.shape == (512, 65535) and S.nnz > 0
+    np.testing.assert_allclose(np.asarray(S.sum(axis=1)).ravel(), dose, rtol=2e-6, atol=1e-6 * dose.max())
+    w = np.random.default_rng(1).random(S.shape[1])
+    y = A.matvec(torch.tensor(w, device="cuda")).cpu().numpy()
+    np.testing.assert_allclose(y, S @ w, rtol=1e-12, atol=1e-12 * np.abs(S @ w).max())
+    big = dpm.Source(particle=0, e0=6.0, e1=6.0, shape=2, nbx=256, nby=256, fx=0.06, fy=0.06)
+    with pytest.raises(dpm.DpmxError) as e:
+        dpm.run(tables_wlb, [dpm.Job(ph, big, 1000, 5)], batches=2, tag_beamlets=True)
+    assert e.value.code == dpm.ERR_ARG
