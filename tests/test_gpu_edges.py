@@ -8,7 +8,8 @@
 * phantoms at the largest dimensions (2047 x 2047 x 1023 voxels: the packed
   voxel index), beams into their last column and through their last planes;
   voxels of 0.05 and 20 mm; history indices up to 2^32 - 1; sources at the
-  ends of the data set's energy range and every spectrum form;
+  ends of the data set's energy range and every spectrum form; 65536
+  statistical batches;
 * the full-size precision workload (128x128x256 x 2 mm, 1e7 histories):
   every history conserves energy, nothing is lost, and the FP32 dose agrees
   with the FP64 plain form within statistics.
@@ -257,3 +258,27 @@ def test_source_energy_extremes(tables_wlb, dpm, particle, spectrum, e0, e1):
     # a history deposits between 0 and its energy: sd <= max(e0, e1) / 2
     se = 0.5 * max(e0, e1) * np.sqrt(1.0 / 20000 + 1.0 / 200000)
     assert abs(mean[dpm.FP32_EVENT] - mean[dpm.FP64_PLAIN]) < 5.0 * se, (mean, se)
+
+
+def test_largest_batch_count(tables_wlb, dpm):
+    """65536 statistical batches (the most a run takes; 65537 is refused) on
+    a small phantom, two histories per batch: both forms run them, the dose
+    is the sum of the batch tallies (dose^2 >= dose^2 / batches bin by bin),
+    and the FP32 dose equals the same job run in 4 batches up to FP64
+    summation order (a history's deposits do not depend on its batch)"""
+    ph = dpm.Phantom.voxels(tables_wlb, np.zeros((8, 8, 8), dtype=np.uint8), 2.0)
+    src = dpm.Source(particle=-1, e0=5.0, e1=5.0, shape=1, fx=8.0, fy=8.0)
+    B = 65536
+    with pytest.raises(dpm.DpmxError) as e:
+        dpm.run(tables_wlb, [dpm.Job(ph, src, 1000, 4)], batches=B + 1)
+    assert e.value.code == dpm.ERR_ARG
+    for prec in (dpm.FP64_PLAIN, dpm.FP32_EVENT):
+        r = dpm.run(tables_wlb, [dpm.Job(ph, src, 2 * B, 4)], precision=prec, batches=B)
+        st = r.stats(0)
+        assert st.histories == 2 * B and st.lost == 0 and st.residual_violations == 0
+        assert abs(st.edep + st.escaped - st.primary_energy) <= 1e-6 * st.primary_energy
+        d, q, _ = r.tally(0)
+        assert d.sum() > 0.0
+        assert np.all(q >= d * d / B * (1.0 - 1e-9))
+        few = dpm.run(tables_wlb, [dpm.Job(ph, src, 2 * B, 4)], precision=prec, batches=4).tally(0)[0]
+        np.testing.assert_allclose(d, few, rtol=1e-9, atol=1e-12 * few.max())
