@@ -125,3 +125,23 @@ def test_fp64_batched_matches_oracle_voxel(tables_wlb, oracle_wlb, dpm):
     # the run through dpmx_run gives the same dose as the per-history hook
     res = dpm.run(tables_wlb, [dpm.Job(ph, src, n, 77)], precision=dpm.FP64_PLAIN, batches=1)
     np.testing.assert_allclose(res.tally(0)[0].reshape(-1), g, rtol=1e-9, atol=1e-12 * g.max())
+
+
+def test_largest_job_count(tables_wlb, dpm):
+    """256 jobs in one run (the job field of a particle's sub-job has 8 bits;
+    257 are refused): every job is complete, and jobs at both ends and in
+    the middle equal the same job run alone"""
+    ph = dpm.Phantom.voxels(tables_wlb, np.zeros((8, 8, 8), dtype=np.uint8), 2.0)
+    jobs = [dpm.Job(ph, dpm.Source(particle=-1 if j % 2 else 0, e0=2.0 + (j % 7), e1=2.0 + (j % 7), shape=1,
+                                   fx=8.0, fy=8.0), 300, 1000 + j) for j in range(256)]
+    with pytest.raises(dpm.DpmxError) as e:
+        dpm.run(tables_wlb, jobs + [jobs[0]], batches=2)
+    assert e.value.code == dpm.ERR_ARG
+    r = dpm.run(tables_wlb, jobs, batches=2)
+    for j in range(256):
+        st = r.stats(j)
+        assert st.histories == 300 and st.lost == 0 and st.residual_violations == 0
+        assert abs(st.edep + st.escaped - st.primary_energy) <= 1e-6 * st.primary_energy
+    for j in (0, 15, 16, 128, 255):
+        alone = dpm.run(tables_wlb, [jobs[j]], batches=2).tally(0)[0]
+        np.testing.assert_allclose(r.tally(j)[0], alone, rtol=1e-10, atol=1e-12 * max(1e-30, alone.max()))
