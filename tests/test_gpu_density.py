@@ -94,3 +94,30 @@ def test_density_validation(tables_wlb, dpm):
     bad = np.zeros(m.shape, dtype=np.float32)
     with pytest.raises(dpm.DpmxError):
         dpm.Phantom.voxels(tables_wlb, m, 2.0, density=bad)
+
+
+@pytest.mark.parametrize("particle,e", [(0, 6.0), (-1, 10.0)])
+def test_density_extremes(tables_wlb, dpm, particle, e):
+    """water layers at 0.001 and 10 g/cm3 (a Woodcock majorant scaled by 10,
+    electron steps hundreds of voxels long in the thin layer): the FP32 form
+    agrees with the FP64 form voxel by voxel, and both conserve energy"""
+    dc = importlib.import_module("dpm-g4cpp_gb300.dosecheck")
+    m = np.zeros((48, 12, 12), dtype=np.uint8)
+    rho = np.ones(m.shape, dtype=np.float32)
+    rho[6:18] = 0.001
+    rho[30:36] = 10.0
+    ph = dpm.Phantom.voxels(tables_wlb, m, 2.0, density=rho)
+    src = dpm.Source(particle=particle, e0=e, e1=e, shape=1, fx=6.0, fy=6.0)
+    est = {}
+    for prec, n in ((dpm.FP64_PLAIN, 40000), (dpm.FP32_EVENT, 400000)):
+        r = dpm.run(tables_wlb, [dpm.Job(ph, src, n, 31)], precision=prec, batches=10)
+        st = r.stats(0)
+        assert st.lost == 0 and st.residual_violations == 0
+        assert abs(st.edep + st.escaped - st.primary_energy) <= 1e-6 * st.primary_energy
+        d, q, _ = r.tally(0)
+        est[prec] = dc.batch_estimate(d, q, 10, n)
+    c = dc.compare(est[dpm.FP32_EVENT][0], est[dpm.FP32_EVENT][1], 10,
+                   est[dpm.FP64_PLAIN][0], est[dpm.FP64_PLAIN][1], 10)
+    assert c["voxels"] >= 20
+    assert c["within_2sigma"] > 0.88, c
+    assert abs(c["mean_signed_pct"]) < 1.0, c
