@@ -145,3 +145,30 @@ def test_largest_job_count(tables_wlb, dpm):
     for j in (0, 15, 16, 128, 255):
         alone = dpm.run(tables_wlb, [jobs[j]], batches=2).tally(0)[0]
         np.testing.assert_allclose(r.tally(j)[0], alone, rtol=1e-10, atol=1e-12 * max(1e-30, alone.max()))
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_concurrent_runs_from_threads(tables_wlb, dpm, precision):
+    """runs made at once from four host threads (each on its own stream, with
+    its own executable graph; the scratch pool lends a block to one run at a
+    time) give the doses of the same runs made one after another"""
+    from concurrent.futures import ThreadPoolExecutor
+    m = np.zeros((32, 16, 16), dtype=np.uint8)
+    m[10:14] = 2
+    ph = dpm.Phantom.voxels(tables_wlb, m, 2.0)
+    n = 4000 if precision == dpm.FP64_PLAIN else 200000
+    jobs = [dpm.Job(ph, dpm.Source(particle=k % 2 - 1, e0=4.0 + k, e1=4.0 + k, shape=1, fx=12.0, fy=12.0), n, 70 + k)
+            for k in range(8)]
+
+    def one(job):
+        r = dpm.run(tables_wlb, [job], precision=precision, batches=4)
+        d = r.tally(0)[0]
+        r.close()
+        return d
+
+    seq = [one(j) for j in jobs]
+    with ThreadPoolExecutor(4) as ex:
+        par = list(ex.map(one, jobs))
+    for a, b in zip(seq, par):
+        assert a.sum() > 0.0
+        np.testing.assert_allclose(b, a, rtol=1e-10, atol=1e-12 * a.max())
