@@ -61,3 +61,25 @@ def test_depth_profile_voxels(tables_wlb, dpm, tmp_path):
     assert len(h) == m.shape[0]
     np.testing.assert_allclose(h[:, 2], d.sum(axis=(1, 2)) / (n * 0.2 * rho), rtol=1e-4, atol=1e-12)
     assert not h[:, 3].any()
+
+
+def test_result_outlives_its_phantom(tables_wlb, dpm, tmp_path):
+    """a result keeps the material ids its dose outputs need: written after
+    its phantom is freed and the device blocks have served another phantom
+    and run, it gives the file written before"""
+    m = np.zeros((20, 10, 10), dtype=np.uint8)
+    m[5:10] = 2
+    ph = dpm.Phantom.voxels(tables_wlb, m, 2.0)
+    r = dpm.run(tables_wlb, [dpm.Job(ph, dpm.Source(particle=-1, e0=8.0, e1=8.0, shape=1, fx=6.0, fy=6.0), 20000, 4)],
+                batches=4)
+    r.write(tmp_path / "before.raw", fmt=dpm.DOSE_RAW)
+    ph.close()
+    other = dpm.Phantom.voxels(tables_wlb, np.ones((20, 10, 10), dtype=np.uint8), 2.0)
+    dpm.run(tables_wlb, [dpm.Job(other, dpm.Source(particle=0, e0=3.0, e1=3.0), 5000, 5)], batches=2).close()
+    other.close()
+    r.write(tmp_path / "after.raw", fmt=dpm.DOSE_RAW)
+    a, ra, ha = dpm.read_dose_raw(tmp_path / "before.raw")
+    b, rb, hb = dpm.read_dose_raw(tmp_path / "after.raw")
+    assert a.sum() > 0.0 and ha == hb
+    np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(ra, rb)
