@@ -27,7 +27,8 @@ def batch_sigma(dose, dose2, nb):
     return np.sqrt(var / max(nb - 1, 1)) * nb
 
 
-@pytest.mark.parametrize("ise,e,geom", [(True, 15.0, 3), (False, 15.0, 3), (True, 6.0, 0)])
+@pytest.mark.parametrize("ise,e,geom", [(True, 15.0, 3), (False, 15.0, 3), (True, 6.0, 0), (True, 12.0, 1),
+                                        (False, 10.0, 2)])
 def test_fp64_histories_match_oracle(tables_c3, oracle_c3, dpm, ise, e, geom):
     n = 400
     he, _ = dpm.simulate_histories(tables_c3, n, e, ise, 1.0, geom, seed=2468)
