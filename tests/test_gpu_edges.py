@@ -9,7 +9,7 @@
   voxel index), beams into their last column and through their last planes;
   voxels of 0.05 and 20 mm; history indices up to 2^32 - 1; sources at the
   ends of the data set's energy range and every spectrum form; 65536
-  statistical batches;
+  statistical batches; a pencil beam along the faces between voxel columns;
 * the full-size precision workload (128x128x256 x 2 mm, 1e7 histories):
   every history conserves energy, nothing is lost, and the FP32 dose agrees
   with the FP64 plain form within statistics.
@@ -282,3 +282,29 @@ def test_largest_batch_count(tables_wlb, dpm):
         assert np.all(q >= d * d / B * (1.0 - 1e-9))
         few = dpm.run(tables_wlb, [dpm.Job(ph, src, 2 * B, 4)], precision=prec, batches=4).tally(0)[0]
         np.testing.assert_allclose(d, few, rtol=1e-9, atol=1e-12 * few.max())
+
+
+@pytest.mark.parametrize("particle,e", [(-1, 6.0), (0, 6.0)])
+def test_pencil_beam_on_a_voxel_face(tables_wlb, dpm, particle, e):
+    """a pencil beam at x = y = 0 of a phantom with an even number of voxels
+    runs along the faces between four voxel columns: both forms put the
+    particle in the same column (the one above the face) and agree voxel by
+    voxel"""
+    from importlib import import_module
+    dc = import_module("dpm-g4cpp_gb300.dosecheck")
+    ph = dpm.Phantom.voxels(tables_wlb, np.zeros((30, 16, 16), dtype=np.uint8), 2.0)
+    src = dpm.Source(particle=particle, e0=e, e1=e)
+    est, cols = {}, {}
+    for prec, n in ((dpm.FP64_PLAIN, 40000), (dpm.FP32_EVENT, 400000)):
+        r = dpm.run(tables_wlb, [dpm.Job(ph, src, n, 12)], precision=prec, batches=10)
+        st = r.stats(0)
+        assert st.lost == 0 and st.residual_violations == 0
+        d, q, _ = r.tally(0)
+        est[prec] = dc.batch_estimate(d, q, 10, n)
+        first = d.reshape(30, 16, 16)[0]
+        cols[prec] = np.unravel_index(first.argmax(), first.shape)
+    assert cols[dpm.FP32_EVENT] == cols[dpm.FP64_PLAIN], cols
+    c = dc.compare(est[dpm.FP32_EVENT][0], est[dpm.FP32_EVENT][1], 10,
+                   est[dpm.FP64_PLAIN][0], est[dpm.FP64_PLAIN][1], 10)
+    assert c["within_2sigma"] > 0.85, c
+    assert abs(c["mean_signed_pct"]) < max(0.5, 3.0 * c["mean_rel_sigma_pct"]), c
