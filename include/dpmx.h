@@ -95,7 +95,7 @@ typedef struct {
   int shape;          /* 0 pencil at (cx,cy); 1 rectangle fx*fy centred at (cx,cy);
                          2 grid of nbx*nby beamlets fx*fy each, centred at (cx,cy) */
   double cx, cy, fx, fy;  /* mm */
-  int nbx, nby;
+  int nbx, nby;       /* shape 2: nbx * nby <= 65535 */
 } dpmx_source;
 
 typedef struct {
@@ -112,7 +112,7 @@ typedef struct {
 
 typedef struct {
   int precision;             /* DPMX_FP64_PLAIN or DPMX_FP32_EVENT */
-  int batches;               /* statistical batches for dose^2 (default 10) */
+  int batches;               /* statistical batches for dose^2 (default 10, at most 65536) */
   int block_size;            /* threads per block (0: default / tuned) */
   int blocks_per_sm;         /* resident blocks per SM (0: default / tuned) */
   long long chunk_histories; /* histories per transport chunk (0: as few equal chunks of at most
@@ -149,6 +149,10 @@ typedef struct {
   long long histories;
 } dpmx_job_stats;
 
+/* runs njobs jobs (1..256) as one run; DPMX_ERR_ARG beyond the limits: at
+ * most 65536 batches, history indices in [0, 2^32), source energies strictly
+ * inside the data set's range. Safe to call from several host threads at once
+ * (each run has its own stream unless opt->stream is given). */
 int dpmx_run(const dpmx_tables* t, const dpmx_job* jobs, int njobs, const dpmx_run_options* opt,
              dpmx_result** out);
 /* host copies of a job's tallies; any output pointer may be NULL.
