@@ -262,11 +262,11 @@ def main():
 
     import numpy as np
     import torch
+    torch.cuda.set_device(local)   # before the process group: each rank's communicator on its own GPU
     dist = None
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-    torch.cuda.set_device(local)
     dpm = importlib.import_module("dpm-g4cpp_gb300")
     wl = importlib.import_module("dpm-g4cpp_gb300.workloads")
     tables = dpm.Tables(DATA)
